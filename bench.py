@@ -1,0 +1,327 @@
+"""Benchmark: MD steps/s and ns/day of the hybrid particle-field rRESPA step.
+
+Workload (default): the 162k-bead lipid membrane -- 6000 twelve-bead lipids +
+90k W, box 27 nm, mesh 64^3, sigma 0.5, kappa 0.05, chi as in the membrane
+recipe, bonds + angles, time_step 0.03 ps, respa_inner 10.  One step = one
+outer rRESPA step (10 inner bonded steps + one field evaluation), run from a
+CUDA graph.  Inputs (the system state) are resident in HBM; the working set
+(~70 MB) fits in L2, so L2 is flushed (256 MB write) between timed steps,
+outside the per-step CUDA-event windows.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl hpf|reference]
+
+--impl reference times the CPU restatement of the same step (oracle/, the
+reference's own CPU code cannot be built here) on the host cores.
+N > 1 (torchrun): independent replicas, one per GPU; value = sum over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MD steps/s & ns/day per GB300 vs plain GPU form at <=1e-5 force rel-RMS vs FP64"
+WORKLOAD = "membrane162k"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _config_block(cfg, n, extra=None):
+    d = {"workload": "lipid membrane 162k beads (6000 x 12-bead lipids + 90k W), "
+                     "box 27 nm, mesh 64^3, 5 types",
+         "n_beads": int(n), "mesh": list(cfg.mesh()), "respa_inner": int(cfg.respa_inner),
+         "time_step_ps": float(cfg.time_step), "sigma": cfg.sigma, "kappa": cfg.kappa,
+         "l2": "flushed between timed steps (256 MB write, outside the timed windows)",
+         "parallelism": "replicas only"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _time_kernel(fn, reps, flush, torch):
+    """Average device time of fn() (CUDA events on the current stream), with
+    an L2 flush before each launch outside the timed window."""
+    st = torch.cuda.current_stream()
+    tot = 0.0
+    for _ in range(reps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        fn()
+        b.record(st)
+        b.synchronize()
+        tot += a.elapsed_time(b)
+    return tot / reps
+
+
+def cpu_baseline(sys_, steps=2, workers=1):
+    """The oracle (FP64 numpy field + C bonded) on the host: a bounded sample
+    of `steps` outer steps of the same workload."""
+    from oracle import field as of
+    from oracle import hamiltonian as oh
+    from oracle import md as omd
+    of.FFT_WORKERS = workers
+    cfg = sys_["config"]
+    T = cfg.n_types
+    names = cfg.unique_names
+    chi = np.zeros((T, T))
+    for c in cfg.chi:
+        i, j = names.index(c.atom_1), names.index(c.atom_2)
+        chi[i, j] = chi[j, i] = c.interaction_energy
+    fun = oh.quadratic_from_params("DefaultWithChi", T, cfg.kappa, cfg.rho0, cfg.a, chi)
+    r = sys_["positions"].copy()
+    v = sys_["velocities"].copy()
+    ff = omd.field_forces(r, sys_["types"], cfg, fun)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r, v, ff = omd.respa_step(r, v, ff, sys_["types"], sys_["topology"], cfg, fun)
+    dt = time.perf_counter() - t0
+    return steps / dt, dt
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    from hymd_gb300 import systems
+    s = systems.BUILDERS[WORKLOAD]()
+    cfg = s["config"]
+    workers = os.cpu_count() or 1
+    cpu_baseline(s, steps=1, workers=workers)  # warm-up (one step)
+    # bounded sample: at most K steps and at most ~90 s of host work
+    t0 = time.perf_counter()
+    done = 0
+    secs = 0.0
+    while done < max(1, args.steps) and time.perf_counter() - t0 < 90.0:
+        _, dt = cpu_baseline(s, steps=1, workers=workers)
+        secs += dt
+        done += 1
+    sps = done / secs
+    ns_day = sps * cfg.respa_inner * cfg.time_step * 86400 / 1000.0
+    line = {"impl": "reference", "metric": METRIC, "value": sps, "unit": "steps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 field / f32 bonded", "data": "synthetic",
+            "ns_per_day": ns_day,
+            "config": _config_block(cfg, len(s["positions"])),
+            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": workers, "kind": "port",
+                             "sample": f"{done} outer steps of the full workload "
+                                       f"({secs:.1f} s); FFTs threaded over {workers} cores"},
+            "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from hymd_gb300 import _lib, systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+
+    s = systems.BUILDERS[WORKLOAD](seed=2 + rank)
+    cfg = s["config"]
+    n = len(s["positions"])
+    ham = get_hamiltonian(cfg)
+    md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"],
+                 device=dev)
+    md.prime()
+    md.capture()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    for _ in range(max(3, args.warmup)):
+        md.run(1)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    st = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for a, b in evs:
+            flush.zero_()
+            a.record(st)
+            md.graph.replay()
+            b.record(st)
+        torch.cuda.synchronize()
+    barrier()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    sps = 1000.0 / ms_step
+    md.check_errors()
+
+    # ---- end to end through the public API with host buffers -------------
+    r_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    v_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    r_out = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    r_h.copy_(md.r.cpu())
+    v_h.copy_(md.v.cpu())
+    e2e_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+    for a, b in e2e_evs:
+        flush.zero_()
+        a.record(st)
+        md.r.copy_(r_h, non_blocking=True)
+        md.v.copy_(v_h, non_blocking=True)
+        md.run(1)
+        r_out.copy_(md.r, non_blocking=True)
+        b.record(st)
+    torch.cuda.synchronize()
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_evs) / args.steps
+
+    # ---- roofline of the dominant field kernel (paint) --------------------
+    peak, peak_kind = _peaks()
+    T = cfg.n_types
+    M = int(np.prod(cfg.mesh()))
+    phi = md.pm.real_field(T)
+    masses = _lib.dvec(cfg.m)
+
+    def paint():
+        _lib.call("hpf_paint", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), n, masses,
+                  _lib.ptr(phi), _lib.stream_ptr())
+
+    paint_ms = _time_kernel(paint, 20, flush, torch)
+    paint_bytes = 16 * n + 4 * T * M
+    achieved = paint_bytes / (paint_ms * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "paint_traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get("bytes_per_launch")
+
+    ns_day = sps * cfg.respa_inner * cfg.time_step * 86400 / 1000.0
+    # CPU baseline (rank 0, N=1 only): bounded oracle sample
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        c_sps, c_secs = cpu_baseline(s, steps=2, workers=1)
+        cpu = {"value": c_sps, "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": f"2 outer steps of the full workload on the oracle "
+                         f"(FP64 numpy field + C bonded), {c_secs:.1f} s"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": sps * ws, "unit": "steps/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 (f64 energies/virial)", "data": "synthetic",
+                "ns_per_day": ns_day * ws,
+                "config": _config_block(cfg, n),
+                "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "steps/s",
+                        "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 12 * n},
+                "gpu_launches": md.launches_per_step * args.steps,
+                "roofline": {"kernel": "paint (k_paint + k_paint_finalize)", "bound": "hbm",
+                             "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic,
+                             "peak_kind": peak_kind, "ms_per_launch": paint_ms,
+                             "algorithmic_bytes": paint_bytes},
+                "clocks": clk.summary(),
+                "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="hpf", choices=["hpf", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

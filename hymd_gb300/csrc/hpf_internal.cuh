@@ -1,0 +1,192 @@
+// Internal device helpers shared by the hpf_gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+#include "../../include/hpf_gb300.h"
+
+#define HPF_MAX_TYPES 16
+
+// Box state kept in device memory so that graphs replayed after a device-side
+// barostat rescale see the new box.  The first five doubles are part of the
+// C ABI (hpf_ctx_box_state): L[3], V, dV.
+struct BoxState {
+    double L[3];
+    double V;
+    double dV;
+    float Lf[3];      // float box, used by the position wrap
+    float ih_hi[3];   // n_d / L_d split into two floats (hi + lo)
+    float ih_lo[3];
+    float kf[3];      // 2 pi / L_d
+    float inv_dV;
+    int n[3];
+    int pad;
+};
+
+// Quadratic functional w = 1/2 phi.Q.phi + b.phi + c (per context).
+struct Functional {
+    float Q[HPF_MAX_TYPES * HPF_MAX_TYPES];
+    float b[HPF_MAX_TYPES];
+    double Qd[HPF_MAX_TYPES * HPF_MAX_TYPES];
+    double bd[HPF_MAX_TYPES];
+    double c;
+    float sigma2_half;   // 0.5 * sigma^2
+    float pad;
+};
+
+struct hpf_ctx {
+    int n0, n1, n2, T;
+    int64_t M, Mc;
+    int device;
+    BoxState* d_box;          // device
+    BoxState h_box;           // host mirror (last value set from the host)
+    Functional* d_fun;        // device
+    Functional h_fun;
+    unsigned long long* d_acc;  // paint accumulators int64[T+1][M] (the +1 is for charges)
+    float* d_grid;            // real scratch float[3T][M] (densities / force mesh)
+    float2* d_spec;           // spectral scratch float2[3T][Mc]
+    float2* d_spec_phi;       // raw density spectra float2[T][Mc]
+    double* d_ws;             // reduction workspace (HPF_OUT_DOUBLES)
+    int* d_err;               // first device error code
+    void* fft_work;
+    size_t fft_work_size;
+    cufftHandle plan_r2c[HPF_MAX_TYPES + 1];   // batch b at index b (created lazily)
+    cufftHandle plan_c2r[3 * HPF_MAX_TYPES + 2];
+    bool has_r2c[HPF_MAX_TYPES + 1];
+    bool has_c2r[3 * HPF_MAX_TYPES + 2];
+};
+
+// Layout of a reduction workspace (see HPF_OUT_DOUBLES in the C ABI header).
+__host__ __device__ inline double* ws_partials(double* ws) { return ws + 8; }
+__host__ __device__ inline unsigned int* ws_ticket(double* ws) {
+    return reinterpret_cast<unsigned int*>(ws + 8 + 8 * HPF_REDUCE_BLOCKS);
+}
+
+static inline int reduce_grid(int64_t work, int threads) {
+    int64_t b = (work + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > HPF_REDUCE_BLOCKS) b = HPF_REDUCE_BLOCKS;
+    return (int)b;
+}
+
+// Derived box quantities, shared by the host setter and the device barostat.
+__host__ __device__ inline void fill_box_state(BoxState& s, double L0, double L1, double L2,
+                                               const int n[3]) {
+    const double Ls[3] = {L0, L1, L2};
+    s.V = L0 * L1 * L2;
+    s.dV = s.V / ((double)n[0] * (double)n[1] * (double)n[2]);
+    for (int d = 0; d < 3; ++d) {
+        s.L[d] = Ls[d];
+        s.n[d] = n[d];
+        s.Lf[d] = (float)Ls[d];
+        double ih = (double)n[d] / Ls[d];
+        s.ih_hi[d] = (float)ih;
+        s.ih_lo[d] = (float)(ih - (double)s.ih_hi[d]);
+        s.kf[d] = (float)(2.0 * 3.14159265358979323846 / Ls[d]);
+    }
+    s.inv_dV = (float)(1.0 / s.dV);
+}
+
+#define HPF_CUDA_TRY(x)                                   \
+    do {                                                  \
+        cudaError_t e_ = (x);                             \
+        if (e_ != cudaSuccess) return HPF_ERR_CUDA;       \
+    } while (0)
+
+#define HPF_LAUNCH_CHECK()                                \
+    do {                                                  \
+        cudaError_t e_ = cudaGetLastError();              \
+        if (e_ != cudaSuccess) return HPF_ERR_CUDA;       \
+    } while (0)
+
+static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+__device__ __forceinline__ void hpf_flag(int* err, int code) {
+    if (err) atomicCAS(err, 0, code);
+}
+
+// Grid coordinate s = x * n/L split into a node index and a fraction in
+// [0,1), using only FP32 arithmetic.  n/L is held as hi+lo floats and the
+// product's rounding error is recovered with an FMA, so the fraction is
+// accurate to ~1e-7 absolute (a plain float product would lose up to
+// n * 6e-8 near the far edge of the box).
+__device__ __forceinline__ void grid_coord(float x, float ih_hi, float ih_lo, int n, int& i,
+                                           float& frac) {
+    float s = x * ih_hi;
+    float e = fmaf(x, ih_hi, -s);          // exact residual of the product
+    float fl = floorf(s);
+    float f = (s - fl) + fmaf(x, ih_lo, e);
+    if (f >= 1.0f) { f -= 1.0f; fl += 1.0f; }
+    if (f < 0.0f) { f += 1.0f; fl -= 1.0f; }
+    int ii = (int)fl;
+    ii %= n;
+    if (ii < 0) ii += n;
+    i = ii;
+    frac = f;
+}
+
+// Warp + block reduction of K doubles; thread 0 returns the block totals.
+template <int K>
+__device__ __forceinline__ void block_reduce(double (&v)[K], double* smem /* K*32 */) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) smem[k * 32 + warp] = v[k];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double x = lane < nw ? smem[k * 32 + lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            v[k] = x;
+        }
+    }
+}
+
+// Deterministic grid-wide sum: each block stores its K partials; the last
+// block to finish (ticket) adds them -- thread j takes blocks j, j+B, ...,
+// then a fixed tree -- and writes out[k] (overwrite or accumulate).  The
+// order never depends on scheduling, and the ticket resets itself, so the
+// pattern is graph-replay safe.
+template <int K>
+__device__ __forceinline__ void grid_reduce_store(double (&v)[K], double* partials,
+                                                  unsigned int* ticket, double* out,
+                                                  bool accumulate) {
+    __shared__ double red[K * 32];
+    __shared__ bool is_last;
+    block_reduce<K>(v, red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) partials[(size_t)blockIdx.x * K + k] = v[k];
+        __threadfence();
+        unsigned int t = atomicAdd(ticket, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    for (unsigned int bI = threadIdx.x; bI < gridDim.x; bI += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] += ((volatile double*)partials)[(size_t)bI * K + k];
+    }
+    __syncthreads();
+    block_reduce<K>(acc, red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = (accumulate ? out[k] : 0.0) + acc[k];
+        *ticket = 0u;
+    }
+}

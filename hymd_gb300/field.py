@@ -1,0 +1,381 @@
+"""Particle-field forces and energies on GB300 -- drop-in for hymd/field.py.
+
+Same function names and positional signatures as the reference
+(hymd/field.py:10-703); pmesh RealField / ComplexField objects become CUDA
+torch tensors and the pmesh ParticleMesh becomes a `ParticleMesh` context
+that owns the cuFFT plans.  Every numerical step runs in libhpf_gb300.so.
+
+Grid layout: the lists returned by `initialize_pm` are views into stacked,
+contiguous tensors -- phi is phi_all[t] of phi_all (T, n0, n1, n2),
+force_on_grid[t][d] is force_all[t, d] of (T, 3, n0, n1, n2), complex fields
+are complex64 (n0, n1, n2//2 + 1).  The stacked layout lets one kernel launch
+serve all types; functions here accept only such stacks (ValueError otherwise).
+
+`layouts` / `layout_q` arguments (pmesh domain layouts) are accepted and
+ignored: one GPU holds the whole system.
+"""
+import numpy as np
+import torch
+
+from . import _lib
+from .hamiltonian import quadratic_form
+
+_REGISTRY = {}
+
+
+class ParticleMesh:
+    """Mesh context: geometry, box state, functional and cuFFT plans on the
+    current CUDA device (replaces pmesh.pm.ParticleMesh)."""
+
+    def __init__(self, mesh_size, box_size, n_types, device=None):
+        n = np.asarray(mesh_size, dtype=np.int64).reshape(-1)
+        if n.size == 1:
+            n = np.repeat(n, 3)
+        self.Nmesh = tuple(int(x) for x in n)
+        self.n_types = int(n_types)
+        self.device = torch.device(device) if device is not None else torch.device(
+            "cuda", torch.cuda.current_device())
+        self.BoxSize = np.asarray(box_size, dtype=np.float64).reshape(3).copy()
+        self.M = int(np.prod(self.Nmesh))
+        self.Mc = self.Nmesh[0] * self.Nmesh[1] * (self.Nmesh[2] // 2 + 1)
+        handle = _lib.P()
+        with torch.cuda.device(self.device):
+            _lib.call("hpf_ctx_create", _lib.ctypes.byref(handle), self.Nmesh[0], self.Nmesh[1],
+                      self.Nmesh[2], self.n_types, _lib.dvec(self.BoxSize))
+        self._h = handle
+        st = _lib.P()
+        _lib.call("hpf_ctx_box_state", self._h, _lib.ctypes.byref(st))
+        self.box_state_ptr = st.value
+        self._functional = None
+        self.ws = _lib.new_workspace(self.device)
+        self.spec_raw = self.complex_field(self.n_types)
+        self.spec_force = self.complex_field(3 * self.n_types)
+
+    # -- allocation helpers -------------------------------------------------
+    def real_field(self, *lead):
+        return torch.zeros(*lead, *self.Nmesh, dtype=torch.float32, device=self.device)
+
+    def complex_field(self, *lead):
+        return torch.zeros(*lead, self.Nmesh[0], self.Nmesh[1], self.Nmesh[2] // 2 + 1,
+                           dtype=torch.complex64, device=self.device)
+
+    def create(self, kind, value=0.0):
+        """pmesh-style single field."""
+        f = self.real_field() if kind == "real" else self.complex_field()
+        if value:
+            f.fill_(value)
+        return f
+
+    def decompose(self, positions, smoothing=None):
+        """Domain layouts are not needed on one GPU."""
+        return None
+
+    # -- state ----------------------------------------------------------------
+    def set_box(self, box_size):
+        self.BoxSize = np.asarray(box_size, dtype=np.float64).reshape(3).copy()
+        _lib.call("hpf_ctx_set_box", self._h, _lib.dvec(self.BoxSize), _lib.stream_ptr())
+
+    def box_tensor(self):
+        """(3,) float64 device tensor aliasing the context box state (L)."""
+        return _box_view(self)
+
+    def set_functional(self, hamiltonian):
+        Q, b, c, sigma = quadratic_form(hamiltonian, self.n_types)
+        key = (Q.tobytes(), b.tobytes(), c, sigma)
+        if key != self._functional:
+            T = self.n_types
+            if Q.shape != (T, T):
+                raise ValueError(f"functional has {Q.shape[0]} types, mesh context has {T}")
+            _lib.call("hpf_ctx_set_functional", self._h, _lib.dvec(Q.reshape(-1)), _lib.dvec(b),
+                      float(c), float(sigma))
+            self._functional = key
+        return Q, b, c, sigma
+
+    def check_errors(self):
+        code = _lib.ctypes.c_int(0)
+        _lib.call("hpf_get_error", self._h, _lib.stream_ptr(), _lib.ctypes.byref(code))
+        if code.value:
+            raise _lib.HPFError("device check", code.value)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().hpf_ctx_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+def _box_view(pm):
+    """A (3,) float64 tensor over the device box state (no copy)."""
+    if getattr(pm, "_box_t", None) is None:
+        # wrap the raw device pointer: the first 3 doubles of the box state
+        holder = _DevicePtrArray(pm.box_state_ptr, 3, pm.device)
+        pm._box_t = holder.tensor
+        pm._box_holder = holder
+    return pm._box_t
+
+
+class _DevicePtrArray:
+    """Expose a library-owned device array as a torch tensor via DLPack-free
+    __cuda_array_interface__ (lifetime tied to the owning context)."""
+
+    def __init__(self, ptr, n, device):
+        self.__cuda_array_interface__ = {
+            "shape": (n,), "typestr": "<f8", "data": (int(ptr), False), "version": 2,
+            "strides": None,
+        }
+        with torch.cuda.device(device):
+            self.tensor = torch.as_tensor(self, device=device)
+
+
+def _stack_base(lst, lead_shape, dtype, name):
+    """Return the stacked tensor that the list elements are views of."""
+    flat = []
+
+    def walk(x):
+        if isinstance(x, (list, tuple)):
+            for y in x:
+                walk(y)
+        else:
+            flat.append(x)
+
+    walk(lst)
+    first = flat[0]
+    _lib.require_cuda(first, name + "[0]", dtype)
+    per = first.numel() * first.element_size()
+    for i, x in enumerate(flat):
+        if x.dtype != dtype or x.data_ptr() != first.data_ptr() + i * per or not x.is_contiguous():
+            raise ValueError(f"{name} must be views of one stacked tensor as created by "
+                             "initialize_pm")
+    base = torch.as_strided(first, (len(flat),) + tuple(first.shape),
+                            (first.numel(),) + tuple(first.stride()))
+    return base.reshape(tuple(lead_shape) + tuple(first.shape))
+
+
+def initialize_pm(pmesh, config, comm=None):
+    """hymd/field.py:10-149.  `pmesh` is ignored (may be None).
+
+    Returns (pm, field_list, elec_common_list, coulomb_list) with the same
+    nesting as the reference; fields are CUDA tensors (views of stacks).
+    """
+    T = config.n_types
+    pm = ParticleMesh(config.mesh_size, config.box_size, T)
+    phi_all = pm.real_field(T)
+    phi_fourier_all = pm.complex_field(T)
+    force_all = pm.real_field(T, 3)
+    v_ext_fourier_all = pm.complex_field(4)
+    v_ext_all = pm.real_field(T)
+    phi_transfer_all = pm.complex_field(3)
+    phi_lap_all = pm.real_field(T, 3)
+    phi = [phi_all[t] for t in range(T)]
+    phi_fourier = [phi_fourier_all[t] for t in range(T)]
+    force_on_grid = [[force_all[t, d] for d in range(3)] for t in range(T)]
+    v_ext_fourier = [v_ext_fourier_all[i] for i in range(4)]
+    v_ext = [v_ext_all[t] for t in range(T)]
+    phi_transfer = [phi_transfer_all[i] for i in range(3)]
+    phi_laplacian = [[phi_lap_all[t, d] for d in range(3)] for t in range(T)]
+    elec_common_list = [None, None, None, None]
+    coulomb_list = []
+    if config.coulombtype in ("PIC_Spectral", "PIC_Spectral_GPE"):
+        phi_q = pm.real_field()
+        phi_q_fourier = pm.complex_field()
+        psi = pm.real_field()
+        ef_all = pm.real_field(3)
+        elec_common_list = [phi_q, phi_q_fourier, psi, [ef_all[d] for d in range(3)]]
+    if config.coulombtype == "PIC_Spectral":
+        eff_all = pm.complex_field(3)
+        coulomb_list = [[eff_all[d] for d in range(3)], pm.complex_field()]
+    elif config.coulombtype == "PIC_Spectral_GPE":
+        raise NotImplementedError("PIC_Spectral_GPE has no GPU implementation")
+    field_list = [phi, phi_fourier, force_on_grid, v_ext_fourier, v_ext, phi_transfer,
+                  phi_laplacian]
+    _REGISTRY[phi_all.data_ptr()] = pm
+    pm.fields = dict(phi=phi_all, phi_fourier=phi_fourier_all, force=force_all,
+                     v_ext=v_ext_all, phi_laplacian=phi_lap_all)
+    return pm, field_list, elec_common_list, coulomb_list
+
+
+def _pm_of(phi):
+    pm = _REGISTRY.get(phi[0].data_ptr())
+    if pm is None:
+        raise ValueError("phi was not created by hymd_gb300.field.initialize_pm")
+    return pm
+
+
+def _masses(m, T):
+    if m is None or len(m) == 0:
+        return [1.0] * T
+    return [float(x) for x in m]
+
+
+def _types32(types, n):
+    if types.dtype != torch.int32:
+        types = types.to(torch.int32)
+    return _lib.require_cuda(types.contiguous(), "types", torch.int32, (n,))
+
+
+def update_field(phi, phi_laplacian, phi_transfer, layouts, force_mesh, hamiltonian, pm,
+                 positions, types, config, v_ext, phi_fourier, v_ext_fourier, m,
+                 compute_potential=False):
+    """hymd/field.py:428-616.
+
+    On return (as in the reference): phi[t] holds the filtered density
+    phi~_t, phi_fourier[t] = H r2c(phi_t), force_mesh[t][d] = c2r(-i k_d H
+    r2c(v_ext_t(phi~))) and, with compute_potential, v_ext[t] the filtered
+    external potential.  v_ext_fourier is scratch in the reference and is not
+    written here.
+    """
+    T = pm.n_types
+    pos = _lib.require_cuda(positions, "positions", torch.float32)
+    n = pos.shape[0]
+    typ = _types32(types, n)
+    phi_all = _stack_base(phi, (T,), torch.float32, "phi")
+    phif_all = _stack_base(phi_fourier, (T,), torch.complex64, "phi_fourier")
+    force_all = _stack_base(force_mesh, (T, 3), torch.float32, "force_mesh")
+    pm.set_functional(hamiltonian)
+    st = _lib.stream_ptr()
+    masses = _lib.dvec(_masses(m, T))
+    _lib.call("hpf_paint", pm._h, _lib.ptr(pos), _lib.ptr(typ), n, masses, _lib.ptr(phi_all), st)
+    _lib.call("hpf_r2c", pm._h, _lib.ptr(phi_all), _lib.ptr(pm.spec_raw), T, st)
+    v_k = pm.complex_field(T) if compute_potential else None
+    _lib.call("hpf_kspace_force", pm._h, _lib.ptr(pm.spec_raw), _lib.ptr(pm.spec_force),
+              _lib.ptr(phif_all), _lib.ptr(v_k), None, st)
+    _lib.call("hpf_c2r", pm._h, _lib.ptr(pm.spec_force), _lib.ptr(force_all), 3 * T, st)
+    _lib.call("hpf_c2r", pm._h, _lib.ptr(phif_all), _lib.ptr(phi_all), T, st)
+    if compute_potential:
+        vext_all = _stack_base(v_ext, (T,), torch.float32, "v_ext")
+        _lib.call("hpf_c2r", pm._h, _lib.ptr(v_k), _lib.ptr(vext_all), T, st)
+    pm._last_counts = None
+
+
+def compute_field_force(layouts, r, force_mesh, force, types, n_types):
+    """hymd/field.py:152-200: force[types == t, d] = readout(force_mesh[t][d])."""
+    pos = _lib.require_cuda(r, "r", torch.float32)
+    n = pos.shape[0]
+    _lib.require_cuda(force, "force", torch.float32, (n, 3))
+    force_all = _stack_base(force_mesh, (n_types, 3), torch.float32, "force_mesh")
+    pm = _REGISTRY_FORCE.get(force_all.data_ptr())
+    if pm is None:
+        pm = _find_pm_for_force(force_all)
+    typ = _types32(types, n)
+    _lib.call("hpf_readout", pm._h, _lib.ptr(force_all), _lib.ptr(pos), _lib.ptr(typ), n,
+              _lib.ptr(force), _lib.stream_ptr())
+
+
+_REGISTRY_FORCE = {}
+
+
+def _find_pm_for_force(force_all):
+    for pm in _REGISTRY.values():
+        if pm.fields["force"].data_ptr() == force_all.data_ptr():
+            _REGISTRY_FORCE[force_all.data_ptr()] = pm
+            return pm
+    raise ValueError("force_mesh was not created by hymd_gb300.field.initialize_pm")
+
+
+def _sum(pm, x, y=None):
+    st = _lib.stream_ptr()
+    _lib.call("hpf_sum_dot", _lib.ptr(x), _lib.ptr(y), x.numel(), _lib.ptr(pm.ws), st)
+    return pm.ws[0]
+
+
+def field_energy_parts(pm, phi_all, hamiltonian):
+    """W of the filtered densities phi_all (T, n0, n1, n2), FP64.
+
+    k != 0 modes by Parseval in one k-space pass; the k = 0 part V w(mean phi)
+    from FP64 sums of the grids, so that the incompressibility term's
+    cancellation (sum phi - a) happens exactly.
+    """
+    T = pm.n_types
+    Q, b, c, sigma = pm.set_functional(hamiltonian)
+    st = _lib.stream_ptr()
+    spec = pm.complex_field(T)
+    _lib.call("hpf_r2c", pm._h, _lib.ptr(phi_all), _lib.ptr(spec), T, st)
+    spec.mul_(1.0 / pm.M)
+    sums = torch.zeros(8, dtype=torch.float64, device=pm.device)
+    _lib.call("hpf_kspace_sums", pm._h, _lib.ptr(spec), None, None, _lib.ptr(sums), st)
+    means = np.array([float(_sum(pm, phi_all[t])) / pm.M for t in range(T)])
+    V = float(np.prod(pm.BoxSize))
+    A = float(sums[0])
+    W_dc = V * (0.5 * means @ Q @ means + b @ means + c)
+    return W_dc + 0.5 * V * A, means, sums
+
+
+def compute_field_and_kinetic_energy(phi, phi_q, psi, velocity, hamiltonian, positions, types,
+                                     v_ext, config, layouts, comm=None):
+    """hymd/field.py:619-703 -> (field_energy, kinetic_energy, field_q_energy).
+
+    W = sum_g w_0(phi~) dV is evaluated from the given phi~ grids in FP64 (see
+    `field_energy_parts`); KE = m/2 sum v^2; with PIC_Spectral, W_elec =
+    sum_g (phi_q psi / 2 - E_self / V) dV.
+    """
+    pm = _pm_of(phi)
+    T = pm.n_types
+    phi_all = _stack_base(phi, (T,), torch.float32, "phi")
+    W, _, _ = field_energy_parts(pm, phi_all, hamiltonian)
+    vel = _lib.require_cuda(velocity, "velocity", torch.float32)
+    _lib.call("hpf_sum_v2", _lib.ptr(vel), vel.shape[0], _lib.ptr(pm.ws), _lib.stream_ptr())
+    ke = 0.5 * float(config.mass) * float(pm.ws[0])
+    wq = 0.0
+    if config.coulombtype == "PIC_Spectral":
+        V = float(np.prod(pm.BoxSize))
+        dV = V / pm.M
+        dot = float(_sum(pm, phi_q, psi))
+        wq = 0.5 * dot * dV - float(config.self_energy or 0.0)
+    return W, ke, wq
+
+
+def compute_self_energy_q(config, charges, comm=None):
+    """hymd/field.py:203-238: k_e/eps sqrt(1/(2 pi sigma^2)) sum q^2 (FP64)."""
+    q = _lib.require_cuda(charges, "charges", torch.float32)
+    ws = _lib.new_workspace(q.device)
+    _lib.call("hpf_sum_dot", _lib.ptr(q), _lib.ptr(q), q.numel(), _lib.ptr(ws), _lib.stream_ptr())
+    pref = config.coulomb_constant / config.dielectric_const * np.sqrt(
+        1.0 / (2.0 * np.pi * config.sigma * config.sigma))
+    return float(pref * float(ws[0]))
+
+
+def update_field_force_q(charges, phi_q, phi_q_fourier, psi, psi_fourier, elec_field_fourier,
+                         elec_field, elec_forces, layout_q, hamiltonian, pm, positions, config):
+    """hymd/field.py:241-403 (PIC_Spectral).
+
+    Writes phi_q (painted q / dV), psi, elec_field[d], psi_fourier and
+    elec_forces = q * readout(E).  phi_q_fourier and elec_field_fourier are
+    transform scratch in the reference and are not written.
+    """
+    pos = _lib.require_cuda(positions, "positions", torch.float32)
+    n = pos.shape[0]
+    q = _lib.require_cuda(charges, "charges", torch.float32, (n,))
+    _lib.require_cuda(elec_forces, "elec_forces", torch.float32, (n, 3))
+    pm.set_functional(hamiltonian)
+    ef_all = _stack_base(elec_field, (3,), torch.float32, "elec_field")
+    fac = config.coulomb_constant / config.dielectric_const
+    _lib.call("hpf_pic_step", pm._h, _lib.ptr(pos), _lib.ptr(q), n, float(fac),
+              _lib.ptr(elec_forces), _lib.ptr(phi_q), _lib.ptr(psi), _lib.ptr(ef_all),
+              _lib.ptr(psi_fourier), None, _lib.stream_ptr())
+
+
+def comp_laplacian(phi_fourier, phi_transfer, phi_laplacian, hamiltonian, config):
+    """hymd/field.py:406-425: phi_laplacian[t][d] = c2r(-k_d^2 phi_fourier[t])."""
+    pm = _pm_of_fourier(phi_fourier)
+    T = pm.n_types
+    phif_all = _stack_base(phi_fourier, (T,), torch.complex64, "phi_fourier")
+    lap_all = _stack_base(phi_laplacian, (T, 3), torch.float32, "phi_laplacian")
+    _lib.call("hpf_laplacian", pm._h, _lib.ptr(phif_all), _lib.ptr(lap_all), _lib.stream_ptr())
+
+
+def _pm_of_fourier(phi_fourier):
+    p = phi_fourier[0].data_ptr()
+    for pm in _REGISTRY.values():
+        if pm.fields["phi_fourier"].data_ptr() == p:
+            return pm
+    raise ValueError("phi_fourier was not created by hymd_gb300.field.initialize_pm")
+
+
+def domain_decomposition(positions, pm, *args, molecules=None, bonds=None, topol=False,
+                         verbose=0, comm=None):
+    """hymd/field.py:1115-1178.  One GPU holds the whole system, so there is
+    nothing to exchange: the arrays are returned unchanged."""
+    return (positions, *args)

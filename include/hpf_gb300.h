@@ -1,0 +1,193 @@
+/*
+ * hpf_gb300 -- C ABI of the GB300 (sm_103a) hybrid particle-field force path.
+ *
+ * Every entry point takes raw device pointers, element counts and a CUDA
+ * stream (as void*), returns an int status (HPF_OK = 0) and throws nothing.
+ * Scalars that a kernel produces (energies, virials) are written to
+ * caller-provided DEVICE buffers, so no entry point synchronises the stream
+ * unless its comment says so; all of them can be captured in a CUDA graph
+ * except hpf_ctx_create/destroy/set_* and hpf_get_error.
+ *
+ * Array conventions (all row-major, device memory):
+ *   positions, velocities, forces   float[N][3]
+ *   types                           int32[N]      (0 <= type < n_types)
+ *   real mesh                       float[n0][n1][n2]        (M = n0*n1*n2)
+ *   half spectrum                   float2[n0][n1][n2/2+1]   (Mc points)
+ *   per-type stacks                 float[T][M] / float2[T][Mc]
+ *   force-mesh stack                float[T][3][M]
+ * Spectra follow the reference mesh library's convention: r2c is normalised
+ * by 1/M and c2r is unnormalised.
+ *
+ * Each declaration names the reference function it replaces (paths inside the
+ * HyMD project).
+ */
+#ifndef HPF_GB300_H
+#define HPF_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    HPF_OK = 0,
+    HPF_ERR_ARG = 1,          /* bad argument (null pointer, size, shape)        */
+    HPF_ERR_CUDA = 2,         /* a CUDA runtime call failed                      */
+    HPF_ERR_CUFFT = 3,        /* a cuFFT call failed                             */
+    HPF_ERR_INDEX = 4,        /* device saw a particle/type index out of range   */
+    HPF_ERR_NONFINITE = 5,    /* device saw a non-finite position                */
+    HPF_ERR_TIMEOUT = 6,      /* a bounded device wait ran out                   */
+    HPF_ERR_NOT_IMPLEMENTED = 7
+};
+
+typedef struct hpf_ctx hpf_ctx; /* mesh context: geometry, cuFFT plans, scratch */
+
+/* Reductions are deterministic: every block stores its partial sums, the
+ * last block adds them in block order.  Entry points without a context
+ * (bonded, integrator) take a caller-owned device workspace `out` of
+ * HPF_OUT_DOUBLES doubles: out[0..7] are the results, the rest holds the
+ * block partials and a self-resetting ticket.  Zero it once before first use. */
+#define HPF_REDUCE_BLOCKS 1024
+#define HPF_OUT_DOUBLES (8 + 8 * HPF_REDUCE_BLOCKS + 8)
+
+/* ---- context ------------------------------------------------------------
+ * Replaces initialize_pm (hymd/field.py:10-149): builds the mesh geometry and
+ * the cuFFT plans for n_types densities.  Allocates the paint accumulators,
+ * the box state and the cuFFT work area on the current device.               */
+int hpf_ctx_create(hpf_ctx** out, int n0, int n1, int n2, int n_types, const double box[3]);
+int hpf_ctx_destroy(hpf_ctx* ctx);
+/* Box change (barostat rescale, hymd/barostat_scr.py:131): rewrites the
+ * device box state; plans are kept.  Stream-ordered. */
+int hpf_ctx_set_box(hpf_ctx* ctx, const double box[3], void* stream);
+/* Device pointer to the box state (double L[3], V, dV at offsets 0..4). */
+int hpf_ctx_box_state(hpf_ctx* ctx, void** d_state);
+/* Quadratic interaction functional w = 1/2 phi.Q.phi + b.phi + c and filter
+ * width sigma (hymd/hamiltonian.py:74-486, H at :57-71).  Q is T*T row-major. */
+int hpf_ctx_set_functional(hpf_ctx* ctx, const double* Q, const double* b, double c,
+                           double sigma);
+/* First error recorded by a device-side check since the last call; clears
+ * it.  Synchronises the stream. */
+int hpf_get_error(hpf_ctx* ctx, void* stream, int* code);
+const char* hpf_status_string(int status);
+
+/* ---- particle -> mesh ----------------------------------------------------
+ * pm.paint(positions[types == t], mass=m[t]) / dV for every t
+ * (hymd/field.py:573-575).  Deterministic CIC with 64-bit fixed-point
+ * accumulation.  type_mass: host float[T].  phi_out: float[T][M].          */
+int hpf_paint(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_t n,
+              const double* type_mass, float* phi_out, void* stream);
+/* pm.paint(positions, mass=charges) / dV (hymd/field.py:363-364). */
+int hpf_paint_charge(hpf_ctx* ctx, const float* pos, const float* charges, int64_t n,
+                     float* rho_out, void* stream);
+
+/* ---- transforms (cuFFT, FP32) --------------------------------------------
+ * r2c / c2r of `batch` stacked grids (phi[t].r2c, phi_fourier[t].c2r). */
+int hpf_r2c(hpf_ctx* ctx, const float* grids, void* spectra, int batch, void* stream);
+int hpf_c2r(hpf_ctx* ctx, const void* spectra, float* grids, int batch, void* stream);
+
+/* ---- fused k-space pass --------------------------------------------------
+ * One pass over the half spectrum replacing field.py:576-616: from the raw
+ * (unnormalised) r2c spectra of the T density grids it writes
+ *   force_k[t][d] = -i k_d H(k) v_t(k),  v_t = H (Q phi~)_t + b_t delta_k0,
+ *   phi~ = H phi / M
+ * and, when the pointers are non-null, the filtered spectra phi_fourier[t]
+ * = phi~ and the potential spectra v_k[t].  When sums != NULL it adds FP64
+ * Parseval sums over k != 0 with half-spectrum weights:
+ *   sums[0] = sum_k w_k sum_ij Q_ij Re(phi~_i conj phi~_j)
+ *   sums[1+d] = sum_k w_k k_d^2 (same)            (d = 0, 1, 2)
+ * (energy, p1 and the laplacian pressure term of hymd/pressure.py:84-121).
+ * sums is a device double[4] that this call overwrites. */
+int hpf_kspace_force(hpf_ctx* ctx, const void* phi_k_raw, void* force_k,
+                     void* phi_fourier, void* v_k, double* sums, void* stream);
+/* Parseval sums (as above) from already filtered spectra phi~[t] and, when
+ * psi_k != NULL, the PIC cross terms with per-type charges (host float[T]):
+ *   sums[4] = sum_k w_k sum_t q_t Re(psi conj phi~_t)   (k = 0 included)
+ *   sums[5+d] = sum_k w_k k_d^2 sum_t q_t Re(psi conj phi~_t)
+ * sums: device double[8]. */
+int hpf_kspace_sums(hpf_ctx* ctx, const void* phi_fourier, const void* psi_k,
+                    const double* type_charges, double* sums, void* stream);
+
+/* comp_laplacian (hymd/field.py:406-425): lap_out[t][d] = c2r(-k_d^2
+ * phi_fourier[t]) for all T types and d = 0..2.  lap_out: float[T][3][M]. */
+int hpf_laplacian(hpf_ctx* ctx, const void* phi_fourier, float* lap_out, void* stream);
+
+/* ---- mesh -> particle ----------------------------------------------------
+ * force[types == t, d] = force_mesh[t][d].readout(r[types == t])
+ * (hymd/field.py:197-200).  force_mesh: float[T][3][M]; force: float[N][3]. */
+int hpf_readout(hpf_ctx* ctx, const float* force_mesh, const float* pos,
+                const int32_t* types, int64_t n, float* force, void* stream);
+
+/* ---- whole field evaluation ----------------------------------------------
+ * update_field + compute_field_force (field.py:428-616, 152-200) without the
+ * real-space intermediates: paint -> r2c -> fused k-space -> c2r(3T) ->
+ * readout.  Scratch spectra/grids belong to the context.  sums as in
+ * hpf_kspace_force (may be NULL). */
+int hpf_field_step(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_t n,
+                   const double* type_mass, float* force, double* sums, void* stream);
+
+/* ---- PIC_Spectral electrostatics ------------------------------------------
+ * update_field_force_q (hymd/field.py:241-403): paint q/dV -> r2c -> H ->
+ * psi = 4 pi k_e/eps H rho / k^2 (k=0 -> 1) -> E_d = -i k_d psi -> c2r ->
+ * F = q readout(E).  Writes elec_forces float[N][3]; when non-null also
+ * phi_q float[M], psi float[M], elec_field float[3][M], psi_k float2[Mc] and
+ * sums[0] = sum_k w_k Re(rho_k conj psi_k) (k=0 included), so that
+ * W_elec = V/2 sums[0] - E_self (field.py:698-699).  elec_factor = k_e/eps. */
+int hpf_pic_step(hpf_ctx* ctx, const float* pos, const float* charges, int64_t n,
+                 double elec_factor, float* elec_forces, float* phi_q, float* psi,
+                 float* elec_field, void* psi_k, double* sums, void* stream);
+
+/* ---- bonded (f2py calling form, hymd/force.py:8-23, main.py:509-550) ------
+ * All three zero their force array first, as the Fortran does.  Indices are
+ * int32, 0-based.  out: device workspace (HPF_OUT_DOUBLES); out[0..3] =
+ * {energy, virial_x, virial_y, virial_z} (virial = bond_pr / angle_pr).  d_err: device int (may be NULL)
+ * receives HPF_ERR_INDEX for out-of-range indices (the term is skipped).
+ * box: DEVICE double[3] (e.g. the context box state), so that a captured
+ * graph follows box changes made on the device. */
+/* cbf, hymd/compute_bond_forces.f90:1-61 */
+int hpf_bonds(float* f, const float* r, int64_t n, const double box[3], const int32_t* a,
+              const int32_t* b, const float* r0, const float* k, int64_t nb, double* out,
+              int* d_err, void* stream);
+/* caf, hymd/compute_angle_forces.f90:1-93 */
+int hpf_angles(float* f, const float* r, int64_t n, const double box[3], const int32_t* a,
+               const int32_t* b, const int32_t* c, const float* t0, const float* k,
+               int64_t na, double* out, int* d_err, void* stream);
+/* cdf, hymd/compute_dihedral_forces.f90:1-137 (+ dipole_reconstruction.f90).
+ * coeff: float[D][6][5]; dtype, last: int32[D]; dipoles float[D][4][3];
+ * transfer float[D][6][3][3] (both zeroed, written when dipole_flag = 1).
+ * out: device workspace (HPF_OUT_DOUBLES); out[0] = energy. */
+int hpf_dihedrals(float* f, const float* r, int64_t n, float* dipoles, float* transfer,
+                  const double box[3], const int32_t* a, const int32_t* b, const int32_t* c,
+                  const int32_t* d, const float* coeff, const int32_t* dtype,
+                  const int32_t* last, int64_t nd, int dipole_flag, double* out, int* d_err,
+                  void* stream);
+/* dipole_forces_redistribution, hymd/force.py:855-877: zeroes f_on_bead
+ * (float[N][3]) and adds the transfer-matrix images of the dipole forces. */
+int hpf_dipole_redistribute(float* f_on_bead, int64_t n, const float* f_dipoles,
+                            const float* transfer, const int32_t* a, const int32_t* b,
+                            const int32_t* c, const int32_t* d, const int32_t* dtype,
+                            const int32_t* last, int64_t nd, void* stream);
+
+/* ---- integrator (hymd/integrator.py:9-73, main.py:802-887) ---------------
+ * v += 0.5 dt F_i / mass for each of the n_f force arrays in order (one f32
+ * rounding per array, as repeated integrate_velocity calls do). */
+int hpf_kick(float* v, const float* const* forces, int n_f, int64_t n, double mass,
+             double dt, void* stream);
+/* Inner rRESPA step pieces: v += 0.5 dt (fb+fa+fd)/mass [times `kicks`],
+ * then r = r + dt v when drift != 0, wrapped as np.mod(r, box) when box is
+ * non-NULL.  fb/fa/fd may be NULL; box is a DEVICE double[3]. */
+int hpf_inner_kick_drift(float* r, float* v, const float* fb, const float* fa,
+                         const float* fd, int64_t n, double mass, double dt, int kicks,
+                         int drift, const double box[3], void* stream);
+/* FP64 sum of x[0..n) (y == NULL) or of x[e]*y[e] into out[0] (device
+ * workspace, HPF_OUT_DOUBLES).  Used for csum-style grid reductions
+ * (hymd/field.py:693, 699; hymd/pressure.py:100-121). */
+int hpf_sum_dot(const float* x, const float* y, int64_t n, double* out, void* stream);
+/* Sum over particles of v^2 into out[0] (device workspace, HPF_OUT_DOUBLES);
+ * KE = mass/2 * out[0]. */
+int hpf_sum_v2(const float* v, int64_t n, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HPF_GB300_H */

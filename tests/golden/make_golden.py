@@ -148,7 +148,8 @@ def main(ref):
     A = force.Angle
     uniq = sorted(set(n.decode() for n in names))
     cfg.bonds = [B(x, y, 0.5, 1000.0) for i, x in enumerate(uniq) for y in uniq[i:]]
-    cfg.angle_bonds = [A(x, y, z, 120.0, 25.0) for x in uniq for y in uniq for z in uniq if x <= z]
+    cfg.angle_bonds = [A(atom_1=x, atom_2=y, atom_3=z, equilibrium=120.0, strength=25.0)
+                       for x in uniq for y in uniq for z in uniq if x <= z]
     cfg.dihedrals = []
     packed = force.prepare_bonds(molecules, names, bonds, idx, cfg)
     topo["mws/r"] = r
