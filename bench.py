@@ -43,7 +43,9 @@ def _config_block(cfg, n, extra=None):
          "n_beads": int(n), "mesh": list(cfg.mesh()), "respa_inner": int(cfg.respa_inner),
          "time_step_ps": float(cfg.time_step), "sigma": cfg.sigma, "kappa": cfg.kappa,
          "l2": "flushed between timed steps (256 MB write, outside the timed windows)",
-         "parallelism": "replicas only"}
+         "parallelism": "replicas only",
+         "ensemble": "NPT: SCR barostat (isotropic, 1 bar, tau_p 1 ps, every step) + "
+                     "CSVR thermostat (323 K, tau 0.1 ps)"}
     if extra:
         d.update(extra)
     return d
@@ -208,6 +210,9 @@ def run_gpu(args):
     ham = get_hamiltonian(cfg)
     md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"],
                  device=dev)
+    # the membrane workload runs NPT: SCR barostat at 1 bar every step and the
+    # CSVR thermostat at 323 K; their random numbers come from a seeded table
+    md.couple(thermostat=True, barostat="isotropic", seed=100 + rank, n_steps=20000)
     md.prime()
     md.capture()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2

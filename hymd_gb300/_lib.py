@@ -50,6 +50,7 @@ _SIGNATURES = {
     "hpf_kspace_force": [P, P, P, P, P, P, P],
     "hpf_kspace_sums": [P, P, P, ctypes.POINTER(D), P, P],
     "hpf_laplacian": [P, P, P, P],
+    "hpf_energy_fp64": [P, P, P, I64, ctypes.POINTER(D), P, ctypes.POINTER(D), D, P, P],
     "hpf_readout": [P, P, P, P, I64, P, P],
     "hpf_field_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P],
     "hpf_pic_step": [P, P, P, I64, D, P, P, P, P, P, P, P],
@@ -59,9 +60,34 @@ _SIGNATURES = {
     "hpf_dipole_redistribute": [P, I64, P, P, P, P, P, P, P, P, I64, P],
     "hpf_kick": [P, ctypes.POINTER(P), I, I64, D, D, P],
     "hpf_inner_kick_drift": [P, P, P, P, P, I64, D, D, I, I, P, P],
+    "hpf_respa_plan_create": [ctypes.POINTER(P), I64, I64, P, P, P, P, I64, P, P, P, P, P, I64,
+                              P, P, P, P, P, P, P, I],
+    "hpf_respa_plan_destroy": [P],
+    "hpf_respa_plan_info": [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
+    "hpf_respa_step": [P, P, P, P, ctypes.POINTER(P), I, D, D, I, P, P, P, P, P, P],
     "hpf_sum_dot": [P, P, I64, P, P],
     "hpf_sum_v2": [P, I64, P, P],
 }
+
+class CsvrArgs(ctypes.Structure):
+    """HpfCsvrArgs of include/hpf_gb300.h."""
+    _fields_ = [("n_groups", I), ("remove_com", I), ("n_steps", I), ("stride", I),
+                ("offset", I), ("advance", I), ("every", I), ("pad", I), ("count", D * 2),
+                ("mass", D), ("gas_constant", D), ("target_temperature", D), ("c", D)]
+
+
+class ScrArgs(ctypes.Structure):
+    """HpfScrArgs of include/hpf_gb300.h."""
+    _fields_ = [("n_types", I), ("n_steps", I), ("stride", I), ("advance", I), ("every", I),
+                ("pad", I * 3), ("mass_count", D * 16), ("mass", D), ("gas_constant", D),
+                ("target_temperature", D), ("target_pressure", D), ("beta", D), ("tau_p", D),
+                ("dt_outer", D), ("n_b", D)]
+
+
+_SIGNATURES.update({
+    "hpf_csvr": [P, P, I64, ctypes.POINTER(CsvrArgs), P, P, P, P, P, P],
+    "hpf_scr_isotropic": [P, P, P, I64, P, P, ctypes.POINTER(ScrArgs), P, P, P, P, P, P],
+})
 
 _LIB = None
 

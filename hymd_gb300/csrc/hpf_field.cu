@@ -28,6 +28,10 @@ struct TypeScale {
     float s[HPF_MAX_TYPES + 1];
 };
 
+struct TypeScaleD {
+    double s[HPF_MAX_TYPES + 1];
+};
+
 // ---------------------------------------------------------------- paint ---
 // One thread per particle; 8 CIC deposits as 64-bit fixed-point integer
 // atomics (weight * 2^32), so the accumulated grid is independent of the
@@ -337,6 +341,95 @@ __global__ void k_kspace_pic(const float2* __restrict__ rho_raw, float2* __restr
     if (sums) grid_reduce_store<1>(acc, partials, ticket, sums, false);
 }
 
+// ------------------------------------------------------- FP64 energy path ---
+// Energies and pressure sums in FP64 from the fixed-point densities: the
+// accumulators are converted to double grids, transformed with a D2Z cuFFT
+// and reduced over the half spectrum in FP64.  Used where the reference
+// reports energies (print steps, barostat), never inside the MD step.
+__global__ void k_paint_finalize_f64(unsigned long long* __restrict__ acc,
+                                     double* __restrict__ out, int64_t M, int G, TypeScaleD sc,
+                                     const BoxState* __restrict__ bs) {
+    const double inv_dV = 1.0 / bs->dV;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)G * M;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int g = (int)(e / M);
+        out[e] = (double)(long long)acc[e] * (sc.s[g] * inv_dV * 2.3283064365386963e-10);
+        acc[e] = 0ull;
+    }
+}
+
+template <int TT>
+__global__ void k_energy_f64(const double2* __restrict__ spec, int T_rt, int has_q, int64_t Mc,
+                             KGeom g, double invM, const BoxState* __restrict__ bs,
+                             const Functional* __restrict__ fun, TypeScale qt, double four_pi_fac,
+                             double* out, double* partials, unsigned int* ticket) {
+    constexpr int TM = TT > 0 ? TT : HPF_MAX_TYPES;
+    const int T = TT > 0 ? TT : T_rt;
+    double acc[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+    const double kf0 = 2.0 * 3.14159265358979323846 / bs->L[0];
+    const double kf1 = 2.0 * 3.14159265358979323846 / bs->L[1];
+    const double kf2 = 2.0 * 3.14159265358979323846 / bs->L[2];
+    const double sig2h = fun->sigma2_half_d;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(idx % g.n2h);
+        const int64_t rest = idx / g.n2h;
+        const int iy = (int)(rest % g.n1);
+        const int ix = (int)(rest / g.n1);
+        const double kx = (ix <= g.n0 / 2 ? ix : ix - g.n0) * kf0;
+        const double ky = (iy <= g.n1 / 2 ? iy : iy - g.n1) * kf1;
+        const double kz = iz * kf2;
+        const double wk = (iz == 0 || ((g.n2 & 1) == 0 && iz == g.n2 / 2)) ? 1.0 : 2.0;
+        const double k2 = kx * kx + ky * ky + kz * kz;
+        const double H = exp(-sig2h * k2);
+        const double kk[3] = {kx * kx, ky * ky, kz * kz};
+        double2 ph[TM];
+#pragma unroll
+        for (int j = 0; j < TM; ++j) {
+            if (j < T) {
+                const double2 r = spec[(int64_t)j * Mc + idx];
+                ph[j] = make_double2(r.x * H * invM, r.y * H * invM);
+                if (idx == 0) out[16 + j] = r.x * invM;  // mean of phi_j
+            } else {
+                ph[j] = make_double2(0.0, 0.0);
+            }
+        }
+        double q = 0.0;
+#pragma unroll
+        for (int t = 0; t < TM; ++t) {
+            if (t >= T) break;
+            double ux = 0.0, uy = 0.0;
+#pragma unroll
+            for (int j = 0; j < TM; ++j) {
+                if (j >= T) break;
+                const double Qtj = fun->Qd[t * T + j];
+                ux += Qtj * ph[j].x;
+                uy += Qtj * ph[j].y;
+            }
+            q += ph[t].x * ux + ph[t].y * uy;
+        }
+        if (idx != 0) {
+            acc[0] += wk * q;
+            for (int d = 0; d < 3; ++d) acc[1 + d] += wk * kk[d] * q;
+        }
+        if (has_q) {
+            const double2 r = spec[(int64_t)T * Mc + idx];
+            const double2 rho = make_double2(r.x * invM, r.y * invM);
+            const double kn = idx == 0 ? 1.0 : k2;  // k.normp(p=2, zeromode=1)
+            const double s = four_pi_fac * H / kn;
+            const double2 psi = make_double2(rho.x * s, rho.y * s);
+            acc[4] += wk * (rho.x * psi.x + rho.y * psi.y);
+            double cr = 0.0;
+            for (int t = 0; t < T; ++t) cr += (double)qt.s[t] * (psi.x * ph[t].x + psi.y * ph[t].y);
+            acc[5] += wk * cr;
+            for (int d = 0; d < 3; ++d) acc[6 + d] += wk * kk[d] * cr;
+        }
+    }
+    grid_reduce_store<9>(acc, partials, ticket, out, false);
+}
+
 // -------------------------------------------------------------- laplacian ---
 // lap[t][d](k) = -k_d^2 phi~_t(k)  (comp_laplacian, hymd/field.py:406-425)
 __global__ void k_laplacian(const float2* __restrict__ phi_f, float2* __restrict__ out, int T,
@@ -487,6 +580,9 @@ int hpf_ctx_destroy(hpf_ctx* c) {
     cudaFree(c->d_spec_phi);
     cudaFree(c->d_ws);
     cudaFree(c->d_err);
+    if (c->has_d2z) cufftDestroy(c->plan_d2z);
+    cudaFree(c->d_grid64);
+    cudaFree(c->d_spec64);
     free(c);
     return HPF_OK;
 }
@@ -602,6 +698,7 @@ int hpf_ctx_set_functional(hpf_ctx* c, const double* Q, const double* b, double 
     }
     c->h_fun.c = cc;
     c->h_fun.sigma2_half = (float)(0.5 * sigma * sigma);
+    c->h_fun.sigma2_half_d = 0.5 * sigma * sigma;
     HPF_CUDA_TRY(cudaMemcpy(c->d_fun, &c->h_fun, sizeof(Functional), cudaMemcpyHostToDevice));
     return HPF_OK;
 }
@@ -681,6 +778,74 @@ int hpf_kspace_sums(hpf_ctx* c, const void* phi_fourier, const void* psi_k,
         default: HPF_KSS(0); break;
     }
 #undef HPF_KSS
+    HPF_LAUNCH_CHECK();
+    return HPF_OK;
+}
+
+int hpf_energy_fp64(hpf_ctx* c, const float* pos, const int32_t* types, int64_t n,
+                    const double* type_mass, const float* charges, const double* type_charges,
+                    double elec_factor, double* out, void* stream) {
+    if (!c || !type_mass || !out || n < 0 || (n > 0 && (!pos || !types))) return HPF_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    const int T = c->T;
+    if (!c->has_d2z) {
+        // lazily: the FP64 buffers and the D2Z plan are only needed for energies
+        HPF_CUDA_TRY(cudaMalloc(&c->d_grid64, sizeof(double) * (size_t)(T + 1) * c->M));
+        HPF_CUDA_TRY(cudaMalloc(&c->d_spec64, sizeof(double2) * (size_t)(T + 1) * c->Mc));
+        long long nn[3] = {c->n0, c->n1, c->n2};
+        size_t ws = 0;
+        if (cufftCreate(&c->plan_d2z) != CUFFT_SUCCESS) return HPF_ERR_CUFFT;
+        if (cufftMakePlanMany64(c->plan_d2z, 3, nn, NULL, 1, c->M, NULL, 1, c->Mc, CUFFT_D2Z,
+                                T + 1, &ws) != CUFFT_SUCCESS) {
+            cufftDestroy(c->plan_d2z);
+            return HPF_ERR_CUFFT;
+        }
+        c->has_d2z = true;
+    }
+    TypeScaleD sc;
+    for (int t = 0; t < T; ++t) sc.s[t] = type_mass[t];
+    sc.s[T] = 1.0;
+    // densities into accumulator slots 0..T-1, charges into slot T
+    if (n > 0) {
+        k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, types, nullptr, n, T, c->d_box,
+                                                           c->d_acc, c->M, c->d_err);
+        HPF_LAUNCH_CHECK();
+        if (charges) {
+            k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(
+                pos, nullptr, charges, n, 1, c->d_box, c->d_acc + (int64_t)T * c->M, c->M,
+                c->d_err);
+            HPF_LAUNCH_CHECK();
+        }
+    }
+    k_paint_finalize_f64<<<grid_for((int64_t)(T + 1) * c->M, kThreads), kThreads, 0, st>>>(
+        c->d_acc, c->d_grid64, c->M, T + 1, sc, c->d_box);
+    HPF_LAUNCH_CHECK();
+    if (cufftSetStream(c->plan_d2z, st) != CUFFT_SUCCESS) return HPF_ERR_CUFFT;
+    if (cufftExecD2Z(c->plan_d2z, c->d_grid64, reinterpret_cast<cufftDoubleComplex*>(c->d_spec64)) !=
+        CUFFT_SUCCESS)
+        return HPF_ERR_CUFFT;
+    TypeScale qt;
+    for (int t = 0; t < T; ++t) qt.s[t] = type_charges ? (float)type_charges[t] : 0.0f;
+    KGeom g = kgeom(c);
+    int grid = reduce_grid(c->Mc, kThreads);
+    if (grid > 896) grid = 896;  // 9 partials per block must fit the workspace
+    const double fpf = 4.0 * 3.14159265358979323846 * elec_factor;
+    double* part = ws_partials(c->d_ws);
+    unsigned int* tick = ws_ticket(c->d_ws);
+    const int hq = charges ? 1 : 0;
+    const double invM = 1.0 / (double)c->M;
+#define HPF_KE(TT)                                                                          \
+    k_energy_f64<TT><<<grid, kThreads, 0, st>>>(c->d_spec64, T, hq, c->Mc, g, invM, c->d_box, \
+                                                c->d_fun, qt, fpf, out, part, tick)
+    switch (T) {
+        case 1: HPF_KE(1); break;
+        case 2: HPF_KE(2); break;
+        case 3: HPF_KE(3); break;
+        case 4: HPF_KE(4); break;
+        case 5: HPF_KE(5); break;
+        default: HPF_KE(0); break;
+    }
+#undef HPF_KE
     HPF_LAUNCH_CHECK();
     return HPF_OK;
 }

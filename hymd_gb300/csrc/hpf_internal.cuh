@@ -32,7 +32,8 @@ struct Functional {
     double Qd[HPF_MAX_TYPES * HPF_MAX_TYPES];
     double bd[HPF_MAX_TYPES];
     double c;
-    float sigma2_half;   // 0.5 * sigma^2
+    double sigma2_half_d;  // 0.5 * sigma^2
+    float sigma2_half;
     float pad;
 };
 
@@ -52,6 +53,11 @@ struct hpf_ctx {
     int* d_err;               // first device error code
     void* fft_work;
     size_t fft_work_size;
+    // FP64 energy path (created on first use, outside graph capture)
+    cufftHandle plan_d2z;     // batch T+1: T densities + charges
+    bool has_d2z;
+    double* d_grid64;         // double[T+1][M]
+    double2* d_spec64;        // double2[T+1][Mc]
     cufftHandle plan_r2c[HPF_MAX_TYPES + 1];   // batch b at index b (created lazily)
     cufftHandle plan_c2r[3 * HPF_MAX_TYPES + 2];
     bool has_r2c[HPF_MAX_TYPES + 1];

@@ -1,0 +1,259 @@
+// Per-term bonded arithmetic shared by the stand-alone bonded kernels and the
+// fused rRESPA kernel.  Each function takes the term's bead positions and
+// returns the forces on its beads (no memory traffic of its own).
+//
+// Reference behaviour (paths inside the HyMD project):
+//   cbf   hymd/compute_bond_forces.f90:45-61
+//   caf   hymd/compute_angle_forces.f90:58-92
+//   cdf   hymd/compute_dihedral_forces.f90:29-135
+//   cosine_series / reconstruct  hymd/dipole_reconstruction.f90:37-220
+// Differences of stored positions are taken in FP32 as the Fortran does
+// (real(4) operands); the rest is FP32 arithmetic formulated to stay well
+// conditioned: angles use atan2(|e_a x e_c|, e_a . e_c) instead of acos.
+#pragma once
+
+#include <math.h>
+
+struct V3 {
+    float x, y, z;
+};
+
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float norm(V3 a) { return sqrtf(dot(a, a)); }
+
+struct Box {
+    float L[3], iL[3];
+};
+
+__device__ __forceinline__ Box load_box(const double* box) {
+    Box b;
+    for (int d = 0; d < 3; ++d) {
+        b.L[d] = (float)box[d];
+        b.iL[d] = (float)(1.0 / box[d]);
+    }
+    return b;
+}
+
+// r - box * nint(r / box); nint rounds half away from zero (roundf).
+__device__ __forceinline__ V3 min_image(V3 r, const Box& b) {
+    r.x = fmaf(-b.L[0], roundf(r.x * b.iL[0]), r.x);
+    r.y = fmaf(-b.L[1], roundf(r.y * b.iL[1]), r.y);
+    r.z = fmaf(-b.L[2], roundf(r.z * b.iL[2]), r.z);
+    return r;
+}
+
+// Harmonic bond between a and b.  Returns the force on b (minus on a);
+// e = 1/2 k (|r|-r0)^2; vir = fa * rab (componentwise, bond_pr).
+__device__ __forceinline__ V3 bond_term(V3 pa, V3 pb, float r0, float k, const Box& bx,
+                                        float& e, V3& vir) {
+    const V3 rab = min_image(pb - pa, bx);
+    const float rn = norm(rab);
+    const float dr = rn - r0;
+    const V3 fa = (-k * dr / rn) * rab;
+    e = 0.5f * k * dr * dr;
+    vir = v3(fa.x * rab.x, fa.y * rab.y, fa.z * rab.z);
+    return fa;
+}
+
+// Harmonic angle a-b-c.  Writes the positive gradients ga (on a) and gc (on
+// c); the force on a is -ga, on c -gc, on b ga+gc.  Returns false for an
+// exactly collinear triple (skipped, as the Fortran skips cos^2 >= 1).
+__device__ __forceinline__ bool angle_term(V3 pa, V3 pb, V3 pc, float t0, float k, const Box& bx,
+                                           V3& ga, V3& gc, float& e, V3& vir) {
+    const V3 ra = min_image(pa - pb, bx);
+    const V3 rc = min_image(pc - pb, bx);
+    const float na_ = norm(ra), nc_ = norm(rc);
+    const V3 ea = (1.0f / na_) * ra, ec = (1.0f / nc_) * rc;
+    const float cosphi = dot(ea, ec);
+    const float sinphi = norm(cross(ea, ec));
+    if (!(sinphi > 0.0f)) return false;
+    const float theta = atan2f(sinphi, cosphi);
+    const float d = theta - t0;
+    const float ff = k * d;
+    ga = (-ff / (na_ * sinphi)) * (ec - cosphi * ea);
+    gc = (-ff / (nc_ * sinphi)) * (ea - cosphi * ec);
+    e = 0.5f * ff * d;
+    vir = v3(-(ga.x * ra.x) - (gc.x * rc.x), -(ga.y * ra.y) - (gc.y * rc.y),
+             -(ga.z * ra.z) - (gc.z * rc.z));
+    return true;
+}
+
+__device__ __forceinline__ void cosine_series(const float* cn, const float* dn, float phi,
+                                              float& e, float& de) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        float s, c;
+        sincosf(i * phi - dn[i], &s, &c);
+        e = fmaf(cn[i], 1.0f + c, e);
+        de = fmaf(-(float)i * cn[i], s, de);
+    }
+}
+
+// reconstruct (dipole_reconstruction.f90:50-220): CBT bending energy of the
+// angle (rab, rcb) at bead rb and, with dipole_flag, the two dipole
+// pseudo-charge positions (dipole[0..5]) and the three 3x3 transfer matrices
+// (tm[0..26]).  Outputs the positive gradients fa, fb, fc.  Where
+// cos^2(gamma) >= 1 the Fortran leaves its outputs unassigned; here they are
+// zero.
+static __device__ void reconstruct(V3 rab, V3 rb, V3 rcb, const Box& bx, const float* c_k,
+                            const float* d_k, float phi, int dipole_flag, float& e_cbt,
+                            float& df_cbt, V3& fa, V3& fb, V3& fc, float* dipole, float* tm) {
+    // cos(1.392947) / sin(1.392947): single-precision literals in the Fortran
+    const float cos_psi = cosf(1.392947f), sin_psi = sinf(1.392947f);
+    const float delta = 0.3f;
+    float k = 0.0f, dk = 0.0f;
+    const float gamma_0 = 1.85f - 0.227f * cosf(phi - 0.785f);
+    const float dg = 0.227f * sinf(phi - 0.785f);
+    cosine_series(c_k, d_k, phi, k, dk);
+    const float norm_a = norm(rab), norm_c = norm(rcb);
+    const V3 w = (1.0f / norm_a) * rab, v = (1.0f / norm_c) * rcb;
+    const float cos_gamma = dot(w, v);
+    e_cbt = 0.0f;
+    df_cbt = 0.0f;
+    fa = fb = fc = v3(0.f, 0.f, 0.f);
+    if (!(cos_gamma * cos_gamma < 1.0f)) return;
+    const float gamm = acosf(cos_gamma);
+    float sin_gamma = sqrtf(1.0f - cos_gamma * cos_gamma);
+    if (sin_gamma < 0.1f) sin_gamma = 0.1f;
+    fa = (-1.0f / (norm_a * sin_gamma)) * (v - cos_gamma * w);
+    fc = (-1.0f / (norm_c * sin_gamma)) * (w - cos_gamma * v);
+    fb = -(fa + fc);
+    const float df_ang = k * (gamm - gamma_0);
+    const float var_sq = (gamm - gamma_0) * (gamm - gamma_0);
+    e_cbt = 0.5f * k * var_sq;
+    df_cbt = 0.5f * dk * var_sq - df_ang * dg;
+    if (dipole_flag && dipole) {
+        const float fac = expf((gamm - 1.73f) / 0.025f);
+        const float theta = -1.607f * gamm + 0.094f + 1.883f / (1.0f + fac);
+        const float d_theta = -1.607f - 1.883f / 0.025f * fac / ((1.0f + fac) * (1.0f + fac));
+        float sin_theta, cos_theta;
+        sincosf(theta, &sin_theta, &cos_theta);
+        const V3 nn = (1.0f / sin_gamma) * cross(w, v);
+        const V3 m = cross(nn, v);
+        const V3 r0 = rb + 0.5f * rcb;
+        const V3 d = (0.5f * delta) * (cos_psi * v + sin_psi * (cos_theta * nn + sin_theta * m));
+        const V3 p[2] = {r0 + d, r0 - d};
+        for (int q = 0; q < 2; ++q) {
+            const V3 pw = min_image(p[q], bx);
+            dipole[3 * q] = pw.x;
+            dipole[3 * q + 1] = pw.y;
+            dipole[3 * q + 2] = pw.z;
+        }
+        const float wv[3] = {w.x, w.y, w.z}, vv[3] = {v.x, v.y, v.z};
+        const float nv[3] = {nn.x, nn.y, nn.z}, mv[3] = {m.x, m.y, m.z};
+        const float fav[3] = {fa.x, fa.y, fa.z}, fbv[3] = {fb.x, fb.y, fb.z},
+                    fcv[3] = {fc.x, fc.y, fc.z};
+        for (int i = 0; i < 3; ++i) {
+            float Vb[3], Wb[3];
+            for (int j = 0; j < 3; ++j) {
+                Vb[j] = (vv[i] * vv[j] - (i == j ? 1.0f : 0.0f)) / norm_c;
+                Wb[j] = (wv[i] * wv[j] - (i == j ? 1.0f : 0.0f)) / norm_a;
+            }
+            // cross_matrix(Mx, x): row i = cross(Mx(i,:), x); with Vc = -Vb, Wa = -Wb
+            const V3 Wbi = v3(Wb[0], Wb[1], Wb[2]);
+            const V3 Vbi = v3(Vb[0], Vb[1], Vb[2]);
+            const V3 cWb_v = cross(Wbi, v), cVb_w = cross(Vbi, w), cVb_n = cross(Vbi, nn);
+            const V3 Na = (1.0f / sin_gamma) * (cos_gamma * fav[i] * nn - cWb_v);
+            const V3 Nb = (1.0f / sin_gamma) * (cos_gamma * fbv[i] * nn + cWb_v - cVb_w);
+            const V3 Nc = (1.0f / sin_gamma) * (cos_gamma * fcv[i] * nn + cVb_w);
+            const V3 Ma = cross(Na, v);
+            const V3 Mb = cross(Nb, v) - cVb_n;
+            const V3 Mc = cross(Nc, v) + cVb_n;
+            const float Ma_[3] = {Ma.x, Ma.y, Ma.z}, Mb_[3] = {Mb.x, Mb.y, Mb.z},
+                        Mc_[3] = {Mc.x, Mc.y, Mc.z};
+            const float Na_[3] = {Na.x, Na.y, Na.z}, Nb_[3] = {Nb.x, Nb.y, Nb.z},
+                        Nc_[3] = {Nc.x, Nc.y, Nc.z};
+            const float st_dt = sin_theta * d_theta, ct_dt = cos_theta * d_theta;
+            for (int j = 0; j < 3; ++j) {
+                const float FNa = st_dt * fav[i] * nv[j], FMa = ct_dt * fav[i] * mv[j];
+                const float FNb = st_dt * fbv[i] * nv[j], FMb = ct_dt * fbv[i] * mv[j];
+                const float FNc = st_dt * fcv[i] * nv[j], FMc = ct_dt * fcv[i] * mv[j];
+                tm[0 * 9 + i * 3 + j] =
+                    0.5f * delta * (sin_psi * (cos_theta * Na_[j] + sin_theta * Ma_[j] + FNa - FMa));
+                tm[1 * 9 + i * 3 + j] =
+                    0.5f * delta * (cos_psi * Vb[j] +
+                                    sin_psi * (cos_theta * Nb_[j] + sin_theta * Mb_[j] + FNb - FMb));
+                tm[2 * 9 + i * 3 + j] =
+                    0.5f * delta * (-cos_psi * Vb[j] +
+                                    sin_psi * (cos_theta * Nc_[j] + sin_theta * Mc_[j] + FNc - FMc));
+            }
+        }
+    }
+    fa = df_ang * fa;
+    fb = df_ang * fb;
+    fc = df_ang * fc;
+}
+
+// Four-body term a-b-c-d of type ty (0 cosine series, 1 + CBT, 2 improper).
+// coeff: 30 floats (6 rows x 5).  Writes the forces on the four beads
+// (F[0..3]) and the energy; with dipole_flag writes dipole[0..11] and
+// tm[0..53] for type 1 (the caller zeroes them first).
+__device__ __forceinline__ void dihedral_term(V3 pa, V3 pb, V3 pc, V3 pd, const float* cf, int ty,
+                                              int last, int dipole_flag, const Box& bx, V3 F[4],
+                                              float& e_out, float* dip, float* tmx) {
+    const V3 fv = min_image(pa - pb, bx);
+    const V3 g = min_image(pb - pc, bx);
+    const V3 h = min_image(pd - pc, bx);
+    const V3 v = cross(fv, g), w = cross(h, g);
+    const float v_sq = dot(v, v), w_sq = dot(w, w);
+    const float g_norm = norm(g);
+    const float cos_phi = dot(v, w);
+    const float sin_phi = dot(w, fv) * g_norm;
+    const float phi = atan2f(sin_phi, cos_phi);
+    const float f_dot_g = dot(fv, g), h_dot_g = dot(h, g);
+    float row[6][5];
+    for (int p = 0; p < 6; ++p)
+        for (int q = 0; q < 5; ++q) row[p][q] = cf[5 * p + q];
+    float e = 0.0f, df_dih = 0.0f;
+    F[0] = F[1] = F[2] = F[3] = v3(0.f, 0.f, 0.f);
+    if (ty == 0 || ty == 1) {
+        cosine_series(row[0], row[1], phi, e, df_dih);
+        bool nz_c = false, nz_d = false;
+        for (int q = 0; q < 5; ++q) {
+            nz_c |= row[2][q] != 0.0f;
+            nz_d |= row[3][q] != 0.0f;
+        }
+        if (nz_c && nz_d) cosine_series(row[2], row[3], phi, e, df_dih);
+    }
+    if (ty == 1) {
+        float e_cbt, df_cbt;
+        V3 fa, fb, fc, fd;
+        reconstruct(fv, pb, -g, bx, row[4], row[5], phi, dipole_flag, e_cbt, df_cbt, fa, fb, fc,
+                    dip, tmx);
+        e += e_cbt;
+        df_dih += df_cbt;
+        F[0] = F[0] - fa;
+        F[1] = F[1] - fb;
+        F[2] = F[2] - fc;
+        if (last == 1) {
+            reconstruct(g, pc, h, bx, row[4], row[5], phi, dipole_flag, e_cbt, df_cbt, fb, fc, fd,
+                        dip ? dip + 6 : nullptr, tmx ? tmx + 27 : nullptr);
+            e += e_cbt;
+            df_dih += df_cbt;
+            F[1] = F[1] - fb;
+            F[2] = F[2] - fc;
+            F[3] = F[3] - fd;
+        }
+    }
+    if (ty == 2) {
+        const float eq = row[0][0], kc = row[0][1];
+        df_dih = kc * (phi - eq);
+        e += 0.5f * kc * (phi - eq) * (phi - eq);
+    }
+    const V3 sc = (f_dot_g / (v_sq * g_norm)) * v - (h_dot_g / (w_sq * g_norm)) * w;
+    const V3 fa = (-df_dih * g_norm / v_sq) * v;
+    const V3 fd = (df_dih * g_norm / w_sq) * w;
+    F[0] = F[0] + fa;
+    F[1] = F[1] + (df_dih * sc - fa);
+    F[2] = F[2] + (-df_dih * sc - fd);
+    F[3] = F[3] + fd;
+    e_out = e;
+}

@@ -247,7 +247,7 @@ def update_field(phi, phi_laplacian, phi_transfer, layouts, force_mesh, hamilton
     if compute_potential:
         vext_all = _stack_base(v_ext, (T,), torch.float32, "v_ext")
         _lib.call("hpf_c2r", pm._h, _lib.ptr(v_k), _lib.ptr(vext_all), T, st)
-    pm._last_counts = None
+    pm.last_types = typ
 
 
 def compute_field_force(layouts, r, force_mesh, force, types, n_types):
@@ -275,56 +275,58 @@ def _find_pm_for_force(force_all):
     raise ValueError("force_mesh was not created by hymd_gb300.field.initialize_pm")
 
 
-def _sum(pm, x, y=None):
-    st = _lib.stream_ptr()
-    _lib.call("hpf_sum_dot", _lib.ptr(x), _lib.ptr(y), x.numel(), _lib.ptr(pm.ws), st)
-    return pm.ws[0]
+def energy_fp64(pm, positions, types, masses, hamiltonian, charges=None, type_charges=None,
+                elec_factor=0.0):
+    """FP64 energy and pressure sums of the current positions (hpf_energy_fp64).
 
-
-def field_energy_parts(pm, phi_all, hamiltonian):
-    """W of the filtered densities phi_all (T, n0, n1, n2), FP64.
-
-    k != 0 modes by Parseval in one k-space pass; the k = 0 part V w(mean phi)
-    from FP64 sums of the grids, so that the incompressibility term's
-    cancellation (sum phi - a) happens exactly.
-    """
+    Returns dict(W, A, B[3], Eq, C0, C[3], means[T], V): W = V w(means) + V/2 A."""
     T = pm.n_types
     Q, b, c, sigma = pm.set_functional(hamiltonian)
-    st = _lib.stream_ptr()
-    spec = pm.complex_field(T)
-    _lib.call("hpf_r2c", pm._h, _lib.ptr(phi_all), _lib.ptr(spec), T, st)
-    spec.mul_(1.0 / pm.M)
-    sums = torch.zeros(8, dtype=torch.float64, device=pm.device)
-    _lib.call("hpf_kspace_sums", pm._h, _lib.ptr(spec), None, None, _lib.ptr(sums), st)
-    means = np.array([float(_sum(pm, phi_all[t])) / pm.M for t in range(T)])
+    pos = _lib.require_cuda(positions, "positions", torch.float32)
+    n = pos.shape[0]
+    typ = _types32(types, n)
+    q = None if charges is None else _lib.require_cuda(charges, "charges", torch.float32, (n,))
+    out = torch.zeros(32, dtype=torch.float64, device=pm.device)
+    qt = _lib.dvec(list(type_charges)) if type_charges is not None else None
+    _lib.call("hpf_energy_fp64", pm._h, _lib.ptr(pos), _lib.ptr(typ), n,
+              _lib.dvec(_masses(masses, T)), _lib.ptr(q), qt, float(elec_factor), _lib.ptr(out),
+              _lib.stream_ptr())
+    o = out.cpu().numpy()
     V = float(np.prod(pm.BoxSize))
-    A = float(sums[0])
-    W_dc = V * (0.5 * means @ Q @ means + b @ means + c)
-    return W_dc + 0.5 * V * A, means, sums
+    means = o[16:16 + T].copy()
+    W = V * (0.5 * means @ Q @ means + b @ means + c) + 0.5 * V * o[0]
+    return dict(W=W, A=o[0], B=o[1:4].copy(), Eq=o[4], C0=o[5], C=o[6:9].copy(), means=means,
+                V=V, Q=Q, b=b, sigma=sigma)
 
 
 def compute_field_and_kinetic_energy(phi, phi_q, psi, velocity, hamiltonian, positions, types,
                                      v_ext, config, layouts, comm=None):
     """hymd/field.py:619-703 -> (field_energy, kinetic_energy, field_q_energy).
 
-    W = sum_g w_0(phi~) dV is evaluated from the given phi~ grids in FP64 (see
-    `field_energy_parts`); KE = m/2 sum v^2; with PIC_Spectral, W_elec =
-    sum_g (phi_q psi / 2 - E_self / V) dV.
+    W = sum_g w_0(phi~) dV and, with PIC_Spectral, W_elec = sum_g (phi_q psi /
+    2 - E_self / V) dV are evaluated in FP64 for the given positions (the
+    positions that produced phi in update_field): fixed-point densities ->
+    FP64 FFT -> FP64 Parseval sums, with the k = 0 term from the exact means.
+    The charges are those of the last update_field_force_q on this mesh.
+    KE = m/2 sum v^2 (FP64 sum).
     """
     pm = _pm_of(phi)
-    T = pm.n_types
-    phi_all = _stack_base(phi, (T,), torch.float32, "phi")
-    W, _, _ = field_energy_parts(pm, phi_all, hamiltonian)
+    charges = None
+    fac = 0.0
+    if config.coulombtype == "PIC_Spectral":
+        charges = getattr(pm, "pic_charges", None)
+        if charges is None:
+            raise ValueError("PIC_Spectral energy needs a preceding update_field_force_q")
+        fac = config.coulomb_constant / config.dielectric_const
+    e = energy_fp64(pm, positions, types, config.m, hamiltonian, charges=charges,
+                    elec_factor=fac)
     vel = _lib.require_cuda(velocity, "velocity", torch.float32)
     _lib.call("hpf_sum_v2", _lib.ptr(vel), vel.shape[0], _lib.ptr(pm.ws), _lib.stream_ptr())
     ke = 0.5 * float(config.mass) * float(pm.ws[0])
     wq = 0.0
-    if config.coulombtype == "PIC_Spectral":
-        V = float(np.prod(pm.BoxSize))
-        dV = V / pm.M
-        dot = float(_sum(pm, phi_q, psi))
-        wq = 0.5 * dot * dV - float(config.self_energy or 0.0)
-    return W, ke, wq
+    if charges is not None:
+        wq = 0.5 * e["V"] * e["Eq"] - float(config.self_energy or 0.0)
+    return e["W"], ke, wq
 
 
 def compute_self_energy_q(config, charges, comm=None):
@@ -352,9 +354,13 @@ def update_field_force_q(charges, phi_q, phi_q_fourier, psi, psi_fourier, elec_f
     pm.set_functional(hamiltonian)
     ef_all = _stack_base(elec_field, (3,), torch.float32, "elec_field")
     fac = config.coulomb_constant / config.dielectric_const
+    if getattr(pm, "pic_sums", None) is None:
+        pm.pic_sums = torch.zeros(8, dtype=torch.float64, device=pm.device)
     _lib.call("hpf_pic_step", pm._h, _lib.ptr(pos), _lib.ptr(q), n, float(fac),
               _lib.ptr(elec_forces), _lib.ptr(phi_q), _lib.ptr(psi), _lib.ptr(ef_all),
-              _lib.ptr(psi_fourier), None, _lib.stream_ptr())
+              _lib.ptr(psi_fourier), _lib.ptr(pm.pic_sums), _lib.stream_ptr())
+    # the charges of this evaluation, for the FP64 energy / pressure
+    pm.pic_charges = q
 
 
 def comp_laplacian(phi_fourier, phi_transfer, phi_laplacian, hamiltonian, config):

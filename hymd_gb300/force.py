@@ -338,7 +338,11 @@ def _dev_box(box, device):
 
 
 def _err(device):
-    return _ws(device, "err")
+    """Device int32 error word shared by the bonded entry points."""
+    k = (str(device), "err")
+    if k not in _WS:
+        _WS[k] = torch.zeros(8, dtype=torch.int32, device=device)
+    return _WS[k]
 
 
 def _check_err(device):
@@ -349,6 +353,11 @@ def _check_err(device):
         raise _lib.HPFError("bonded device check", int(code))
 
 
+# Every device argument below is bound to a local name until the library call
+# has been issued: a temporary that died earlier would return its memory to
+# torch's caching allocator, and the next temporary could reuse it before the
+# kernel reads it.
+
 def compute_bond_forces(f, r, box, a, b, r0, k, sync=True):
     """cbf (hymd/compute_bond_forces.f90:1-61) -> (energy, bond_pr).
 
@@ -357,12 +366,13 @@ def compute_bond_forces(f, r, box, a, b, r0, k, sync=True):
     _lib.require_cuda(f, "f", torch.float32)
     _lib.require_cuda(r, "r", torch.float32)
     dev = r.device
-    ws = _ws(dev, "bonds")
-    err = _err(dev)
+    ws, err = _ws(dev, "bonds"), _err(dev)
+    bx = _dev_box(box, dev)
     A, B = _dev_i32(a, dev), _dev_i32(b, dev)
-    _lib.call("hpf_bonds", _lib.ptr(f), _lib.ptr(r), r.shape[0], _lib.ptr(_dev_box(box, dev)),
-              _lib.ptr(A), _lib.ptr(B), _lib.ptr(_dev_f32(r0, dev)), _lib.ptr(_dev_f32(k, dev)),
-              A.numel(), _lib.ptr(ws), _lib.ctypes.c_void_p(err.data_ptr()), _lib.stream_ptr())
+    R0, K = _dev_f32(r0, dev), _dev_f32(k, dev)
+    _lib.call("hpf_bonds", _lib.ptr(f), _lib.ptr(r), r.shape[0], _lib.ptr(bx), _lib.ptr(A),
+              _lib.ptr(B), _lib.ptr(R0), _lib.ptr(K), A.numel(), _lib.ptr(ws), _lib.ptr(err),
+              _lib.stream_ptr())
     if not sync:
         return ws
     out = ws[:4].cpu().numpy()
@@ -375,13 +385,13 @@ def compute_angle_forces(f, r, box, a, b, c, t0, k, sync=True):
     _lib.require_cuda(f, "f", torch.float32)
     _lib.require_cuda(r, "r", torch.float32)
     dev = r.device
-    ws = _ws(dev, "angles")
-    err = _err(dev)
+    ws, err = _ws(dev, "angles"), _err(dev)
+    bx = _dev_box(box, dev)
     A, B, C = _dev_i32(a, dev), _dev_i32(b, dev), _dev_i32(c, dev)
-    _lib.call("hpf_angles", _lib.ptr(f), _lib.ptr(r), r.shape[0], _lib.ptr(_dev_box(box, dev)),
-              _lib.ptr(A), _lib.ptr(B), _lib.ptr(C), _lib.ptr(_dev_f32(t0, dev)),
-              _lib.ptr(_dev_f32(k, dev)), A.numel(), _lib.ptr(ws),
-              _lib.ctypes.c_void_p(err.data_ptr()), _lib.stream_ptr())
+    T0, K = _dev_f32(t0, dev), _dev_f32(k, dev)
+    _lib.call("hpf_angles", _lib.ptr(f), _lib.ptr(r), r.shape[0], _lib.ptr(bx), _lib.ptr(A),
+              _lib.ptr(B), _lib.ptr(C), _lib.ptr(T0), _lib.ptr(K), A.numel(), _lib.ptr(ws),
+              _lib.ptr(err), _lib.stream_ptr())
     if not sync:
         return ws
     out = ws[:4].cpu().numpy()
@@ -397,16 +407,18 @@ def compute_dihedral_forces(f, r, dipoles, transfer, box, a, b, c, d, coeff, dty
     _lib.require_cuda(f, "f", torch.float32)
     _lib.require_cuda(r, "r", torch.float32)
     dev = r.device
-    ws = _ws(dev, "dihedrals")
-    err = _err(dev)
+    ws, err = _ws(dev, "dihedrals"), _err(dev)
+    bx = _dev_box(box, dev)
     A, B, C, Dd = (_dev_i32(x, dev) for x in (a, b, c, d))
     nd = A.numel()
     cf = _dev_f32(coeff, dev).reshape(nd, 6, 5).contiguous()
+    ty, la = _dev_i32(dtype, dev), _dev_i32(last, dev)
+    _lib.require_cuda(dipoles, "dipoles", torch.float32, (nd, 4, 3))
+    _lib.require_cuda(transfer, "transfer", torch.float32, (nd, 6, 3, 3))
     _lib.call("hpf_dihedrals", _lib.ptr(f), _lib.ptr(r), r.shape[0], _lib.ptr(dipoles),
-              _lib.ptr(transfer), _lib.ptr(_dev_box(box, dev)), _lib.ptr(A), _lib.ptr(B),
-              _lib.ptr(C), _lib.ptr(Dd), _lib.ptr(cf), _lib.ptr(_dev_i32(dtype, dev)),
-              _lib.ptr(_dev_i32(last, dev)), nd, int(dipole_flag), _lib.ptr(ws),
-              _lib.ctypes.c_void_p(err.data_ptr()), _lib.stream_ptr())
+              _lib.ptr(transfer), _lib.ptr(bx), _lib.ptr(A), _lib.ptr(B), _lib.ptr(C),
+              _lib.ptr(Dd), _lib.ptr(cf), _lib.ptr(ty), _lib.ptr(la), nd, int(dipole_flag),
+              _lib.ptr(ws), _lib.ptr(err), _lib.stream_ptr())
     if not sync:
         return ws
     e = float(ws[0].item())
@@ -424,7 +436,7 @@ def dipole_forces_redistribution(f_on_bead, f_dipoles, trans_matrices, a, b, c, 
     nd = A.numel()
     fd = _dev_f32(f_dipoles, dev).reshape(nd, 4, 3).contiguous()
     tm = _dev_f32(trans_matrices, dev).reshape(nd, 6, 3, 3).contiguous()
+    ty, la = _dev_i32(type_array, dev), _dev_i32(last_bb, dev)
     _lib.call("hpf_dipole_redistribute", _lib.ptr(f_on_bead), f_on_bead.shape[0], _lib.ptr(fd),
-              _lib.ptr(tm), _lib.ptr(A), _lib.ptr(B), _lib.ptr(C), _lib.ptr(Dd),
-              _lib.ptr(_dev_i32(type_array, dev)), _lib.ptr(_dev_i32(last_bb, dev)), nd,
-              _lib.stream_ptr())
+              _lib.ptr(tm), _lib.ptr(A), _lib.ptr(B), _lib.ptr(C), _lib.ptr(Dd), _lib.ptr(ty),
+              _lib.ptr(la), nd, _lib.stream_ptr())

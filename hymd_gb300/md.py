@@ -1,17 +1,20 @@
 """GPU-resident rRESPA driver (the loop of hymd/main.py:764-1169).
 
 One outer step, as in the reference:
-  1. outer half kick with the slow forces (field [+ PIC] [+ dipole]),
+  1. outer half kick with the slow forces (field [+ PIC]),
      dt_outer = respa_inner * time_step                     (main.py:802-827)
   2. respa_inner times: half kick with the bonded forces, drift, wrap
      np.mod(r, box), bonded forces, half kick              (main.py:830-887)
   3. slow forces at the new positions: field (paint -> r2c -> fused k-space
      -> c2r -> readout) and, with charges, PIC_Spectral     (main.py:975-1095)
   4. second outer half kick                                 (main.py:1143-1169)
-The half kick closing inner step i and the one opening step i+1 run in one
-launch (two FP32 roundings, as two reference calls).  The whole step is a
-fixed launch sequence with no host synchronisation, so `capture()` records it
-once in a CUDA graph and `run()` replays it.
+
+fused=True (default): steps 1-2 are one launch of the molecule-blocked
+rRESPA kernel (hpf_respa_step); molecules that do not fit a CTA fall back to
+the per-term kernels.  fused=False: per-term kernels and one kick/drift
+launch per inner step (the reference's call sequence, kept for comparison).
+Either way a step is a fixed launch sequence with no host synchronisation, so
+`capture()` records it once in a CUDA graph and `run()` replays it.
 """
 import numpy as np
 import torch
@@ -23,7 +26,7 @@ from .force import BondedTopology
 
 class RespaMD:
     def __init__(self, positions, velocities, types, config, hamiltonian, topology=None,
-                 charges=None, device="cuda"):
+                 charges=None, device="cuda", fused=True, max_block_beads=512):
         self.device = torch.device(device)
         self.config = config
         self.r = torch.as_tensor(np.asarray(positions, np.float32), device=self.device).contiguous()
@@ -40,8 +43,13 @@ class RespaMD:
         self.respa = int(config.respa_inner)
         z = lambda: torch.zeros((self.n, 3), dtype=torch.float32, device=self.device)
         self.f_field, self.f_bond, self.f_angle, self.f_dih = z(), z(), z(), z()
-        self.topo = topology if (topology is None or isinstance(topology, BondedTopology)) \
-            else BondedTopology(topology, device=self.device)
+        self.f_b = z()  # combined bonded force carried by the fused kernel
+        packed = None
+        if topology is None or isinstance(topology, BondedTopology):
+            self.topo = topology
+        else:
+            packed = topology
+            self.topo = BondedTopology(topology, device=self.device)
         self.charges = None
         self.f_elec = None
         if charges is not None:
@@ -51,23 +59,149 @@ class RespaMD:
         self.ws_bond = _lib.new_workspace(self.device)
         self.ws_angle = _lib.new_workspace(self.device)
         self.ws_dih = _lib.new_workspace(self.device)
+        self.bonded_out = torch.zeros(16, dtype=torch.float64, device=self.device)
         self.err = torch.zeros(8, dtype=torch.int32, device=self.device)
-        self.field_sums = torch.zeros(8, dtype=torch.float64, device=self.device)
+        self.dipoles = self.transfer = None
         if self.topo is not None and self.topo.n_dihedrals:
             nd = self.topo.n_dihedrals
             self.dipoles = torch.zeros((nd, 4, 3), dtype=torch.float32, device=self.device)
             self.transfer = torch.zeros((nd, 6, 3, 3), dtype=torch.float32, device=self.device)
+        self.plan = None
+        if fused and self.topo is not None and packed is not None:
+            self.plan = self._make_plan(packed, max_block_beads)
         self.graph = None
-        # kernels of this library launched per outer step (cuFFT's own
-        # kernels and memsets not counted): 2 outer kicks, per inner step one
-        # kick/drift plus one per bonded term kind, one closing kick, and the
-        # field step (paint, paint finalize, k-space, readout) [+ PIC: paint,
-        # finalize, k-space, readout]
+        self.field_sums = torch.zeros(8, dtype=torch.float64, device=self.device)
+        self.thermo_args = None
+        self.baro_args = None
+        self.counter = torch.zeros(4, dtype=torch.int32, device=self.device)
+        self.state = torch.zeros(16, dtype=torch.float64, device=self.device)
+        self.ws_md = _lib.new_workspace(self.device)
+        self.names = None
         t = self.topo
         kinds = 0 if t is None else (int(t.n_bonds > 0) + int(t.n_angles > 0)
                                      + int(t.n_dihedrals > 0))
-        self.launches_per_step = (2 + self.respa * (1 + kinds) + 1 + 4
-                                  + (4 if charges is not None else 0))
+        # kernels of this library per outer step (cuFFT's own kernels and
+        # memsets not counted): field step = paint, finalize, k-space, readout
+        field = 4 + (4 if charges is not None else 0)
+        if self.plan is not None:
+            self.launches_per_step = 1 + field + 1
+        else:
+            self.launches_per_step = 2 + self.respa * (1 + kinds) + 1 + field
+
+    def _make_plan(self, packed, max_block_beads):
+        (b2a, b2b, b2r, b2k, b3a, b3b, b3c, b3t, b3k,
+         b4a, b4b, b4c, b4d, coeff, b4t, last) = packed
+        i32 = lambda x: np.ascontiguousarray(np.asarray(x, dtype=np.int32))
+        f32 = lambda x: np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+        arrs = [i32(b2a), i32(b2b), f32(b2r), f32(b2k), i32(b3a), i32(b3b), i32(b3c), f32(b3t),
+                f32(b3k), i32(b4a), i32(b4b), i32(b4c), i32(b4d),
+                f32(np.asarray(coeff).reshape(-1, 6, 5)), i32(b4t), i32(last)]
+        p = lambda a: a.ctypes.data_as(_lib.P)
+        h = _lib.P()
+        code = _lib.lib().hpf_respa_plan_create(
+            _lib.ctypes.byref(h), self.n, len(arrs[0]), *[p(a) for a in arrs[0:4]],
+            len(arrs[4]), *[p(a) for a in arrs[4:9]], len(arrs[9]), *[p(a) for a in arrs[9:16]],
+            int(max_block_beads))
+        if code == 7:  # a molecule larger than a CTA can hold
+            return None
+        if code:
+            raise _lib.HPFError("hpf_respa_plan_create", code)
+        return h
+
+    def couple(self, thermostat=True, barostat=None, seed=0, n_steps=100000, groups=None,
+               remove_com=True, target_pressure=1.0, beta=7.6e-4):
+        """Enable the CSVR thermostat (hymd/thermostat.py:111-219) and/or the
+        isotropic SCR barostat (hymd/barostat_scr.py:34-132) on the device.
+
+        The random numbers of `n_steps` outer steps are drawn now with
+        numpy's default_rng(seed), in the reference's order per step: the
+        barostat's normal(), then for each thermostat group normal() and
+        chisquare(3 N_g - 1).  groups: optional int array (0/1) of coupling
+        groups (default: one group of all particles)."""
+        cfg = self.config
+        every = int(cfg.n_b or 1)
+        ng = 1
+        self.group = None
+        counts = [float(self.n), 0.0]
+        if groups is not None:
+            g = np.asarray(groups, np.int32)
+            ng = int(g.max()) + 1
+            if ng > 2:
+                raise NotImplementedError("at most two thermostat coupling groups")
+            self.group = torch.as_tensor(g, device=self.device)
+            counts = [float(np.sum(g == 0)), float(np.sum(g == 1))]
+        stride = 1 + 2 * ng
+        rng = np.random.default_rng(seed)
+        table = np.zeros((n_steps, stride))
+        for s in range(n_steps):
+            if (s + 1) % every:
+                continue
+            if barostat:
+                table[s, 0] = rng.normal()
+            if thermostat:
+                for gi in range(ng):
+                    table[s, 1 + 2 * gi] = rng.normal()
+                    table[s, 2 + 2 * gi] = rng.chisquare(3 * int(counts[gi]) - 1)
+        self.randoms = torch.as_tensor(table.reshape(-1), device=self.device)
+        dt_o = self.respa * self.dt
+        if thermostat:
+            a = _lib.CsvrArgs()
+            a.n_groups, a.remove_com, a.n_steps, a.stride = ng, int(remove_com), n_steps, stride
+            a.offset, a.advance, a.every = 1, 1, every
+            a.count[0], a.count[1] = counts
+            a.mass, a.gas_constant = self.mass, cfg.gas_constant
+            a.target_temperature = float(cfg.target_temperature)
+            a.c = float(np.exp(-dt_o / cfg.tau))
+            self.thermo_args = a
+        if barostat:
+            if barostat != "isotropic":
+                raise NotImplementedError("device barostat: isotropic SCR")
+            b = _lib.ScrArgs()
+            b.n_types, b.n_steps, b.stride = self.T, n_steps, stride
+            b.advance = 0 if thermostat else 1
+            b.every = every
+            types = self.types.cpu().numpy()
+            m = list(cfg.m) if cfg.m else [1.0] * self.T
+            for t in range(self.T):
+                b.mass_count[t] = m[t] * float(np.sum(types == t))
+            b.mass, b.gas_constant = self.mass, cfg.gas_constant
+            b.target_temperature = float(cfg.target_temperature)
+            b.target_pressure = float(target_pressure)
+            b.beta, b.tau_p, b.dt_outer, b.n_b = beta, float(cfg.tau_p), dt_o, float(every)
+            self.baro_args = b
+        self.launches_per_step += (3 if thermostat else 0) + (3 if barostat else 0)
+
+    def _thermostat(self, st):
+        _lib.call("hpf_csvr", _lib.ptr(self.v), _lib.ptr(self.group), self.n,
+                  _lib.ctypes.byref(self.thermo_args), _lib.ptr(self.randoms),
+                  _lib.ptr(self.counter), _lib.ptr(self.state), _lib.ptr(self.ws_md),
+                  _lib.ptr(self.err), st)
+
+    def _barostat(self, st):
+        _lib.call("hpf_scr_isotropic", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.v), self.n,
+                  _lib.ptr(self.field_sums), _lib.ptr(self.bonded_out),
+                  _lib.ctypes.byref(self.baro_args), _lib.ptr(self.randoms),
+                  _lib.ptr(self.counter), _lib.ptr(self.state), _lib.ptr(self.ws_md),
+                  _lib.ptr(self.err), st)
+
+    def box_now(self):
+        return self.box.cpu().numpy().copy()
+
+    def plan_info(self):
+        if self.plan is None:
+            return None
+        a, b, c = _lib.I(), _lib.I(), _lib.I()
+        _lib.call("hpf_respa_plan_info", self.plan, _lib.ctypes.byref(a), _lib.ctypes.byref(b),
+                  _lib.ctypes.byref(c))
+        return dict(mol_blocks=a.value, free_beads=b.value, max_block_beads=c.value)
+
+    def __del__(self):
+        if getattr(self, "plan", None) is not None:
+            try:
+                _lib.lib().hpf_respa_plan_destroy(self.plan)
+            except Exception:
+                pass
+            self.plan = None
 
     # ------------------------------------------------------------------
     def _slow_forces(self):
@@ -83,7 +217,7 @@ class RespaMD:
         t = self.topo
         if t is None:
             return
-        err = _lib.ctypes.c_void_p(self.err.data_ptr())
+        err = _lib.ptr(self.err)
         box = _lib.ptr(self.box)
         if t.n_bonds:
             _lib.call("hpf_bonds", _lib.ptr(self.f_bond), _lib.ptr(self.r), self.n, box,
@@ -120,11 +254,25 @@ class RespaMD:
         """Bonded and slow forces at the initial positions (main.py:494-588)."""
         st = _lib.stream_ptr()
         self._bonded(st, 0)
-        self._field(st)
+        if self.topo is not None:
+            self.f_b.copy_(self.f_bond)
+            self.f_b.add_(self.f_angle)
+            self.f_b.add_(self.f_dih)
+        self._field(st, self.field_sums)
+        if self.baro_args is not None:
+            # the barostat reads the bonded virials of the last inner step
+            for k, ws in ((0, self.ws_bond), (4, self.ws_angle)):
+                self.bonded_out[k:k + 4].copy_(ws[:4])
 
-    def step(self):
-        """One outer rRESPA step (launch sequence only; no host sync)."""
-        st = _lib.stream_ptr()
+    def _inner_fused(self, st):
+        fs = self._slow_forces()
+        arr = (_lib.P * len(fs))(*[_lib.ptr(f) for f in fs])
+        _lib.call("hpf_respa_step", self.plan, _lib.ptr(self.r), _lib.ptr(self.v),
+                  _lib.ptr(self.f_b), arr, len(fs), self.mass, self.dt, self.respa,
+                  _lib.ptr(self.box), _lib.ptr(self.dipoles), _lib.ptr(self.transfer),
+                  _lib.ptr(self.bonded_out), _lib.ptr(self.err), st)
+
+    def _inner_unfused(self, st):
         fb, fa, fd = self._bonded_ptrs()
         self._outer_kick(st)
         for inner in range(self.respa):
@@ -134,8 +282,22 @@ class RespaMD:
             self._bonded(st, 1 if inner == self.respa - 1 else 0)
         _lib.call("hpf_inner_kick_drift", _lib.ptr(self.r), _lib.ptr(self.v), fb, fa, fd, self.n,
                   self.mass, self.dt, 1, 0, None, st)
-        self._field(st)
+
+    def step(self):
+        """One outer rRESPA step (launch sequence only; no host sync)."""
+        st = _lib.stream_ptr()
+        if self.plan is not None:
+            self._inner_fused(st)
+        else:
+            self._inner_unfused(st)
+            if self.baro_args is not None:
+                raise NotImplementedError("the device barostat needs the fused inner loop")
+        if self.baro_args is not None:
+            self._barostat(st)
+        self._field(st, self.field_sums)
         self._outer_kick(st)
+        if self.thermo_args is not None:
+            self._thermostat(st)
 
     def capture(self):
         """Record one outer step in a CUDA graph (after a warm-up step)."""
@@ -161,6 +323,9 @@ class RespaMD:
     # ------------------------------------------------------------------
     def energies(self):
         """(bond, angle, dihedral) energies of the last inner step (FP64)."""
+        if self.plan is not None:
+            o = self.bonded_out.cpu().numpy()
+            return [float(o[0]), float(o[4]), float(o[8])]
         out = []
         t = self.topo
         for ws, n in ((self.ws_bond, t.n_bonds if t else 0), (self.ws_angle, t.n_angles if t else 0),

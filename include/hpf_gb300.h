@@ -108,6 +108,24 @@ int hpf_kspace_force(hpf_ctx* ctx, const void* phi_k_raw, void* force_k,
 int hpf_kspace_sums(hpf_ctx* ctx, const void* phi_fourier, const void* psi_k,
                     const double* type_charges, double* sums, void* stream);
 
+/* FP64 energies and pressure sums of the current positions (the quantities
+ * of compute_field_and_kinetic_energy, hymd/field.py:619-703, and of
+ * comp_pressure, hymd/pressure.py:84-121).  The fixed-point densities (and,
+ * when charges != NULL, the charge density) are converted to double grids,
+ * transformed by an FP64 cuFFT and reduced in FP64 over the half spectrum.
+ * out: device double[32]:
+ *   out[0]    A   = sum_{k!=0} w_k sum_ij Q_ij Re(phi~_i conj phi~_j)
+ *   out[1+d]  B_d = sum_{k!=0} w_k k_d^2 (same)
+ *   out[4]    sum_k w_k Re(rho_k conj psi_k)   (W_elec = V/2 out[4] - E_self)
+ *   out[5]    sum_k w_k sum_t q_t Re(psi_k conj phi~_t)   (type_charges q_t)
+ *   out[6+d]  the same weighted by k_d^2
+ *   out[16+t] mean of phi_t
+ * so that W = V w(mean phi) + V/2 A.  Allocates its FP64 buffers and plan
+ * on first use (not capturable then). */
+int hpf_energy_fp64(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_t n,
+                    const double* type_mass, const float* charges, const double* type_charges,
+                    double elec_factor, double* out, void* stream);
+
 /* comp_laplacian (hymd/field.py:406-425): lap_out[t][d] = c2r(-k_d^2
  * phi_fourier[t]) for all T types and d = 0..2.  lap_out: float[T][3][M]. */
 int hpf_laplacian(hpf_ctx* ctx, const void* phi_fourier, float* lap_out, void* stream);
@@ -183,6 +201,87 @@ int hpf_inner_kick_drift(float* r, float* v, const float* fb, const float* fa,
  * workspace, HPF_OUT_DOUBLES).  Used for csum-style grid reductions
  * (hymd/field.py:693, 699; hymd/pressure.py:100-121). */
 int hpf_sum_dot(const float* x, const float* y, int64_t n, double* out, void* stream);
+/* ---- fused rRESPA inner loop (hymd/main.py:802-887) -----------------------
+ * A plan groups the beads joined by bonded terms into blocks of whole
+ * molecules (connected components of the terms) of at most max_block_beads
+ * beads, held in shared memory by one CTA each; beads in no term are "free".
+ * All topology arrays are HOST arrays in the packed form of prepare_bonds
+ * (hymd/force.py:573-728): int32 indices, float32 parameters, coeff
+ * float[D][6][5].  Returns HPF_ERR_NOT_IMPLEMENTED when one molecule exceeds
+ * the shared-memory capacity of a CTA (about 6400 beads); callers then use
+ * the per-term entry points above. */
+typedef struct hpf_respa_plan hpf_respa_plan;
+int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n_beads, int64_t nb, const int32_t* bond_a,
+                          const int32_t* bond_b, const float* bond_r0, const float* bond_k,
+                          int64_t na, const int32_t* ang_a, const int32_t* ang_b,
+                          const int32_t* ang_c, const float* ang_t0, const float* ang_k,
+                          int64_t nd, const int32_t* dih_a, const int32_t* dih_b,
+                          const int32_t* dih_c, const int32_t* dih_d, const float* dih_coeff,
+                          const int32_t* dih_type, const int32_t* dih_last, int max_block_beads);
+int hpf_respa_plan_destroy(hpf_respa_plan* plan);
+int hpf_respa_plan_info(const hpf_respa_plan* plan, int* n_mol_blocks, int* n_free,
+                        int* max_block_beads);
+/* One launch: first outer half kick v += 0.5 respa_inner dt F_s / mass for
+ * each slow force array (field, PIC, dipole, in that order, main.py:802-827),
+ * then respa_inner x [v += 0.5 dt F_b/mass; r = mod(r + dt v, box); F_b =
+ * bonded forces(r); v += 0.5 dt F_b/mass] (main.py:830-887).  f_bonded
+ * (float[N][3]) carries the bonded force between calls and must hold the
+ * bonded force of the current positions on entry (zero for free beads).
+ * dipoles/transfer (may both be NULL) receive the CBT dipoles of the last
+ * inner step (dipole_flag = 1 there, as main.py:863-866).  out (device
+ * double[9], may be NULL) = {E_bond, bond_pr[3], E_angle, angle_pr[3],
+ * E_dihedral} of the last inner step.  box: DEVICE double[3]. */
+int hpf_respa_step(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
+                   const float* const* slow_forces, int n_slow, double mass, double dt,
+                   int respa_inner, const double* box, float* dipoles, float* transfer,
+                   double* out, int* d_err, void* stream);
+
+/* ---- thermostat / barostat on the device -----------------------------------
+ * The random numbers are drawn on the host in the reference's order (numpy
+ * Generator: barostat normal(), then per thermostat group normal() and
+ * chisquare(N_f - 1)) into a device table with one row per outer step; a
+ * device step counter selects the row, so captured graphs replay them. */
+typedef struct {
+    int n_groups;       /* coupling groups, 1 or 2 (group ids from `group`)      */
+    int remove_com;     /* remove / restore each group's centre-of-mass velocity */
+    int n_steps;        /* rows in the random table                              */
+    int stride;         /* doubles per row                                       */
+    int offset;         /* row[offset + 2g] = R, row[offset + 2g + 1] = chi^2    */
+    int advance;        /* increment the step counter afterwards                 */
+    int every;          /* act when (step + 1) % every == 0 (n_b)                */
+    int pad;
+    double count[2];    /* particles per group                                   */
+    double mass, gas_constant, target_temperature;
+    double c;           /* exp(-dt_outer / tau)                                  */
+} HpfCsvrArgs;
+
+typedef struct {
+    int n_types, n_steps, stride, advance;
+    int every, pad[3];
+    double mass_count[16];  /* m_t * N_t: paint mass times particle count       */
+    double mass, gas_constant, target_temperature;
+    double target_pressure; /* bar                                              */
+    double beta;            /* isothermal compressibility (1/bar)               */
+    double tau_p, dt_outer, n_b;
+} HpfScrArgs;
+
+/* csvr_thermostat (hymd/thermostat.py:111-219) for up to two coupling groups.
+ * state: device double[16] ([4g] alpha, [4g+1..3] COM velocity, [8+g]
+ * accumulated thermostat work).  ws: workspace (HPF_OUT_DOUBLES). */
+int hpf_csvr(float* v, const int32_t* group, int64_t n, const HpfCsvrArgs* args,
+             const double* randoms, int* counter, double* state, double* ws, int* d_err,
+             void* stream);
+/* Stochastic cell rescaling, isotropic (hymd/barostat_scr.py:34-132): the
+ * pressure from field_sums (device double[4] = A, B_xyz of the last field
+ * evaluation, see hpf_kspace_force), bonded_out (device double[9] of
+ * hpf_respa_step) and the kinetic energy of v; then box (the context's device
+ * box state, kept in float32 values as the reference does) and positions are
+ * scaled by alpha.  state[12] = alpha, state[13] = P (bar). */
+int hpf_scr_isotropic(hpf_ctx* ctx, float* r, const float* v, int64_t n,
+                      const double* field_sums, const double* bonded_out,
+                      const HpfScrArgs* args, const double* randoms, int* counter,
+                      double* state, double* ws, int* d_err, void* stream);
+
 /* Sum over particles of v^2 into out[0] (device workspace, HPF_OUT_DOUBLES);
  * KE = mass/2 * out[0]. */
 int hpf_sum_v2(const float* v, int64_t n, double* out, void* stream);
