@@ -79,7 +79,7 @@ class CsvrArgs(ctypes.Structure):
 class ScrArgs(ctypes.Structure):
     """HpfScrArgs of include/hpf_gb300.h."""
     _fields_ = [("n_types", I), ("n_steps", I), ("stride", I), ("advance", I), ("every", I),
-                ("pad", I * 3), ("mass_count", D * 16), ("mass", D), ("gas_constant", D),
+                ("pad", I * 3), ("half_mQm", D), ("mass", D), ("gas_constant", D),
                 ("target_temperature", D), ("target_pressure", D), ("beta", D), ("tau_p", D),
                 ("dt_outer", D), ("n_b", D)]
 

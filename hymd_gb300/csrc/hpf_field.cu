@@ -167,7 +167,7 @@ __global__ void k_kspace_force(const float2* __restrict__ phi_raw, float2* __res
         for (int j = 0; j < TM; ++j) Q[i * TM + j] = (i < T && j < T) ? fun->Q[i * T + j] : 0.0f;
     }
     const float s2h = fun->sigma2_half;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
          idx += (int64_t)gridDim.x * blockDim.x) {
         float kx, ky, kz, gx, gy, gz, wk;
@@ -206,14 +206,14 @@ __global__ void k_kspace_force(const float2* __restrict__ phi_raw, float2* __res
             o[2 * Mc] = make_float2(gz * v.y, -gz * v.x);
         }
         if (sums && idx != 0) {
-            const double wq = (double)(wk * q);
+            const float wq = wk * q;
             acc[0] += wq;
-            acc[1] += wq * (double)(kx * kx);
-            acc[2] += wq * (double)(ky * ky);
-            acc[3] += wq * (double)(kz * kz);
+            acc[1] = fmaf(wq, kx * kx, acc[1]);
+            acc[2] = fmaf(wq, ky * ky, acc[2]);
+            acc[3] = fmaf(wq, kz * kz, acc[3]);
         }
     }
-    if (sums) grid_reduce_store<4>(acc, partials, ticket, sums, false);
+    if (sums) grid_reduce_store_f<4>(acc, partials, ticket, sums);
 }
 
 template <int TT>

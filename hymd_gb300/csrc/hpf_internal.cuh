@@ -159,6 +159,66 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double* smem /* K*3
     }
 }
 
+// Same reduction for FP32 per-thread partial sums (a thread adds only a few
+// terms): the warp sums in FP32, everything above the warp in FP64.  GB300's
+// FP64 rate is a small fraction of its FP32 rate, so hot kernels keep FP64
+// arithmetic out of the per-element path.  Returns true on thread 0 of the
+// last block, after out[] has been written (for a fused epilogue).
+template <int K>
+__device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* partials,
+                                                    unsigned int* ticket, double* out) {
+    __shared__ double red[K * 32];
+    __shared__ bool is_last;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) vf[k] += __shfl_down_sync(0xffffffffu, vf[k], o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) red[k * 32 + warp] = (double)vf[k];
+    }
+    __syncthreads();
+    double v[K];
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double x = lane < nw ? red[k * 32 + lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            v[k] = x;
+        }
+    }
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) partials[(size_t)blockIdx.x * K + k] = v[k];
+        __threadfence();
+        unsigned int t = atomicAdd(ticket, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    for (unsigned int bI = threadIdx.x; bI < gridDim.x; bI += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] += ((volatile double*)partials)[(size_t)bI * K + k];
+    }
+    __syncthreads();
+    block_reduce<K>(acc, red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) out[k] = acc[k];
+        *ticket = 0u;
+        return true;
+    }
+    return false;
+}
+
 // Deterministic grid-wide sum: each block stores its K partials; the last
 // block to finish (ticket) adds them -- thread j takes blocks j, j+B, ...,
 // then a fixed tree -- and writes out[k] (overwrite or accumulate).  The

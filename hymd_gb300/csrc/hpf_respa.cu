@@ -49,7 +49,10 @@ struct hpf_respa_plan {
 
 namespace {
 
-constexpr int kThreads = 256;
+// 128 threads per block: molecule blocks are small (a few hundred beads), so
+// several of them share an SM and their __syncthreads-separated phases
+// overlap.
+constexpr int kThreads = 128;
 constexpr int kMaxSlow = 4;
 constexpr int kOut = 9;  // E_bond, pr_bond[3], E_angle, pr_angle[3], E_dihedral
 
@@ -71,9 +74,9 @@ k_respa(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v, float* _
         double* out, int* err) {
     extern __shared__ float smem[];
     const Box bx = load_box(box);
-    double acc[kOut];
+    float acc[kOut];  // a thread adds a few terms; FP64 from the warp sums up
 #pragma unroll
-    for (int k = 0; k < kOut; ++k) acc[k] = 0.0;
+    for (int k = 0; k < kOut; ++k) acc[k] = 0.0f;
     const int tid = threadIdx.x;
     if ((int)blockIdx.x < p.n_mol_blocks) {
         const int b = blockIdx.x;
@@ -123,10 +126,10 @@ k_respa(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v, float* _
                 atomicAdd(fs + 3 * ij.y + 1, fa.y);
                 atomicAdd(fs + 3 * ij.y + 2, fa.z);
                 if (last_it) {
-                    acc[0] += (double)e;
-                    acc[1] += (double)vir.x;
-                    acc[2] += (double)vir.y;
-                    acc[3] += (double)vir.z;
+                    acc[0] += e;
+                    acc[1] += vir.x;
+                    acc[2] += vir.y;
+                    acc[3] += vir.z;
                 }
             }
             for (int t = a0 + tid; t < a1; t += kThreads) {
@@ -148,10 +151,10 @@ k_respa(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v, float* _
                 atomicAdd(fs + 3 * q.y + 1, ga.y + gc.y);
                 atomicAdd(fs + 3 * q.y + 2, ga.z + gc.z);
                 if (last_it) {
-                    acc[4] += (double)e;
-                    acc[5] += (double)vir.x;
-                    acc[6] += (double)vir.y;
-                    acc[7] += (double)vir.z;
+                    acc[4] += e;
+                    acc[5] += vir.x;
+                    acc[6] += vir.y;
+                    acc[7] += vir.z;
                 }
             }
             for (int t = d0 + tid; t < d1; t += kThreads) {
@@ -179,7 +182,7 @@ k_respa(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v, float* _
                     atomicAdd(fs + 3 * li[j] + 1, F[j].y);
                     atomicAdd(fs + 3 * li[j] + 2, F[j].z);
                 }
-                if (last_it) acc[8] += (double)e;
+                if (last_it) acc[8] += e;
             }
             __syncthreads();
         }
@@ -208,7 +211,7 @@ k_respa(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v, float* _
             }
         }
     }
-    if (out) grid_reduce_store<kOut>(acc, p.partials, p.ticket, out, false);
+    if (out) grid_reduce_store_f<kOut>(acc, p.partials, p.ticket, out);
 }
 
 // ------------------------------------------------------------- planner ---
@@ -372,7 +375,7 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
     p->max_block_beads = mx;
     p->smem = sizeof(float) * 9 * (size_t)std::max(mx, 1);
     int nfb = (p->n_free + kThreads - 1) / kThreads;
-    nfb = std::min(nfb, std::max(1, 152 * 4 - B));
+    nfb = std::min(nfb, std::max(1, 152 * 8 - B));
     if (p->n_free == 0) nfb = 0;
     p->n_free_blocks = nfb;
     int st = HPF_OK;

@@ -89,6 +89,7 @@ class ParticleMesh:
             _lib.call("hpf_ctx_set_functional", self._h, _lib.dvec(Q.reshape(-1)), _lib.dvec(b),
                       float(c), float(sigma))
             self._functional = key
+            self._functional_Q = Q
         return Q, b, c, sigma
 
     def check_errors(self):

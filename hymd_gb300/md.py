@@ -26,7 +26,7 @@ from .force import BondedTopology
 
 class RespaMD:
     def __init__(self, positions, velocities, types, config, hamiltonian, topology=None,
-                 charges=None, device="cuda", fused=True, max_block_beads=512):
+                 charges=None, device="cuda", fused=True, max_block_beads=192):
         self.device = torch.device(device)
         self.config = config
         self.r = torch.as_tensor(np.asarray(positions, np.float32), device=self.device).contiguous()
@@ -161,15 +161,16 @@ class RespaMD:
             b.advance = 0 if thermostat else 1
             b.every = every
             types = self.types.cpu().numpy()
-            m = list(cfg.m) if cfg.m else [1.0] * self.T
-            for t in range(self.T):
-                b.mass_count[t] = m[t] * float(np.sum(types == t))
+            m = np.asarray(list(cfg.m) if cfg.m else [1.0] * self.T, dtype=np.float64)
+            mc = m * np.bincount(types, minlength=self.T)[: self.T]
+            Q = np.asarray(self.pm._functional_Q, dtype=np.float64)
+            b.half_mQm = float(0.5 * mc @ Q @ mc)
             b.mass, b.gas_constant = self.mass, cfg.gas_constant
             b.target_temperature = float(cfg.target_temperature)
             b.target_pressure = float(target_pressure)
             b.beta, b.tau_p, b.dt_outer, b.n_b = beta, float(cfg.tau_p), dt_o, float(every)
             self.baro_args = b
-        self.launches_per_step += (3 if thermostat else 0) + (3 if barostat else 0)
+        self.launches_per_step += (2 if thermostat else 0) + (2 if barostat else 0)
 
     def _thermostat(self, st):
         _lib.call("hpf_csvr", _lib.ptr(self.v), _lib.ptr(self.group), self.n,

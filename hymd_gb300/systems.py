@@ -111,8 +111,12 @@ def lipid_membrane(seed=2, n_lipids=6000, n_water=90000, box=27.0, mesh=64):
             pos += rng.normal(0.0, 0.1, size=(12, 3))
             lip.append(pos)
     lip = np.concatenate(lip)
-    w = rng.uniform(0, box, size=(n_water * 2, 3))
-    w = w[np.abs(w[:, 2] - zc) > 2.6][:n_water]
+    # solvent uniformly in the volume outside the bilayer slab |z - zc| <= 2.6
+    w = np.empty((0, 3))
+    while len(w) < n_water:
+        c = rng.uniform(0, box, size=(n_water, 3))
+        w = np.concatenate([w, c[np.abs(c[:, 2] - zc) > 2.6]])
+    w = w[:n_water]
     r = np.mod(np.concatenate([lip, w]), L).astype(np.float32)
     uniq = ["C", "G", "N", "P", "W"]
     tmap = {u.encode(): i for i, u in enumerate(uniq)}

@@ -258,7 +258,8 @@ typedef struct {
 typedef struct {
     int n_types, n_steps, stride, advance;
     int every, pad[3];
-    double mass_count[16];  /* m_t * N_t: paint mass times particle count       */
+    double half_mQm;        /* 1/2 mc.Q.mc with mc_t = m_t N_t (paint mass x count),
+                               so the k = 0 densities are mc_t / V               */
     double mass, gas_constant, target_temperature;
     double target_pressure; /* bar                                              */
     double beta;            /* isothermal compressibility (1/bar)               */
