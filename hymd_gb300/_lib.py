@@ -52,7 +52,7 @@ _SIGNATURES = {
     "hpf_laplacian": [P, P, P, P],
     "hpf_energy_fp64": [P, P, P, I64, ctypes.POINTER(D), P, ctypes.POINTER(D), D, P, P],
     "hpf_readout": [P, P, P, P, I64, P, P],
-    "hpf_field_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P],
+    "hpf_field_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P, P],
     "hpf_pic_step": [P, P, P, I64, D, P, P, P, P, P, P, P],
     "hpf_bonds": [P, P, I64, P, P, P, P, P, I64, P, P, P],
     "hpf_angles": [P, P, I64, P, P, P, P, P, P, I64, P, P, P],
@@ -64,7 +64,8 @@ _SIGNATURES = {
                               P, P, P, P, P, P, P, I],
     "hpf_respa_plan_destroy": [P],
     "hpf_respa_plan_info": [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
-    "hpf_respa_step": [P, P, P, P, ctypes.POINTER(P), I, D, D, I, P, P, P, P, P, P],
+    "hpf_respa_step": [P, P, P, P, ctypes.POINTER(P), I, D, D, I, P, P, P, P, P, P, P, P, P,
+                       P, P, P],
     "hpf_sum_dot": [P, P, I64, P, P],
     "hpf_sum_v2": [P, I64, P, P],
 }
@@ -85,7 +86,7 @@ class ScrArgs(ctypes.Structure):
 
 
 _SIGNATURES.update({
-    "hpf_csvr": [P, P, I64, ctypes.POINTER(CsvrArgs), P, P, P, P, P, P],
+    "hpf_csvr": [P, P, I64, ctypes.POINTER(P), I, D, ctypes.POINTER(CsvrArgs), P, P, P, P, P, P],
     "hpf_scr_isotropic": [P, P, P, I64, P, P, ctypes.POINTER(ScrArgs), P, P, P, P, P, P],
 })
 

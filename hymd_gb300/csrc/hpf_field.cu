@@ -36,16 +36,28 @@ struct TypeScaleD {
 // One thread per particle; 8 CIC deposits as 64-bit fixed-point integer
 // atomics (weight * 2^32), so the accumulated grid is independent of the
 // order in which deposits land: the density is bit-deterministic.
-__global__ void k_paint(const float* __restrict__ pos, const int32_t* __restrict__ types,
+// With `scale` (a barostat's alpha, device double), the positions are first
+// rescaled in place, r = float(alpha) * r (hymd/barostat_scr.py:128).
+__global__ void k_paint(const float* pos, const int32_t* __restrict__ types,
                         const float* __restrict__ charges, int64_t n, int T,
                         const BoxState* __restrict__ bs, unsigned long long* __restrict__ acc,
-                        int64_t M, int* err) {
+                        int64_t M, int* err, const double* __restrict__ scale) {
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
+    const float al = scale ? (float)*scale : 1.0f;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        if (scale) {
+            x = x * al;
+            y = y * al;
+            z = z * al;
+            float* pw = const_cast<float*>(pos);
+            pw[3 * i] = x;
+            pw[3 * i + 1] = y;
+            pw[3 * i + 2] = z;
+        }
         if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
             hpf_flag(err, HPF_ERR_NONFINITE);
             continue;
@@ -504,14 +516,15 @@ int launch_kspace_force(hpf_ctx* c, const float2* phi_raw, float2* force_k, floa
 }
 
 int do_paint(hpf_ctx* c, const float* pos, const int32_t* types, const float* charges,
-             int64_t n, int G, const TypeScale& sc, float* out, cudaStream_t st) {
+             int64_t n, int G, const TypeScale& sc, float* out, cudaStream_t st,
+             const double* scale = nullptr) {
     // G = number of grids (T for densities; 1 for charges, painted into the
     // accumulator slot after the T density slots)
     unsigned long long* acc = c->d_acc + (charges ? (int64_t)c->T * c->M : 0);
     if (n > 0) {
         k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, types, charges, n,
                                                            charges ? 1 : c->T, c->d_box, acc,
-                                                           c->M, c->d_err);
+                                                           c->M, c->d_err, scale);
         HPF_LAUNCH_CHECK();
     }
     if (c->M % 4 == 0) {  // float4 groups never straddle two grids
@@ -808,12 +821,12 @@ int hpf_energy_fp64(hpf_ctx* c, const float* pos, const int32_t* types, int64_t 
     // densities into accumulator slots 0..T-1, charges into slot T
     if (n > 0) {
         k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, types, nullptr, n, T, c->d_box,
-                                                           c->d_acc, c->M, c->d_err);
+                                                           c->d_acc, c->M, c->d_err, nullptr);
         HPF_LAUNCH_CHECK();
         if (charges) {
             k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(
                 pos, nullptr, charges, n, 1, c->d_box, c->d_acc + (int64_t)T * c->M, c->M,
-                c->d_err);
+                c->d_err, nullptr);
             HPF_LAUNCH_CHECK();
         }
     }
@@ -869,14 +882,16 @@ int hpf_readout(hpf_ctx* c, const float* force_mesh, const float* pos, const int
     return HPF_OK;
 }
 
-int hpf_field_step(hpf_ctx* c, const float* pos, const int32_t* types, int64_t n,
-                   const double* type_mass, float* force, double* sums, void* stream) {
+int hpf_field_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
+                   const double* type_mass, float* force, double* sums, const double* pos_scale,
+                   void* stream) {
     if (!c || !type_mass || n < 0 || (n > 0 && (!pos || !types || !force))) return HPF_ERR_ARG;
     cudaStream_t st = as_stream(stream);
     TypeScale sc;
     for (int t = 0; t < c->T; ++t) sc.s[t] = (float)type_mass[t];
     int r;
-    if ((r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st)) != HPF_OK) return r;
+    if ((r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale)) != HPF_OK)
+        return r;
     if ((r = exec_r2c(c, c->d_grid, c->d_spec_phi, c->T, st)) != HPF_OK) return r;
     if ((r = launch_kspace_force(c, c->d_spec_phi, c->d_spec, nullptr, nullptr, sums, st)) !=
         HPF_OK)

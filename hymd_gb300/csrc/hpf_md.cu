@@ -100,16 +100,26 @@ __global__ void k_sum_dot(const float* __restrict__ x, const float* __restrict__
 // form, hymd/thermostat.py:167-219) from the kinetic energy with the
 // centre-of-mass motion removed.  randoms[step * stride + offset + 2g] = R,
 // [.. + 1] = chi^2_{Nf-1}.
-__global__ void k_csvr_sums_alpha(const float* __restrict__ v, const int32_t* __restrict__ group,
-                                  int64_t n, double* ws, HpfCsvrArgs a,
-                                  const double* __restrict__ randoms, int* counter, double* state,
-                                  int* err) {
+// The preceding outer half kick v += 0.5 dt_o F_q/m (forces in `kick`) is
+// applied first, in the same pass.
+__global__ void k_csvr_sums_alpha(float* __restrict__ v, const int32_t* __restrict__ group,
+                                  int64_t n, ForceList kick, float kick_h, double* ws,
+                                  HpfCsvrArgs a, const double* __restrict__ randoms, int* counter,
+                                  double* state, int* err) {
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const float m = (float)a.mass;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
+        float w[3];
+        for (int d = 0; d < 3; ++d) {
+            float x = v[3 * i + d];
+            for (int q = 0; q < kick.n; ++q) x = x + kick_h * (kick.f[q][3 * i + d] / m);
+            w[d] = x;
+            if (kick.n) v[3 * i + d] = x;
+        }
         const int g = group ? group[i] : 0;
         if (g < 0 || g > 1) continue;
-        const float x = v[3 * i], y = v[3 * i + 1], z = v[3 * i + 2];
+        const float x = w[0], y = w[1], z = w[2];
         acc[4 * g + 0] += x;
         acc[4 * g + 1] += y;
         acc[4 * g + 2] += z;
@@ -251,15 +261,23 @@ int hpf_inner_kick_drift(float* r, float* v, const float* fb, const float* fa, c
     return HPF_OK;
 }
 
-int hpf_csvr(float* v, const int32_t* group, int64_t n, const HpfCsvrArgs* args,
-             const double* randoms, int* counter, double* state, double* ws, int* d_err,
-             void* stream) {
-    if (!v || n < 0 || !args || !randoms || !counter || !state || !ws) return HPF_ERR_ARG;
+int hpf_csvr(float* v, const int32_t* group, int64_t n, const float* const* kick_forces,
+             int n_kick, double kick_dt, const HpfCsvrArgs* args, const double* randoms,
+             int* counter, double* state, double* ws, int* d_err, void* stream) {
+    if (!v || n < 0 || !args || !randoms || !counter || !state || !ws || n_kick < 0 ||
+        n_kick > kMaxForces || (n_kick > 0 && !kick_forces))
+        return HPF_ERR_ARG;
     if (args->n_groups < 1 || args->n_groups > 2 || (args->n_groups > 1 && !group))
         return HPF_ERR_ARG;
+    ForceList fl;
+    fl.n = n_kick;
+    for (int q = 0; q < n_kick; ++q) {
+        if (!kick_forces[q]) return HPF_ERR_ARG;
+        fl.f[q] = kick_forces[q];
+    }
     cudaStream_t st = as_stream(stream);
-    k_csvr_sums_alpha<<<reduce_grid_md(n), kThreads, 0, st>>>(v, group, n, ws, *args, randoms,
-                                                              counter, state, d_err);
+    k_csvr_sums_alpha<<<reduce_grid_md(n), kThreads, 0, st>>>(
+        v, group, n, fl, (float)(0.5 * kick_dt), ws, *args, randoms, counter, state, d_err);
     HPF_LAUNCH_CHECK();
     k_csvr_scale<<<grid_for(n), kThreads, 0, st>>>(v, group, n, state, args->remove_com);
     HPF_LAUNCH_CHECK();

@@ -2,18 +2,21 @@
 //
 // Bonded terms never couple different molecules, so the whole inner loop --
 // respa_inner x (half kick, drift, wrap, bonded forces, half kick) -- needs no
-// grid-wide synchronisation if each CTA owns whole molecules.  The planner
-// (host C++) finds the molecules as connected components of the bonded
-// terms, packs them into blocks of at most `max_block_beads` beads, and
-// rewrites every term with block-local bead indices.  One launch then:
-//   * molecule blocks: load positions, velocities and bonded forces of the
-//     block's beads into shared memory, apply the first outer half kick with
-//     the slow forces, run all inner steps on chip (shared-memory force
-//     accumulation, __syncthreads between phases), write back;
+// grid-wide synchronisation if a group of threads owns whole molecules.  The
+// planner (host C++) finds the molecules as connected components of the
+// bonded terms, packs them into groups of at most `max_group_beads` beads and
+// rewrites every term with group-local bead indices.  One launch then:
+//   * molecule groups: load positions, velocities and bonded forces of the
+//     group's beads into shared memory, apply the first outer half kick with
+//     the slow forces, run all inner steps on chip, write back.  Groups of up
+//     to 256 beads are run by one warp each (phases separated by __syncwarp);
+//     larger ones by a whole CTA (__syncthreads);
 //   * free beads (in no bonded term): per thread, the outer kick and
 //     respa_inner drift/wrap steps (their bonded force is zero).
 // Energies and virials of the last inner step (the ones the reference keeps,
-// main.py:964-973) are reduced in FP64 deterministically.
+// main.py:964-973) and sum v^2 are reduced in FP64 by the grid's last block,
+// which can also run the isotropic SCR barostat (hymd/barostat_scr.py:34-132)
+// right there, since the barostat follows the inner loop (main.py:889-963).
 #include <algorithm>
 #include <numeric>
 #include <vector>
@@ -23,21 +26,23 @@
 
 struct hpf_respa_plan {
     int64_t n_beads;
-    int n_mol_blocks;
+    int n_groups;        // molecule groups
     int n_free;
-    int max_block_beads;
+    int max_group_beads;
     int n_free_blocks;
-    size_t smem;
+    int warp_mode;       // 1: one warp per group, 0: one CTA per group
+    int has_dih;
+    size_t smem;         // dynamic shared memory per block
     // device arrays
-    int* blk_bead;    // [n_mol_blocks+1]
-    int* bead_ids;    // bonded beads, block-major
-    int* blk_bond;    // [n_mol_blocks+1]
+    int* grp_bead;    // [n_groups+1]
+    int* bead_ids;    // bonded beads, group-major
+    int* grp_bond;    // [n_groups+1]
     short2* bond_ij;  // local indices
     float2* bond_p;   // (r0, k)
-    int* blk_ang;
+    int* grp_ang;
     short4* ang_ijk;
     float2* ang_p;    // (t0, k)
-    int* blk_dih;
+    int* grp_dih;
     short4* dih_ijkl;
     float* dih_coeff;  // 30 per term
     int2* dih_tl;      // (type, last)
@@ -49,115 +54,135 @@ struct hpf_respa_plan {
 
 namespace {
 
-// 128 threads per block: molecule blocks are small (a few hundred beads), so
-// several of them share an SM and their __syncthreads-separated phases
-// overlap.
-constexpr int kThreads = 128;
+constexpr int kThreads = 128;  // 4 warps
+constexpr int kWarps = kThreads / 32;
 constexpr int kMaxSlow = 4;
-constexpr int kOut = 9;  // E_bond, pr_bond[3], E_angle, pr_angle[3], E_dihedral
+constexpr int kOut = 10;  // E_bond, pr_bond[3], E_angle, pr_angle[3], E_dihedral, sum v^2
+constexpr int kWarpMaxBeads = 256;
 
 struct SlowForces {
     const float* f[kMaxSlow];
     int n;
 };
 
+// Optional barostat run by the last block (all inner steps are done then).
+struct BaroFuse {
+    int on;
+    HpfScrArgs a;
+    const double* field;
+    const double* randoms;
+    int* counter;
+    BoxState* bs;
+    const Functional* fun;
+    double* state;
+};
+
+// np.mod(x, L), L > 0.  A drift moves a bead far less than a box length, so
+// x lies in (-L, 2L): then x - L (Sterbenz, exact) or x + L equals fmod's
+// result; anything else takes fmodf.
 __device__ __forceinline__ float wrapf(float x, float L) {
+    if (x >= 0.0f && x < L) return x;
+    if (x >= L && x < 2.0f * L) return x - L;
+    if (x < 0.0f && x > -L) return x + L;
     float m = fmodf(x, L);
     if (m < 0.0f) m += L;
     return m;
 }
 
-__global__ void __launch_bounds__(kThreads)
-k_respa(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v, float* __restrict__ fb,
-        SlowForces slow, float mass, float h_out, float hdt, float dt, int respa,
-        const double* __restrict__ box, float* __restrict__ dipoles, float* __restrict__ transfer,
-        double* out, int* err) {
-    extern __shared__ float smem[];
-    const Box bx = load_box(box);
-    float acc[kOut];  // a thread adds a few terms; FP64 from the warp sums up
-#pragma unroll
-    for (int k = 0; k < kOut; ++k) acc[k] = 0.0f;
-    const int tid = threadIdx.x;
-    if ((int)blockIdx.x < p.n_mol_blocks) {
-        const int b = blockIdx.x;
-        const int s0 = p.blk_bead[b], nb = p.blk_bead[b + 1] - s0;
-        float* rs = smem;            // [3*nb]
-        float* vs = smem + 3 * nb;   // [3*nb]
-        float* fs = smem + 6 * nb;   // [3*nb]
-        for (int e = tid; e < 3 * nb; e += kThreads) {
-            const int i = e / 3, d = e - 3 * i;
-            const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
-            float x = v[g];
-            for (int q = 0; q < slow.n; ++q) x = x + h_out * (slow.f[q][g] / mass);
+struct WarpSync {
+    __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+struct CtaSync {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
+// Group-local work shared by the warp and CTA variants.  `lane`/`width`
+// enumerate the threads of the group; `sync()` separates the phases.
+template <bool DIH, typename Sync>
+__device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int lane, int width,
+                                          float* rs, float* vs, float* fs, float* __restrict__ r,
+                                          float* __restrict__ v, float* __restrict__ fb,
+                                          const SlowForces& slow, float mass, float h_out,
+                                          float hdt, float dt, int respa, const Box& bx,
+                                          float* __restrict__ dipoles,
+                                          float* __restrict__ transfer, float (&acc)[kOut],
+                                          Sync sync) {
+    const int s0 = p.grp_bead[grp], nb = p.grp_bead[grp + 1] - s0;
+    for (int e = lane; e < 3 * nb; e += width) {
+        const int i = e / 3, d = e - 3 * i;
+        const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
+        float x = v[g];
+        for (int q = 0; q < slow.n; ++q) x = x + h_out * (slow.f[q][g] / mass);
+        vs[e] = x;
+        rs[e] = r[g];
+        fs[e] = fb[g];
+    }
+    sync();
+    const int b0 = p.grp_bond[grp], b1 = p.grp_bond[grp + 1];
+    const int a0 = p.grp_ang[grp], a1 = p.grp_ang[grp + 1];
+    const int d0 = DIH ? p.grp_dih[grp] : 0, d1 = DIH ? p.grp_dih[grp + 1] : 0;
+    for (int it = 0; it < respa; ++it) {
+        const bool last_it = it == respa - 1;
+        // closing half kick of the previous inner step (same forces), the
+        // opening half kick of this one, drift and wrap; clear forces
+        for (int e = lane; e < 3 * nb; e += width) {
+            const float a = fs[e] / mass;
+            float x = vs[e];
+            if (it > 0) x = x + hdt * a;
+            x = x + hdt * a;
             vs[e] = x;
-            rs[e] = r[g];
-            fs[e] = fb[g];
+            rs[e] = wrapf(rs[e] + dt * x, bx.L[e % 3]);
+            fs[e] = 0.0f;
         }
-        __syncthreads();
-        const int b0 = p.blk_bond[b], b1 = p.blk_bond[b + 1];
-        const int a0 = p.blk_ang[b], a1 = p.blk_ang[b + 1];
-        const int d0 = p.blk_dih[b], d1 = p.blk_dih[b + 1];
-        for (int it = 0; it < respa; ++it) {
-            const bool last_it = it == respa - 1;
-            // closing half kick of the previous inner step (same forces), the
-            // opening half kick of this one, drift and wrap; clear forces
-            for (int e = tid; e < 3 * nb; e += kThreads) {
-                const float a = fs[e] / mass;
-                float x = vs[e];
-                if (it > 0) x = x + hdt * a;
-                x = x + hdt * a;
-                vs[e] = x;
-                rs[e] = wrapf(rs[e] + dt * x, bx.L[e % 3]);
-                fs[e] = 0.0f;
+        sync();
+        for (int t = b0 + lane; t < b1; t += width) {
+            const short2 ij = p.bond_ij[t];
+            const float2 pr = p.bond_p[t];
+            float e;
+            V3 vir;
+            const V3 pa = v3(rs[3 * ij.x], rs[3 * ij.x + 1], rs[3 * ij.x + 2]);
+            const V3 pb = v3(rs[3 * ij.y], rs[3 * ij.y + 1], rs[3 * ij.y + 2]);
+            const V3 fa = bond_term(pa, pb, pr.x, pr.y, bx, e, vir);
+            atomicAdd(fs + 3 * ij.x, -fa.x);
+            atomicAdd(fs + 3 * ij.x + 1, -fa.y);
+            atomicAdd(fs + 3 * ij.x + 2, -fa.z);
+            atomicAdd(fs + 3 * ij.y, fa.x);
+            atomicAdd(fs + 3 * ij.y + 1, fa.y);
+            atomicAdd(fs + 3 * ij.y + 2, fa.z);
+            if (last_it) {
+                acc[0] += e;
+                acc[1] += vir.x;
+                acc[2] += vir.y;
+                acc[3] += vir.z;
             }
-            __syncthreads();
-            for (int t = b0 + tid; t < b1; t += kThreads) {
-                const short2 ij = p.bond_ij[t];
-                const float2 pr = p.bond_p[t];
-                float e;
-                V3 vir;
-                const V3 pa = v3(rs[3 * ij.x], rs[3 * ij.x + 1], rs[3 * ij.x + 2]);
-                const V3 pb = v3(rs[3 * ij.y], rs[3 * ij.y + 1], rs[3 * ij.y + 2]);
-                const V3 fa = bond_term(pa, pb, pr.x, pr.y, bx, e, vir);
-                atomicAdd(fs + 3 * ij.x, -fa.x);
-                atomicAdd(fs + 3 * ij.x + 1, -fa.y);
-                atomicAdd(fs + 3 * ij.x + 2, -fa.z);
-                atomicAdd(fs + 3 * ij.y, fa.x);
-                atomicAdd(fs + 3 * ij.y + 1, fa.y);
-                atomicAdd(fs + 3 * ij.y + 2, fa.z);
-                if (last_it) {
-                    acc[0] += e;
-                    acc[1] += vir.x;
-                    acc[2] += vir.y;
-                    acc[3] += vir.z;
-                }
+        }
+        for (int t = a0 + lane; t < a1; t += width) {
+            const short4 q = p.ang_ijk[t];
+            const float2 pr = p.ang_p[t];
+            const V3 pa = v3(rs[3 * q.x], rs[3 * q.x + 1], rs[3 * q.x + 2]);
+            const V3 pb = v3(rs[3 * q.y], rs[3 * q.y + 1], rs[3 * q.y + 2]);
+            const V3 pc = v3(rs[3 * q.z], rs[3 * q.z + 1], rs[3 * q.z + 2]);
+            V3 ga, gc, vir;
+            float e;
+            if (!angle_term(pa, pb, pc, pr.x, pr.y, bx, ga, gc, e, vir)) continue;
+            atomicAdd(fs + 3 * q.x, -ga.x);
+            atomicAdd(fs + 3 * q.x + 1, -ga.y);
+            atomicAdd(fs + 3 * q.x + 2, -ga.z);
+            atomicAdd(fs + 3 * q.z, -gc.x);
+            atomicAdd(fs + 3 * q.z + 1, -gc.y);
+            atomicAdd(fs + 3 * q.z + 2, -gc.z);
+            atomicAdd(fs + 3 * q.y, ga.x + gc.x);
+            atomicAdd(fs + 3 * q.y + 1, ga.y + gc.y);
+            atomicAdd(fs + 3 * q.y + 2, ga.z + gc.z);
+            if (last_it) {
+                acc[4] += e;
+                acc[5] += vir.x;
+                acc[6] += vir.y;
+                acc[7] += vir.z;
             }
-            for (int t = a0 + tid; t < a1; t += kThreads) {
-                const short4 q = p.ang_ijk[t];
-                const float2 pr = p.ang_p[t];
-                const V3 pa = v3(rs[3 * q.x], rs[3 * q.x + 1], rs[3 * q.x + 2]);
-                const V3 pb = v3(rs[3 * q.y], rs[3 * q.y + 1], rs[3 * q.y + 2]);
-                const V3 pc = v3(rs[3 * q.z], rs[3 * q.z + 1], rs[3 * q.z + 2]);
-                V3 ga, gc, vir;
-                float e;
-                if (!angle_term(pa, pb, pc, pr.x, pr.y, bx, ga, gc, e, vir)) continue;
-                atomicAdd(fs + 3 * q.x, -ga.x);
-                atomicAdd(fs + 3 * q.x + 1, -ga.y);
-                atomicAdd(fs + 3 * q.x + 2, -ga.z);
-                atomicAdd(fs + 3 * q.z, -gc.x);
-                atomicAdd(fs + 3 * q.z + 1, -gc.y);
-                atomicAdd(fs + 3 * q.z + 2, -gc.z);
-                atomicAdd(fs + 3 * q.y, ga.x + gc.x);
-                atomicAdd(fs + 3 * q.y + 1, ga.y + gc.y);
-                atomicAdd(fs + 3 * q.y + 2, ga.z + gc.z);
-                if (last_it) {
-                    acc[4] += e;
-                    acc[5] += vir.x;
-                    acc[6] += vir.y;
-                    acc[7] += vir.z;
-                }
-            }
-            for (int t = d0 + tid; t < d1; t += kThreads) {
+        }
+        if (DIH) {
+            for (int t = d0 + lane; t < d1; t += width) {
                 const short4 q = p.dih_ijkl[t];
                 const int2 tl = p.dih_tl[t];
                 const int li[4] = {q.x, q.y, q.z, q.w};
@@ -184,34 +209,124 @@ k_respa(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v, float* _
                 }
                 if (last_it) acc[8] += e;
             }
-            __syncthreads();
         }
-        // closing half kick of the last inner step, write back
-        for (int e = tid; e < 3 * nb; e += kThreads) {
-            const int i = e / 3, d = e - 3 * i;
-            const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
-            const float a = fs[e] / mass;
-            v[g] = vs[e] + hdt * a;
-            r[g] = rs[e];
-            fb[g] = fs[e];
-        }
-    } else {
-        // free beads: zero bonded force, so each inner step is a pure drift
-        const int fb0 = ((int)blockIdx.x - p.n_mol_blocks) * kThreads;
-        const int stride = p.n_free_blocks * kThreads;
-        for (int j = fb0 + tid; j < p.n_free; j += stride) {
-            const int64_t g = 3 * (int64_t)p.free_ids[j];
-            for (int d = 0; d < 3; ++d) {
-                float x = v[g + d];
-                for (int q = 0; q < slow.n; ++q) x = x + h_out * (slow.f[q][g + d] / mass);
-                float y = r[g + d];
-                for (int it = 0; it < respa; ++it) y = wrapf(y + dt * x, bx.L[d]);
-                v[g + d] = x;
-                r[g + d] = y;
-            }
+        sync();
+    }
+    // closing half kick of the last inner step, write back
+    for (int e = lane; e < 3 * nb; e += width) {
+        const int i = e / 3, d = e - 3 * i;
+        const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
+        const float a = fs[e] / mass;
+        const float x = vs[e] + hdt * a;
+        v[g] = x;
+        r[g] = rs[e];
+        fb[g] = fs[e];
+        acc[9] = fmaf(x, x, acc[9]);
+    }
+}
+
+__device__ __forceinline__ void free_beads(const hpf_respa_plan& p, int fblock, float* __restrict__ r,
+                                           float* __restrict__ v, const SlowForces& slow,
+                                           float mass, float h_out, float dt, int respa,
+                                           const Box& bx, float (&acc)[kOut]) {
+    const int stride = p.n_free_blocks * kThreads;
+    for (int j = fblock * kThreads + threadIdx.x; j < p.n_free; j += stride) {
+        const int64_t g = 3 * (int64_t)p.free_ids[j];
+        for (int d = 0; d < 3; ++d) {
+            float x = v[g + d];
+            for (int q = 0; q < slow.n; ++q) x = x + h_out * (slow.f[q][g + d] / mass);
+            float y = r[g + d];
+            for (int it = 0; it < respa; ++it) y = wrapf(y + dt * x, bx.L[d]);
+            v[g + d] = x;
+            r[g + d] = y;
+            acc[9] = fmaf(x, x, acc[9]);
         }
     }
-    if (out) grid_reduce_store_f<kOut>(acc, p.partials, p.ticket, out);
+}
+
+// isotropic SCR step (same arithmetic as k_scr_sums_alpha in hpf_md.cu)
+__device__ void scr_epilogue(const BaroFuse& f, const double* out) {
+    const HpfScrArgs& a = f.a;
+    BoxState* bs = f.bs;
+    const int s = *f.counter;
+    const bool ok = s >= 0 && s < a.n_steps;
+    f.state[12] = 1.0;
+    if (!(a.every > 1 && (s + 1) % a.every != 0)) {
+        const double V = bs->V;
+        const double A = f.field[0];
+        const double p_kin = 2.0 / (3.0 * V) * (0.5 * a.mass * out[9]);
+        const double p01 = 0.5 * A + a.half_mQm / (V * V) - f.fun->c;
+        const double sig2 = 2.0 * f.fun->sigma2_half_d;
+        double ptot[2];
+        for (int d = 0; d < 2; ++d)
+            ptot[d] = p_kin + p01 - sig2 * f.field[1 + d] + (out[1 + d] + out[5 + d]) / V;
+        const double P = 0.5 * (ptot[0] + ptot[1]) * 16.61;
+        const double R = ok ? f.randoms[(int64_t)s * a.stride] : 0.0;
+        const double noise = sqrt(2.0 * a.n_b * a.gas_constant * a.target_temperature * a.beta *
+                                  a.dt_outer * a.n_b / (V * a.tau_p)) * R;
+        const double log_alpha =
+            -a.n_b * a.dt_outer * a.beta / a.tau_p * (a.target_pressure - P) + noise;
+        const double alpha = exp(log_alpha / 3.0);
+        const int nn[3] = {bs->n[0], bs->n[1], bs->n[2]};
+        fill_box_state(*bs, (double)(float)(bs->L[0] * alpha), (double)(float)(bs->L[1] * alpha),
+                       (double)(float)(bs->L[2] * alpha), nn);
+        f.state[12] = alpha;
+        f.state[13] = P;
+    }
+    if (a.advance) *f.counter = s + 1;
+}
+
+template <bool DIH>
+__global__ void __launch_bounds__(kThreads)
+k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
+             float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
+             int respa, const double* __restrict__ box, float* __restrict__ dipoles,
+             float* __restrict__ transfer, double* out, BaroFuse baro, int* err) {
+    extern __shared__ float smem[];
+    const Box bx = load_box(box);
+    float acc[kOut];
+#pragma unroll
+    for (int k = 0; k < kOut; ++k) acc[k] = 0.0f;
+    const int n_grp_blocks = (p.n_groups + kWarps - 1) / kWarps;
+    if ((int)blockIdx.x < n_grp_blocks) {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int grp = blockIdx.x * kWarps + warp;
+        if (grp < p.n_groups) {
+            float* base = smem + (size_t)warp * 9 * p.max_group_beads;
+            run_group<DIH>(p, grp, lane, 32, base, base + 3 * p.max_group_beads,
+                           base + 6 * p.max_group_beads, r, v, fb, slow, mass, h_out, hdt, dt,
+                           respa, bx, dipoles, transfer, acc, WarpSync());
+        }
+    } else {
+        free_beads(p, blockIdx.x - n_grp_blocks, r, v, slow, mass, h_out, dt, respa, bx, acc);
+    }
+    if (!out) return;
+    if (grid_reduce_store_f<kOut>(acc, p.partials, p.ticket, out) && baro.on)
+        scr_epilogue(baro, out);
+}
+
+template <bool DIH>
+__global__ void __launch_bounds__(kThreads)
+k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
+            float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
+            int respa, const double* __restrict__ box, float* __restrict__ dipoles,
+            float* __restrict__ transfer, double* out, BaroFuse baro, int* err) {
+    extern __shared__ float smem[];
+    const Box bx = load_box(box);
+    float acc[kOut];
+#pragma unroll
+    for (int k = 0; k < kOut; ++k) acc[k] = 0.0f;
+    if ((int)blockIdx.x < p.n_groups) {
+        const int nb = p.max_group_beads;
+        run_group<DIH>(p, blockIdx.x, threadIdx.x, kThreads, smem, smem + 3 * nb, smem + 6 * nb,
+                       r, v, fb, slow, mass, h_out, hdt, dt, respa, bx, dipoles, transfer, acc,
+                       CtaSync());
+    } else {
+        free_beads(p, blockIdx.x - p.n_groups, r, v, slow, mass, h_out, dt, respa, bx, acc);
+    }
+    if (!out) return;
+    if (grid_reduce_store_f<kOut>(acc, p.partials, p.ticket, out) && baro.on)
+        scr_epilogue(baro, out);
 }
 
 // ------------------------------------------------------------- planner ---
@@ -242,14 +357,19 @@ int upload(T** dst, const std::vector<T>& src) {
     return HPF_OK;
 }
 
+int grid_size(const hpf_respa_plan* p) {
+    const int g = p->warp_mode ? (p->n_groups + kWarps - 1) / kWarps : p->n_groups;
+    return g + p->n_free_blocks;
+}
+
 }  // namespace
 
 extern "C" {
 
 int hpf_respa_plan_destroy(hpf_respa_plan* p) {
     if (!p) return HPF_OK;
-    void* ptrs[] = {p->blk_bead, p->bead_ids, p->blk_bond, p->bond_ij, p->bond_p, p->blk_ang,
-                    p->ang_ijk, p->ang_p, p->blk_dih, p->dih_ijkl, p->dih_coeff, p->dih_tl,
+    void* ptrs[] = {p->grp_bead, p->bead_ids, p->grp_bond, p->bond_ij, p->bond_p, p->grp_ang,
+                    p->ang_ijk, p->ang_p, p->grp_dih, p->dih_ijkl, p->dih_coeff, p->dih_tl,
                     p->dih_gid, p->free_ids, p->partials, p->ticket};
     for (void* q : ptrs) cudaFree(q);
     delete p;
@@ -262,9 +382,9 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
                           const float* at0, const float* ak, int64_t nd, const int32_t* da,
                           const int32_t* db, const int32_t* dc, const int32_t* dd,
                           const float* dcoeff, const int32_t* dtype, const int32_t* dlast,
-                          int max_block_beads) {
+                          int max_group_beads) {
     if (!out || n < 0 || n > (int64_t)0x7fffffff || nb < 0 || na < 0 || nd < 0 ||
-        max_block_beads < 1)
+        max_group_beads < 1)
         return HPF_ERR_ARG;
     *out = nullptr;
     auto bad = [n](int32_t i) { return i < 0 || (int64_t)i >= n; };
@@ -291,48 +411,53 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
     // components in order of their smallest bead (the DSU root is the minimum)
     std::vector<int> comp_size(n, 0);
     std::vector<int> free_ids;
+    int largest = 0;
     for (int64_t i = 0; i < n; ++i) {
         if (bonded[i]) comp_size[dsu.find((int)i)]++;
         else free_ids.push_back((int)i);
     }
-    // hard limit: the block must fit in shared memory (36 bytes per bead)
+    for (int64_t i = 0; i < n; ++i) largest = std::max(largest, comp_size[i]);
+    // a group must fit in shared memory (36 bytes per bead); a warp takes
+    // groups of up to kWarpMaxBeads beads, a CTA up to ~6400
     const int hard = (227 * 1024) / 36;
-    std::vector<int> comp_block(n, -1);
-    std::vector<int> block_beads;  // bead count per block
+    if (largest > hard) return HPF_ERR_NOT_IMPLEMENTED;
+    int cap = std::max(max_group_beads, largest);
+    const int warp_mode = cap <= kWarpMaxBeads ? 1 : 0;
+    std::vector<int> comp_grp(n, -1);
+    std::vector<int> grp_beads;
     int cur = 0;
     for (int64_t i = 0; i < n; ++i) {
         if (!bonded[i] || dsu.find((int)i) != (int)i) continue;
         const int sz = comp_size[i];
-        if (sz > hard) return HPF_ERR_NOT_IMPLEMENTED;
-        if (block_beads.empty() || cur + sz > max_block_beads) {
-            block_beads.push_back(0);
+        if (grp_beads.empty() || cur + sz > cap) {
+            grp_beads.push_back(0);
             cur = 0;
         }
-        comp_block[i] = (int)block_beads.size() - 1;
-        block_beads.back() += sz;
+        comp_grp[i] = (int)grp_beads.size() - 1;
+        grp_beads.back() += sz;
         cur += sz;
     }
-    const int B = (int)block_beads.size();
-    std::vector<int> blk_bead(B + 1, 0);
-    for (int b = 0; b < B; ++b) blk_bead[b + 1] = blk_bead[b] + block_beads[b];
-    std::vector<int> bead_ids(blk_bead[B]);
-    std::vector<int> local(n, -1), fill(blk_bead.begin(), blk_bead.end() - 1);
+    const int G = (int)grp_beads.size();
+    std::vector<int> grp_bead(G + 1, 0);
+    for (int g = 0; g < G; ++g) grp_bead[g + 1] = grp_bead[g] + grp_beads[g];
+    std::vector<int> bead_ids(grp_bead[G]);
+    std::vector<int> local(n, -1), fill(grp_bead.begin(), grp_bead.end() - 1);
     for (int64_t i = 0; i < n; ++i) {
         if (!bonded[i]) continue;
-        const int b = comp_block[dsu.find((int)i)];
-        local[i] = fill[b] - blk_bead[b];
-        bead_ids[fill[b]++] = (int)i;
+        const int g = comp_grp[dsu.find((int)i)];
+        local[i] = fill[g] - grp_bead[g];
+        bead_ids[fill[g]++] = (int)i;
     }
-    auto blk_of = [&](int i) { return comp_block[dsu.find(i)]; };
+    auto grp_of = [&](int i) { return comp_grp[dsu.find(i)]; };
     auto bucket = [&](int64_t cnt, auto first_bead, std::vector<int>& start,
                       std::vector<int64_t>& order) {
-        std::vector<int> count(B + 1, 0);
-        for (int64_t t = 0; t < cnt; ++t) count[blk_of(first_bead(t)) + 1]++;
-        start.assign(B + 1, 0);
-        for (int b = 0; b < B; ++b) start[b + 1] = start[b] + count[b + 1];
+        std::vector<int> count(G + 1, 0);
+        for (int64_t t = 0; t < cnt; ++t) count[grp_of(first_bead(t)) + 1]++;
+        start.assign(G + 1, 0);
+        for (int g = 0; g < G; ++g) start[g + 1] = start[g] + count[g + 1];
         std::vector<int> pos(start.begin(), start.end() - 1);
         order.assign(cnt, 0);
-        for (int64_t t = 0; t < cnt; ++t) order[pos[blk_of(first_bead(t))]++] = t;
+        for (int64_t t = 0; t < cnt; ++t) order[pos[grp_of(first_bead(t))]++] = t;
     };
     std::vector<int> sb, sa, sd;
     std::vector<int64_t> ob, oa, od;
@@ -368,72 +493,108 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
     hpf_respa_plan* p = new hpf_respa_plan();
     memset(p, 0, sizeof(*p));
     p->n_beads = n;
-    p->n_mol_blocks = B;
+    p->n_groups = G;
     p->n_free = (int)free_ids.size();
+    p->warp_mode = warp_mode;
+    p->has_dih = nd > 0;
     int mx = 0;
-    for (int b = 0; b < B; ++b) mx = std::max(mx, block_beads[b]);
-    p->max_block_beads = mx;
-    p->smem = sizeof(float) * 9 * (size_t)std::max(mx, 1);
+    for (int g = 0; g < G; ++g) mx = std::max(mx, grp_beads[g]);
+    p->max_group_beads = std::max(mx, 1);
+    p->smem = sizeof(float) * 9 * (size_t)p->max_group_beads * (warp_mode ? kWarps : 1);
+    const int grp_blocks = warp_mode ? (G + kWarps - 1) / kWarps : G;
     int nfb = (p->n_free + kThreads - 1) / kThreads;
-    nfb = std::min(nfb, std::max(1, 152 * 8 - B));
+    nfb = std::min(nfb, std::max(1, 152 * 8 - grp_blocks));
     if (p->n_free == 0) nfb = 0;
     p->n_free_blocks = nfb;
     int st = HPF_OK;
-    if ((st = upload(&p->blk_bead, blk_bead)) || (st = upload(&p->bead_ids, bead_ids)) ||
-        (st = upload(&p->blk_bond, sb)) || (st = upload(&p->bond_ij, bond_ij)) ||
-        (st = upload(&p->bond_p, bond_p)) || (st = upload(&p->blk_ang, sa)) ||
+    if ((st = upload(&p->grp_bead, grp_bead)) || (st = upload(&p->bead_ids, bead_ids)) ||
+        (st = upload(&p->grp_bond, sb)) || (st = upload(&p->bond_ij, bond_ij)) ||
+        (st = upload(&p->bond_p, bond_p)) || (st = upload(&p->grp_ang, sa)) ||
         (st = upload(&p->ang_ijk, ang_ijk)) || (st = upload(&p->ang_p, ang_p)) ||
-        (st = upload(&p->blk_dih, sd)) || (st = upload(&p->dih_ijkl, dih_ijkl)) ||
+        (st = upload(&p->grp_dih, sd)) || (st = upload(&p->dih_ijkl, dih_ijkl)) ||
         (st = upload(&p->dih_coeff, dih_coeff)) || (st = upload(&p->dih_tl, dih_tl)) ||
         (st = upload(&p->dih_gid, dih_gid)) || (st = upload(&p->free_ids, free_ids))) {
         hpf_respa_plan_destroy(p);
         return st;
     }
-    const int grid = B + nfb;
+    const int grid = grid_size(p);
     if (cudaMalloc(&p->partials, sizeof(double) * kOut * (size_t)std::max(grid, 1)) != cudaSuccess ||
         cudaMalloc(&p->ticket, sizeof(unsigned int)) != cudaSuccess ||
         cudaMemset(p->ticket, 0, sizeof(unsigned int)) != cudaSuccess) {
         hpf_respa_plan_destroy(p);
         return HPF_ERR_CUDA;
     }
-    if (p->smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_respa, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)p->smem) != cudaSuccess) {
-        hpf_respa_plan_destroy(p);
-        return HPF_ERR_CUDA;
+    if (p->smem > 48 * 1024) {
+        const void* fn = warp_mode ? (p->has_dih ? (const void*)k_respa_warp<true>
+                                                 : (const void*)k_respa_warp<false>)
+                                   : (p->has_dih ? (const void*)k_respa_cta<true>
+                                                 : (const void*)k_respa_cta<false>);
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem) !=
+            cudaSuccess) {
+            hpf_respa_plan_destroy(p);
+            return HPF_ERR_CUDA;
+        }
     }
     *out = p;
     return HPF_OK;
 }
 
-int hpf_respa_plan_info(const hpf_respa_plan* p, int* n_mol_blocks, int* n_free,
-                        int* max_block_beads) {
+int hpf_respa_plan_info(const hpf_respa_plan* p, int* n_groups, int* n_free,
+                        int* max_group_beads) {
     if (!p) return HPF_ERR_ARG;
-    if (n_mol_blocks) *n_mol_blocks = p->n_mol_blocks;
+    if (n_groups) *n_groups = p->n_groups;
     if (n_free) *n_free = p->n_free;
-    if (max_block_beads) *max_block_beads = p->max_block_beads;
+    if (max_group_beads) *max_group_beads = p->max_group_beads;
     return HPF_OK;
 }
 
 int hpf_respa_step(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
                    const float* const* slow_forces, int n_slow, double mass, double dt,
                    int respa_inner, const double* box, float* dipoles, float* transfer,
-                   double* out, int* d_err, void* stream) {
+                   double* out, hpf_ctx* baro_ctx, const HpfScrArgs* baro,
+                   const double* field_sums, const double* randoms, int* counter, double* state,
+                   int* d_err, void* stream) {
     if (!p || !r || !v || !f_bonded || !box || n_slow < 0 || n_slow > kMaxSlow ||
         (n_slow > 0 && !slow_forces) || !(mass > 0) || respa_inner < 1 ||
         (dipoles != nullptr) != (transfer != nullptr))
         return HPF_ERR_ARG;
+    BaroFuse bf;
+    memset(&bf, 0, sizeof(bf));
+    if (baro) {
+        if (!baro_ctx || !field_sums || !randoms || !counter || !state || !out ||
+            baro->n_types != baro_ctx->T)
+            return HPF_ERR_ARG;
+        bf.on = 1;
+        bf.a = *baro;
+        bf.field = field_sums;
+        bf.randoms = randoms;
+        bf.counter = counter;
+        bf.bs = baro_ctx->d_box;
+        bf.fun = baro_ctx->d_fun;
+        bf.state = state;
+    }
     SlowForces sf;
     sf.n = n_slow;
     for (int q = 0; q < n_slow; ++q) {
         if (!slow_forces[q]) return HPF_ERR_ARG;
         sf.f[q] = slow_forces[q];
     }
-    const int grid = p->n_mol_blocks + p->n_free_blocks;
+    const int grid = grid_size(p);
     if (grid == 0) return HPF_OK;
-    k_respa<<<grid, kThreads, p->smem, as_stream(stream)>>>(
-        *p, r, v, f_bonded, sf, (float)mass, (float)(0.5 * respa_inner * dt), (float)(0.5 * dt),
-        (float)dt, respa_inner, box, dipoles, transfer, out, d_err);
+    cudaStream_t st = as_stream(stream);
+    const float h_out = (float)(0.5 * respa_inner * dt), hdt = (float)(0.5 * dt);
+#define HPF_RESPA(K)                                                                          \
+    K<<<grid, kThreads, p->smem, st>>>(*p, r, v, f_bonded, sf, (float)mass, h_out, hdt,        \
+                                       (float)dt, respa_inner, box, dipoles, transfer, out, bf, \
+                                       d_err)
+    if (p->warp_mode) {
+        if (p->has_dih) HPF_RESPA(k_respa_warp<true>);
+        else HPF_RESPA(k_respa_warp<false>);
+    } else {
+        if (p->has_dih) HPF_RESPA(k_respa_cta<true>);
+        else HPF_RESPA(k_respa_cta<false>);
+    }
+#undef HPF_RESPA
     HPF_LAUNCH_CHECK();
     return HPF_OK;
 }

@@ -170,13 +170,22 @@ class RespaMD:
             b.target_pressure = float(target_pressure)
             b.beta, b.tau_p, b.dt_outer, b.n_b = beta, float(cfg.tau_p), dt_o, float(every)
             self.baro_args = b
-        self.launches_per_step += (2 if thermostat else 0) + (2 if barostat else 0)
+        if self.plan is not None:
+            # CSVR: sums (with the fused second kick) + scale; the barostat runs
+            # in the respa kernel's last block and the paint
+            self.launches_per_step += 1 if thermostat else 0
+        else:
+            self.launches_per_step += (1 if thermostat else 0) + (2 if barostat else 0)
 
-    def _thermostat(self, st):
-        _lib.call("hpf_csvr", _lib.ptr(self.v), _lib.ptr(self.group), self.n,
-                  _lib.ctypes.byref(self.thermo_args), _lib.ptr(self.randoms),
-                  _lib.ptr(self.counter), _lib.ptr(self.state), _lib.ptr(self.ws_md),
-                  _lib.ptr(self.err), st)
+    def _thermostat(self, st, kick=False):
+        """CSVR; with kick=True the second outer half kick runs in the same
+        pass, just before the kinetic energy is taken."""
+        fs = self._slow_forces() if kick else []
+        arr = (_lib.P * max(1, len(fs)))(*[_lib.ptr(f) for f in fs])
+        _lib.call("hpf_csvr", _lib.ptr(self.v), _lib.ptr(self.group), self.n, arr, len(fs),
+                  self.respa * self.dt, _lib.ctypes.byref(self.thermo_args),
+                  _lib.ptr(self.randoms), _lib.ptr(self.counter), _lib.ptr(self.state),
+                  _lib.ptr(self.ws_md), _lib.ptr(self.err), st)
 
     def _barostat(self, st):
         _lib.call("hpf_scr_isotropic", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.v), self.n,
@@ -243,9 +252,10 @@ class RespaMD:
                 _lib.ptr(self.f_angle) if t.n_angles else None,
                 _lib.ptr(self.f_dih) if t.n_dihedrals else None)
 
-    def _field(self, st, sums=None):
+    def _field(self, st, sums=None, pos_scale=None):
         _lib.call("hpf_field_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.types), self.n,
-                  self.masses, _lib.ptr(self.f_field), _lib.ptr(sums), st)
+                  self.masses, _lib.ptr(self.f_field), _lib.ptr(sums),
+                  None if pos_scale is None else _lib.ctypes.c_void_p(pos_scale), st)
         if self.charges is not None:
             _lib.call("hpf_pic_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.charges),
                       self.n, float(self.elec_factor), _lib.ptr(self.f_elec), None, None, None,
@@ -266,12 +276,20 @@ class RespaMD:
                 self.bonded_out[k:k + 4].copy_(ws[:4])
 
     def _inner_fused(self, st):
+        """First outer kick + all inner steps (+ the barostat's box update in
+        the last block when coupled; positions follow in the next paint)."""
         fs = self._slow_forces()
         arr = (_lib.P * len(fs))(*[_lib.ptr(f) for f in fs])
+        baro = self.baro_args is not None
         _lib.call("hpf_respa_step", self.plan, _lib.ptr(self.r), _lib.ptr(self.v),
                   _lib.ptr(self.f_b), arr, len(fs), self.mass, self.dt, self.respa,
                   _lib.ptr(self.box), _lib.ptr(self.dipoles), _lib.ptr(self.transfer),
-                  _lib.ptr(self.bonded_out), _lib.ptr(self.err), st)
+                  _lib.ptr(self.bonded_out), self.pm._h if baro else None,
+                  _lib.ctypes.byref(self.baro_args) if baro else None,
+                  _lib.ptr(self.field_sums) if baro else None,
+                  _lib.ptr(self.randoms) if baro else None,
+                  _lib.ptr(self.counter) if baro else None,
+                  _lib.ptr(self.state) if baro else None, _lib.ptr(self.err), st)
 
     def _inner_unfused(self, st):
         fb, fa, fd = self._bonded_ptrs()
@@ -287,18 +305,22 @@ class RespaMD:
     def step(self):
         """One outer rRESPA step (launch sequence only; no host sync)."""
         st = _lib.stream_ptr()
+        scale = None
         if self.plan is not None:
-            self._inner_fused(st)
+            self._inner_fused(st)  # includes the barostat's box update
+            if self.baro_args is not None:
+                scale = self.state.data_ptr() + 12 * 8  # alpha, applied in the paint
         else:
             self._inner_unfused(st)
             if self.baro_args is not None:
-                raise NotImplementedError("the device barostat needs the fused inner loop")
-        if self.baro_args is not None:
-            self._barostat(st)
-        self._field(st, self.field_sums)
-        self._outer_kick(st)
+                self.bonded_out[0:4].copy_(self.ws_bond[:4])
+                self.bonded_out[4:8].copy_(self.ws_angle[:4])
+                self._barostat(st)
+        self._field(st, self.field_sums, pos_scale=scale)
         if self.thermo_args is not None:
-            self._thermostat(st)
+            self._thermostat(st, kick=True)
+        else:
+            self._outer_kick(st)
 
     def capture(self):
         """Record one outer step in a CUDA graph (after a warm-up step)."""

@@ -141,8 +141,12 @@ int hpf_readout(hpf_ctx* ctx, const float* force_mesh, const float* pos,
  * real-space intermediates: paint -> r2c -> fused k-space -> c2r(3T) ->
  * readout.  Scratch spectra/grids belong to the context.  sums as in
  * hpf_kspace_force (may be NULL). */
-int hpf_field_step(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_t n,
-                   const double* type_mass, float* force, double* sums, void* stream);
+int hpf_field_step(hpf_ctx* ctx, float* pos, const int32_t* types, int64_t n,
+                   const double* type_mass, float* force, double* sums,
+                   const double* pos_scale, void* stream);
+/* pos_scale (device double, may be NULL): when given, positions are first
+ * rescaled in place, pos = float(*pos_scale) * pos -- the position update of
+ * a barostat step (hymd/barostat_scr.py:128) fused into the paint. */
 
 /* ---- PIC_Spectral electrostatics ------------------------------------------
  * update_field_force_q (hymd/field.py:241-403): paint q/dV -> r2c -> H ->
@@ -221,20 +225,8 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n_beads, int64_t nb, con
 int hpf_respa_plan_destroy(hpf_respa_plan* plan);
 int hpf_respa_plan_info(const hpf_respa_plan* plan, int* n_mol_blocks, int* n_free,
                         int* max_block_beads);
-/* One launch: first outer half kick v += 0.5 respa_inner dt F_s / mass for
- * each slow force array (field, PIC, dipole, in that order, main.py:802-827),
- * then respa_inner x [v += 0.5 dt F_b/mass; r = mod(r + dt v, box); F_b =
- * bonded forces(r); v += 0.5 dt F_b/mass] (main.py:830-887).  f_bonded
- * (float[N][3]) carries the bonded force between calls and must hold the
- * bonded force of the current positions on entry (zero for free beads).
- * dipoles/transfer (may both be NULL) receive the CBT dipoles of the last
- * inner step (dipole_flag = 1 there, as main.py:863-866).  out (device
- * double[9], may be NULL) = {E_bond, bond_pr[3], E_angle, angle_pr[3],
- * E_dihedral} of the last inner step.  box: DEVICE double[3]. */
-int hpf_respa_step(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
-                   const float* const* slow_forces, int n_slow, double mass, double dt,
-                   int respa_inner, const double* box, float* dipoles, float* transfer,
-                   double* out, int* d_err, void* stream);
+/* hpf_respa_step (the launch itself) is declared after the barostat
+ * arguments below. */
 
 /* ---- thermostat / barostat on the device -----------------------------------
  * The random numbers are drawn on the host in the reference's order (numpy
@@ -269,9 +261,12 @@ typedef struct {
 /* csvr_thermostat (hymd/thermostat.py:111-219) for up to two coupling groups.
  * state: device double[16] ([4g] alpha, [4g+1..3] COM velocity, [8+g]
  * accumulated thermostat work).  ws: workspace (HPF_OUT_DOUBLES). */
-int hpf_csvr(float* v, const int32_t* group, int64_t n, const HpfCsvrArgs* args,
-             const double* randoms, int* counter, double* state, double* ws, int* d_err,
-             void* stream);
+int hpf_csvr(float* v, const int32_t* group, int64_t n, const float* const* kick_forces,
+             int n_kick, double kick_dt, const HpfCsvrArgs* args, const double* randoms,
+             int* counter, double* state, double* ws, int* d_err, void* stream);
+/* kick_forces (n_kick arrays, may be 0): the second outer half kick
+ * v += 0.5 kick_dt F/mass (hymd/main.py:1143-1169) applied in the same pass,
+ * before the kinetic energy is taken. */
 /* Stochastic cell rescaling, isotropic (hymd/barostat_scr.py:34-132): the
  * pressure from field_sums (device double[4] = A, B_xyz of the last field
  * evaluation, see hpf_kspace_force), bonded_out (device double[9] of
@@ -282,6 +277,28 @@ int hpf_scr_isotropic(hpf_ctx* ctx, float* r, const float* v, int64_t n,
                       const double* field_sums, const double* bonded_out,
                       const HpfScrArgs* args, const double* randoms, int* counter,
                       double* state, double* ws, int* d_err, void* stream);
+
+/* One launch of the fused rRESPA inner loop: the first outer half kick
+ * v += 0.5 respa_inner dt F_s / mass for each slow force array (field, PIC,
+ * dipole, in that order, main.py:802-827), then respa_inner x [v += 0.5 dt
+ * F_b/mass; r = mod(r + dt v, box); F_b = bonded forces(r); v += 0.5 dt
+ * F_b/mass] (main.py:830-887).  f_bonded (float[N][3]) carries the bonded
+ * force between calls and must hold the bonded force of the current
+ * positions on entry (zero for free beads).  dipoles/transfer (may both be
+ * NULL) receive the CBT dipoles of the last inner step (dipole_flag = 1
+ * there, main.py:863-866).  out (device double[10], may be NULL) = {E_bond,
+ * bond_pr[3], E_angle, angle_pr[3], E_dihedral, sum v^2} after the loop.
+ * box: DEVICE double[3].
+ * With baro != NULL the grid's last block then runs the isotropic SCR step
+ * of hpf_scr_isotropic on the new box (field_sums, randoms, counter, state
+ * as there; needs out); the positions are NOT rescaled here -- pass
+ * &state[12] as pos_scale to the following hpf_field_step. */
+int hpf_respa_step(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
+                   const float* const* slow_forces, int n_slow, double mass, double dt,
+                   int respa_inner, const double* box, float* dipoles, float* transfer,
+                   double* out, hpf_ctx* baro_ctx, const HpfScrArgs* baro,
+                   const double* field_sums, const double* randoms, int* counter, double* state,
+                   int* d_err, void* stream);
 
 /* Sum over particles of v^2 into out[0] (device workspace, HPF_OUT_DOUBLES);
  * KE = mass/2 * out[0]. */

@@ -63,14 +63,14 @@ def test_scr_barostat_matches_reference_formula():
     md.couple(thermostat=False, barostat="isotropic", seed=5, n_steps=10)
     md.prime()
     r_field = md.r.cpu().numpy().copy()  # positions of the last field evaluation
+    box0 = md.box_now()
     st = _lib.stream_ptr()
-    md._inner_fused(st)
+    md._inner_fused(st)  # inner loop; its last block runs the barostat on the box
     r_before = md.r.cpu().numpy().astype(np.float64)
     v = md.v.cpu().numpy()
     bonded = md.bonded_out.cpu().numpy()
-    box0 = md.box_now()
-    md._barostat(st)
     box1 = md.box_now()
+    md._field(st, md.field_sums, pos_scale=md.state.data_ptr() + 12 * 8)  # rescales positions
     r_after = md.r.cpu().numpy()
     # host pressure: FP64 oracle field at r_field, bonded virials, kinetic energy
     fun = _functional(cfg)
@@ -88,6 +88,8 @@ def test_scr_barostat_matches_reference_formula():
     log_alpha = -1 * dt_o * beta / cfg.tau_p * (1.0 - P) + noise
     alpha = np.exp(log_alpha / 3.0)
     assert float(md.state[13].item()) == pytest.approx(P, rel=1e-5, abs=5e-2)
+    assert float(md.bonded_out[9].item()) == pytest.approx(np.sum(v.astype(np.float64) ** 2),
+                                                          rel=1e-6)
     assert box1 == pytest.approx((box0 * alpha).astype(np.float32).astype(np.float64), rel=1e-7)
     assert np.allclose(r_after, (r_before * alpha).astype(np.float32), rtol=1e-6, atol=1e-6)
 
