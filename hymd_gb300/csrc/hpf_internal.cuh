@@ -64,6 +64,8 @@ struct hpf_ctx {
     bool has_c2r[3 * HPF_MAX_TYPES + 2];
 };
 
+#define HPF_REDUCE_GRID 304  // blocks of a reduction kernel (2 per SM on 152 SMs)
+
 // Layout of a reduction workspace (see HPF_OUT_DOUBLES in the C ABI header).
 __host__ __device__ inline double* ws_partials(double* ws) { return ws + 8; }
 __host__ __device__ inline unsigned int* ws_ticket(double* ws) {
@@ -73,7 +75,9 @@ __host__ __device__ inline unsigned int* ws_ticket(double* ws) {
 static inline int reduce_grid(int64_t work, int threads) {
     int64_t b = (work + threads - 1) / threads;
     if (b < 1) b = 1;
-    if (b > HPF_REDUCE_BLOCKS) b = HPF_REDUCE_BLOCKS;
+    // two blocks per SM are plenty for a grid-stride reduction, and keep the
+    // last block's FP64 pass over the partials short
+    if (b > HPF_REDUCE_GRID) b = HPF_REDUCE_GRID;
     return (int)b;
 }
 
@@ -93,6 +97,75 @@ __host__ __device__ inline void fill_box_state(BoxState& s, double L0, double L1
         s.kf[d] = (float)(2.0 * 3.14159265358979323846 / Ls[d]);
     }
     s.inv_dV = (float)(1.0 / s.dV);
+}
+
+// FP64 reciprocal from the FP32 one and two Newton steps (FMA only): FP64
+// division is a long instruction sequence on GB300's thin FP64 pipe, and the
+// single-thread epilogues below sit on the critical path of a step.
+__device__ __forceinline__ double rcp_d(double x) {
+    double r = (double)(1.0f / (float)x);
+    r = r * fma(-x, r, 2.0);
+    r = r * fma(-x, r, 2.0);
+    return r;
+}
+
+// Device-side box update (barostat): the same quantities as fill_box_state.
+__device__ __forceinline__ void fill_box_state_dev(BoxState& s, double L0, double L1, double L2) {
+    const double Ls[3] = {L0, L1, L2};
+    s.V = L0 * L1 * L2;
+    const double M = (double)s.n[0] * (double)s.n[1] * (double)s.n[2];
+    s.dV = s.V * rcp_d(M);
+    for (int d = 0; d < 3; ++d) {
+        const double iL = rcp_d(Ls[d]);
+        s.L[d] = Ls[d];
+        s.Lf[d] = (float)Ls[d];
+        const double ih = (double)s.n[d] * iL;
+        s.ih_hi[d] = (float)ih;
+        s.ih_lo[d] = (float)(ih - (double)s.ih_hi[d]);
+        s.kf[d] = (float)(2.0 * 3.14159265358979323846 * iL);
+    }
+    s.inv_dV = (float)(M * rcp_d(s.V));
+}
+
+// Isotropic SCR step (hymd/barostat_scr.py:34-132) run by one thread once all
+// sums are final.  The pressure components are added in FP64; with the k = 0
+// densities mean_t = m_t N_t / V the field part of p0 + p1 reduces to
+//   -W/V + A + (Q mean + b).mean = A/2 + (1/2 mc.Q.mc) / V^2 - c.
+// `bonded` holds {E_bond, bond_pr[3], E_angle, angle_pr[3]}.  The box is kept
+// in float32 values, as the reference's float32 box_size array.
+__device__ __forceinline__ void scr_update(const HpfScrArgs& a, double sum_v2,
+                                           const double* field, const double* bonded,
+                                           const double* randoms, int* counter, BoxState* bs,
+                                           const Functional* fun, double* state, int* err) {
+    const int s = *counter;
+    const bool ok = s >= 0 && s < a.n_steps;
+    if (!ok) hpf_flag(err, HPF_ERR_INDEX);
+    state[12] = 1.0;
+    if (!(a.every > 1 && (s + 1) % a.every != 0)) {
+        const double V = bs->V;
+        const double iV = rcp_d(V);
+        const double A = field[0];
+        const double p_kin = (2.0 / 3.0) * iV * (0.5 * a.mass * sum_v2);
+        const double p01 = 0.5 * A + a.half_mQm * iV * iV - fun->c;
+        const double sig2 = 2.0 * fun->sigma2_half_d;
+        double ptot[2];
+        for (int d = 0; d < 2; ++d)
+            ptot[d] = p_kin + p01 - sig2 * field[1 + d] + (bonded[1 + d] + bonded[5 + d]) * iV;
+        // the reference averages p_tot[-3:-1], i.e. the x and y components
+        const double P = 0.5 * (ptot[0] + ptot[1]) * 16.61;
+        const float R = ok ? (float)randoms[(int64_t)s * a.stride] : 0.0f;
+        const float itau = 1.0f / (float)a.tau_p;
+        const float noise = sqrtf((float)(2.0 * a.n_b * a.gas_constant * a.target_temperature *
+                                          a.beta * a.dt_outer * a.n_b * iV) * itau) * R;
+        const float log_alpha =
+            -(float)(a.n_b * a.dt_outer * a.beta) * itau * (float)(a.target_pressure - P) + noise;
+        const double alpha = (double)expf(log_alpha / 3.0f);
+        fill_box_state_dev(*bs, (double)(float)(bs->L[0] * alpha),
+                           (double)(float)(bs->L[1] * alpha), (double)(float)(bs->L[2] * alpha));
+        state[12] = alpha;
+        state[13] = P;
+    }
+    if (a.advance) *counter = s + 1;
 }
 
 #define HPF_CUDA_TRY(x)                                   \

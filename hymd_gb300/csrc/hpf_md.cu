@@ -32,7 +32,7 @@ int grid_for(int64_t work) {
 
 int reduce_grid_md(int64_t work) {
     int64_t g = (work + kThreads - 1) / kThreads;
-    g = g < 1 ? 1 : (g > HPF_REDUCE_BLOCKS ? HPF_REDUCE_BLOCKS : g);
+    g = g < 1 ? 1 : (g > HPF_REDUCE_GRID ? HPF_REDUCE_GRID : g);
     return (int)g;
 }
 
@@ -134,25 +134,32 @@ __global__ void k_csvr_sums_alpha(float* __restrict__ v, const int32_t* __restri
         state[4 * g] = 1.0;
         for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = 0.0;
         if (!act) continue;
-        const double N = a.count[g];
-        double com[3] = {0, 0, 0}, K;
+        // O(1) quantities without cancellation: FP32 (FP64 division and square
+        // root are long sequences on GB300's FP64 pipe, and this runs on one
+        // thread in the step's critical path)
+        const float N = (float)a.count[g];
+        const float iN = 1.0f / N;
+        float com[3] = {0, 0, 0};
+        double K;
         if (a.remove_com && N > 1) {
-            for (int d = 0; d < 3; ++d) com[d] = ws[4 * g + d] / N;
-            K = 0.5 * a.mass * (ws[4 * g + 3] - N * (com[0] * com[0] + com[1] * com[1] + com[2] * com[2]));
+            for (int d = 0; d < 3; ++d) com[d] = (float)ws[4 * g + d] * iN;
+            K = 0.5 * a.mass * (ws[4 * g + 3] - (double)N * (double)(com[0] * com[0] +
+                                                                      com[1] * com[1] +
+                                                                      com[2] * com[2]));
         } else {
             // without COM removal the reference uses the whole system's K
             K = 0.5 * a.mass * (ws[3] + (a.n_groups > 1 ? ws[7] : 0.0));
         }
-        const double Kt = 1.5 * a.gas_constant * N * a.target_temperature;
-        const double Nf = 3.0 * N;
-        const double R = ok ? randoms[(int64_t)s * a.stride + a.offset + 2 * g] : 0.0;
-        const double S = ok ? randoms[(int64_t)s * a.stride + a.offset + 2 * g + 1] : Nf - 1.0;
-        const double c = a.c;
-        const double alpha2 = c + (1.0 - c) * (S + R * R) * Kt / (Nf * K) +
-                              2.0 * R * sqrt(c * (1.0 - c) * Kt / (Nf * K));
-        state[4 * g] = sqrt(alpha2);
-        for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = com[d];
-        state[8 + g] += K * (alpha2 - 1.0);  // thermostat work (config.thermostat_work)
+        const float Kt = (float)(1.5 * a.gas_constant * a.count[g] * a.target_temperature);
+        const float Nf = 3.0f * N;
+        const float R = ok ? (float)randoms[(int64_t)s * a.stride + a.offset + 2 * g] : 0.0f;
+        const float S = ok ? (float)randoms[(int64_t)s * a.stride + a.offset + 2 * g + 1] : Nf - 1.0f;
+        const float c = (float)a.c;
+        const float q = Kt / (Nf * (float)K);
+        const float alpha2 = c + (1.0f - c) * (S + R * R) * q + 2.0f * R * sqrtf(c * (1.0f - c) * q);
+        state[4 * g] = (double)sqrtf(alpha2);
+        for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = (double)com[d];
+        state[8 + g] += K * ((double)alpha2 - 1.0);  // thermostat work (config.thermostat_work)
     }
     if (a.advance) *counter = s + 1;
 }
@@ -192,34 +199,7 @@ __global__ void k_scr_sums_alpha(const float* __restrict__ v, int64_t n3, double
          e += (int64_t)gridDim.x * blockDim.x)
         acc[0] = fmaf(v[e], v[e], acc[0]);
     if (!grid_reduce_store_f<1>(acc, ws_partials(ws), ws_ticket(ws), ws)) return;
-    const int s = *counter;
-    const bool ok = s >= 0 && s < a.n_steps;
-    if (!ok) hpf_flag(err, HPF_ERR_INDEX);
-    state[12] = 1.0;
-    if (!(a.every > 1 && (s + 1) % a.every != 0)) {
-        const double V = bs->V;
-        const double A = field[0];
-        const double p_kin = 2.0 / (3.0 * V) * (0.5 * a.mass * ws[0]);
-        const double p01 = 0.5 * A + a.half_mQm / (V * V) - fun->c;
-        const double sig2 = 2.0 * fun->sigma2_half_d;
-        double ptot[2];
-        for (int d = 0; d < 2; ++d)
-            ptot[d] = p_kin + p01 - sig2 * field[1 + d] + (bonded[1 + d] + bonded[5 + d]) / V;
-        // the reference averages p_tot[-3:-1], i.e. the x and y components
-        const double P = 0.5 * (ptot[0] + ptot[1]) * 16.61;
-        const double R = ok ? randoms[(int64_t)s * a.stride] : 0.0;
-        const double noise = sqrt(2.0 * a.n_b * a.gas_constant * a.target_temperature * a.beta *
-                                  a.dt_outer * a.n_b / (V * a.tau_p)) * R;
-        const double log_alpha =
-            -a.n_b * a.dt_outer * a.beta / a.tau_p * (a.target_pressure - P) + noise;
-        const double alpha = exp(log_alpha / 3.0);
-        const int nn[3] = {bs->n[0], bs->n[1], bs->n[2]};
-        fill_box_state(*bs, (double)(float)(bs->L[0] * alpha), (double)(float)(bs->L[1] * alpha),
-                       (double)(float)(bs->L[2] * alpha), nn);
-        state[12] = alpha;
-        state[13] = P;
-    }
-    if (a.advance) *counter = s + 1;
+    scr_update(a, ws[0], field, bonded, randoms, counter, bs, fun, state, err);
 }
 
 __global__ void k_scale_positions(float* __restrict__ r, int64_t n3, const double* __restrict__ state) {

@@ -244,36 +244,8 @@ __device__ __forceinline__ void free_beads(const hpf_respa_plan& p, int fblock, 
     }
 }
 
-// isotropic SCR step (same arithmetic as k_scr_sums_alpha in hpf_md.cu)
-__device__ void scr_epilogue(const BaroFuse& f, const double* out) {
-    const HpfScrArgs& a = f.a;
-    BoxState* bs = f.bs;
-    const int s = *f.counter;
-    const bool ok = s >= 0 && s < a.n_steps;
-    f.state[12] = 1.0;
-    if (!(a.every > 1 && (s + 1) % a.every != 0)) {
-        const double V = bs->V;
-        const double A = f.field[0];
-        const double p_kin = 2.0 / (3.0 * V) * (0.5 * a.mass * out[9]);
-        const double p01 = 0.5 * A + a.half_mQm / (V * V) - f.fun->c;
-        const double sig2 = 2.0 * f.fun->sigma2_half_d;
-        double ptot[2];
-        for (int d = 0; d < 2; ++d)
-            ptot[d] = p_kin + p01 - sig2 * f.field[1 + d] + (out[1 + d] + out[5 + d]) / V;
-        const double P = 0.5 * (ptot[0] + ptot[1]) * 16.61;
-        const double R = ok ? f.randoms[(int64_t)s * a.stride] : 0.0;
-        const double noise = sqrt(2.0 * a.n_b * a.gas_constant * a.target_temperature * a.beta *
-                                  a.dt_outer * a.n_b / (V * a.tau_p)) * R;
-        const double log_alpha =
-            -a.n_b * a.dt_outer * a.beta / a.tau_p * (a.target_pressure - P) + noise;
-        const double alpha = exp(log_alpha / 3.0);
-        const int nn[3] = {bs->n[0], bs->n[1], bs->n[2]};
-        fill_box_state(*bs, (double)(float)(bs->L[0] * alpha), (double)(float)(bs->L[1] * alpha),
-                       (double)(float)(bs->L[2] * alpha), nn);
-        f.state[12] = alpha;
-        f.state[13] = P;
-    }
-    if (a.advance) *f.counter = s + 1;
+__device__ __forceinline__ void scr_epilogue(const BaroFuse& f, const double* out, int* err) {
+    scr_update(f.a, out[9], f.field, out, f.randoms, f.counter, f.bs, f.fun, f.state, err);
 }
 
 template <bool DIH>
@@ -302,7 +274,7 @@ k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     }
     if (!out) return;
     if (grid_reduce_store_f<kOut>(acc, p.partials, p.ticket, out) && baro.on)
-        scr_epilogue(baro, out);
+        scr_epilogue(baro, out, err);
 }
 
 template <bool DIH>
@@ -326,7 +298,7 @@ k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     }
     if (!out) return;
     if (grid_reduce_store_f<kOut>(acc, p.partials, p.ticket, out) && baro.on)
-        scr_epilogue(baro, out);
+        scr_epilogue(baro, out, err);
 }
 
 // ------------------------------------------------------------- planner ---

@@ -26,7 +26,7 @@ from .force import BondedTopology
 
 class RespaMD:
     def __init__(self, positions, velocities, types, config, hamiltonian, topology=None,
-                 charges=None, device="cuda", fused=True, max_block_beads=192):
+                 charges=None, device="cuda", fused=True, max_block_beads=36):
         self.device = torch.device(device)
         self.config = config
         self.r = torch.as_tensor(np.asarray(positions, np.float32), device=self.device).contiguous()
