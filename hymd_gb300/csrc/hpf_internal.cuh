@@ -99,6 +99,12 @@ __host__ __device__ inline void fill_box_state(BoxState& s, double L0, double L1
     s.inv_dV = (float)(1.0 / s.dV);
 }
 
+// Record the first device-side error code (out-of-range index, non-finite
+// input, exhausted table); the host reads it with hpf_get_error.
+__device__ __forceinline__ void hpf_flag(int* err, int code) {
+    if (err) atomicCAS(err, 0, code);
+}
+
 // FP64 reciprocal from the FP32 one and two Newton steps (FMA only): FP64
 // division is a long instruction sequence on GB300's thin FP64 pipe, and the
 // single-thread epilogues below sit on the critical path of a step.
@@ -182,9 +188,6 @@ __device__ __forceinline__ void scr_update(const HpfScrArgs& a, double sum_v2,
 
 static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-__device__ __forceinline__ void hpf_flag(int* err, int code) {
-    if (err) atomicCAS(err, 0, code);
-}
 
 // Grid coordinate s = x * n/L split into a node index and a fraction in
 // [0,1), using only FP32 arithmetic.  n/L is held as hi+lo floats and the
