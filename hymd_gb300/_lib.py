@@ -52,8 +52,6 @@ _SIGNATURES = {
     "hpf_laplacian": [P, P, P, P],
     "hpf_energy_fp64": [P, P, P, I64, ctypes.POINTER(D), P, ctypes.POINTER(D), D, P, P],
     "hpf_readout": [P, P, P, P, I64, P, P],
-    "hpf_field_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P, P],
-    "hpf_pic_step": [P, P, P, I64, D, P, P, P, P, P, P, P],
     "hpf_bonds": [P, P, I64, P, P, P, P, P, I64, P, P, P],
     "hpf_angles": [P, P, I64, P, P, P, P, P, P, I64, P, P, P],
     "hpf_dihedrals": [P, P, I64, P, P, P, P, P, P, P, P, P, P, I64, I, P, P, P],
@@ -85,7 +83,17 @@ class ScrArgs(ctypes.Structure):
                 ("dt_outer", D), ("n_b", D)]
 
 
+class Kick(ctypes.Structure):
+    """HpfKick of include/hpf_gb300.h."""
+    _fields_ = [("v", P), ("prev", P * 4), ("n_prev", I), ("pad", I), ("mass", D),
+                ("dt_outer", D), ("thermo", ctypes.POINTER(CsvrArgs)), ("group", P),
+                ("randoms", P), ("counter", P), ("state", P), ("ws", P), ("d_err", P)]
+
+
 _SIGNATURES.update({
+    "hpf_field_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P, ctypes.POINTER(Kick), P],
+    "hpf_pic_step": [P, P, P, I64, D, P, P, P, P, P, P, ctypes.POINTER(Kick), P],
+    "hpf_csvr_scale": [P, P, I64, P, I, P],
     "hpf_csvr": [P, P, I64, ctypes.POINTER(P), I, D, ctypes.POINTER(CsvrArgs), P, P, P, P, P, P],
     "hpf_scr_isotropic": [P, P, P, I64, P, P, ctypes.POINTER(ScrArgs), P, P, P, P, P, P],
 })

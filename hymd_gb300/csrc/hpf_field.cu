@@ -274,10 +274,26 @@ __global__ void k_kspace_sums(const float2* __restrict__ phi_f, const float2* __
 }
 
 // ---------------------------------------------------------------- readout ---
+// Kick fused into the readout (MODE 1), plus CSVR velocity sums (MODE 2).
+struct KickDev {
+    float* v;
+    const float* prev[4];
+    int n_prev;
+    float mass, h;
+    HpfCsvrArgs a;
+    const int32_t* group;
+    const double* randoms;
+    int* counter;
+    double* state;
+    double* ws;
+};
+
+template <int MODE>
 __global__ void k_readout(const float* __restrict__ fm, const float* __restrict__ pos,
                           const int32_t* __restrict__ types, const float* __restrict__ charges,
                           int64_t n, int T, int64_t M, const BoxState* __restrict__ bs,
-                          float* __restrict__ force, int* err) {
+                          float* __restrict__ force, int* err, KickDev kd) {
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
@@ -323,6 +339,31 @@ __global__ void k_readout(const float* __restrict__ fm, const float* __restrict_
         force[3 * i] = out[0];
         force[3 * i + 1] = out[1];
         force[3 * i + 2] = out[2];
+        if (MODE >= 1) {
+            // v += 0.5 dt_o F_q / m for the earlier slow forces, then this one
+            float w[3];
+            for (int d = 0; d < 3; ++d) {
+                float x = kd.v[3 * i + d];
+                for (int q2 = 0; q2 < kd.n_prev; ++q2)
+                    x = x + kd.h * (kd.prev[q2][3 * i + d] / kd.mass);
+                x = x + kd.h * (out[d] / kd.mass);
+                kd.v[3 * i + d] = x;
+                w[d] = x;
+            }
+            if (MODE == 2) {
+                const int g = kd.group ? kd.group[i] : 0;
+                if (g == 0 || g == 1) {
+                    acc[4 * g + 0] += w[0];
+                    acc[4 * g + 1] += w[1];
+                    acc[4 * g + 2] += w[2];
+                    acc[4 * g + 3] += fmaf(w[0], w[0], fmaf(w[1], w[1], w[2] * w[2]));
+                }
+            }
+        }
+    }
+    if (MODE == 2) {
+        if (grid_reduce_store_f<8>(acc, ws_partials(kd.ws), ws_ticket(kd.ws), kd.ws))
+            csvr_update(kd.a, kd.ws, kd.randoms, kd.counter, kd.state, err);
     }
 }
 
@@ -534,6 +575,54 @@ int do_paint(hpf_ctx* c, const float* pos, const int32_t* types, const float* ch
         k_paint_finalize1<<<grid_for((int64_t)G * c->M, kThreads), kThreads, 0, st>>>(
             acc, out, c->M, G, sc, c->d_box);
     }
+    HPF_LAUNCH_CHECK();
+    return HPF_OK;
+}
+
+int launch_readout(hpf_ctx* c, const float* fm, const float* pos, const int32_t* types,
+                   const float* charges, int64_t n, int T, float* force, const HpfKick* kick,
+                   cudaStream_t st) {
+    KickDev kd;
+    memset(&kd, 0, sizeof(kd));
+    int mode = 0;
+    if (kick) {
+        if (!kick->v || kick->n_prev < 0 || kick->n_prev > 4 || !(kick->mass > 0))
+            return HPF_ERR_ARG;
+        kd.v = kick->v;
+        kd.n_prev = kick->n_prev;
+        for (int q = 0; q < kick->n_prev; ++q) {
+            if (!kick->prev[q]) return HPF_ERR_ARG;
+            kd.prev[q] = kick->prev[q];
+        }
+        kd.mass = (float)kick->mass;
+        kd.h = (float)(0.5 * kick->dt_outer);
+        mode = 1;
+        if (kick->thermo) {
+            const HpfCsvrArgs& a = *kick->thermo;
+            if (!kick->randoms || !kick->counter || !kick->state || !kick->ws ||
+                a.n_groups < 1 || a.n_groups > 2 || (a.n_groups > 1 && !kick->group))
+                return HPF_ERR_ARG;
+            kd.a = a;
+            kd.group = kick->group;
+            kd.randoms = kick->randoms;
+            kd.counter = kick->counter;
+            kd.state = kick->state;
+            kd.ws = kick->ws;
+            mode = 2;
+        }
+    }
+    if (mode == 0)
+        k_readout<0><<<grid_for(n, kThreads), kThreads, 0, st>>>(fm, pos, types, charges, n, T,
+                                                                 c->M, c->d_box, force, c->d_err,
+                                                                 kd);
+    else if (mode == 1)
+        k_readout<1><<<grid_for(n, kThreads), kThreads, 0, st>>>(fm, pos, types, charges, n, T,
+                                                                 c->M, c->d_box, force, c->d_err,
+                                                                 kd);
+    else
+        k_readout<2><<<reduce_grid(n, kThreads), kThreads, 0, st>>>(
+            fm, pos, types, charges, n, T, c->M, c->d_box, force,
+            kick->d_err ? kick->d_err : c->d_err, kd);
     HPF_LAUNCH_CHECK();
     return HPF_OK;
 }
@@ -876,15 +965,13 @@ int hpf_readout(hpf_ctx* c, const float* force_mesh, const float* pos, const int
                 int64_t n, float* force, void* stream) {
     if (!c || !force_mesh || n < 0 || (n > 0 && (!pos || !types || !force))) return HPF_ERR_ARG;
     if (n == 0) return HPF_OK;
-    k_readout<<<grid_for(n, kThreads), kThreads, 0, as_stream(stream)>>>(
-        force_mesh, pos, types, nullptr, n, c->T, c->M, c->d_box, force, c->d_err);
-    HPF_LAUNCH_CHECK();
-    return HPF_OK;
+    return launch_readout(c, force_mesh, pos, types, nullptr, n, c->T, force, nullptr,
+                          as_stream(stream));
 }
 
 int hpf_field_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
                    const double* type_mass, float* force, double* sums, const double* pos_scale,
-                   void* stream) {
+                   const HpfKick* kick, void* stream) {
     if (!c || !type_mass || n < 0 || (n > 0 && (!pos || !types || !force))) return HPF_ERR_ARG;
     cudaStream_t st = as_stream(stream);
     TypeScale sc;
@@ -897,18 +984,14 @@ int hpf_field_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
         HPF_OK)
         return r;
     if ((r = exec_c2r(c, c->d_spec, c->d_grid, 3 * c->T, st)) != HPF_OK) return r;
-    if (n > 0) {
-        k_readout<<<grid_for(n, kThreads), kThreads, 0, st>>>(c->d_grid, pos, types, nullptr, n,
-                                                              c->T, c->M, c->d_box, force,
-                                                              c->d_err);
-        HPF_LAUNCH_CHECK();
-    }
+    if (n > 0) return launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, kick, st);
     return HPF_OK;
 }
 
 int hpf_pic_step(hpf_ctx* c, const float* pos, const float* charges, int64_t n,
                  double elec_factor, float* elec_forces, float* phi_q, float* psi,
-                 float* elec_field, void* psi_k, double* sums, void* stream) {
+                 float* elec_field, void* psi_k, double* sums, const HpfKick* kick,
+                 void* stream) {
     if (!c || n < 0 || (n > 0 && (!pos || !charges || !elec_forces))) return HPF_ERR_ARG;
     cudaStream_t st = as_stream(stream);
     TypeScale sc;
@@ -935,12 +1018,9 @@ int hpf_pic_step(hpf_ctx* c, const float* pos, const float* charges, int64_t n,
     if (elec_field)
         HPF_CUDA_TRY(cudaMemcpyAsync(elec_field, c->d_grid + c->M, sizeof(float) * 3 * c->M,
                                      cudaMemcpyDeviceToDevice, st));
-    if (n > 0) {
-        k_readout<<<grid_for(n, kThreads), kThreads, 0, st>>>(c->d_grid + c->M, pos, nullptr,
-                                                              charges, n, 1, c->M, c->d_box,
-                                                              elec_forces, c->d_err);
-        HPF_LAUNCH_CHECK();
-    }
+    if (n > 0)
+        return launch_readout(c, c->d_grid + c->M, pos, nullptr, charges, n, 1, elec_forces, kick,
+                              st);
     return HPF_OK;
 }
 

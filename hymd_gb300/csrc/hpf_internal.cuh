@@ -133,6 +133,50 @@ __device__ __forceinline__ void fill_box_state_dev(BoxState& s, double L0, doubl
     s.inv_dV = (float)(M * rcp_d(s.V));
 }
 
+// CSVR scale factors (hymd/thermostat.py:167-219, Bussi-Parrinello 2008 form)
+// from the per-group sums ws[4g..4g+3] = (sum v_x, sum v_y, sum v_z, sum v^2),
+// run by one thread once the sums are final.  state[4g] = alpha,
+// state[4g+1..3] = the group's centre-of-mass velocity, state[8+g] += work.
+// The O(1) quantities have no cancellation and are formed in FP32 (FP64
+// division and square root are long sequences on GB300's FP64 pipe).
+__device__ __forceinline__ void csvr_update(const HpfCsvrArgs& a, const double* ws,
+                                            const double* randoms, int* counter, double* state,
+                                            int* err) {
+    const int s = *counter;
+    const bool ok = s >= 0 && s < a.n_steps;
+    if (!ok) hpf_flag(err, HPF_ERR_INDEX);
+    const bool act = !(a.every > 1 && (s + 1) % a.every != 0);
+    for (int g = 0; g < a.n_groups; ++g) {
+        state[4 * g] = 1.0;
+        for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = 0.0;
+        if (!act) continue;
+        const float N = (float)a.count[g];
+        const float iN = 1.0f / N;
+        float com[3] = {0, 0, 0};
+        double K;
+        if (a.remove_com && N > 1) {
+            for (int d = 0; d < 3; ++d) com[d] = (float)ws[4 * g + d] * iN;
+            K = 0.5 * a.mass * (ws[4 * g + 3] - (double)N * (double)(com[0] * com[0] +
+                                                                      com[1] * com[1] +
+                                                                      com[2] * com[2]));
+        } else {
+            // without COM removal the reference uses the whole system's K
+            K = 0.5 * a.mass * (ws[3] + (a.n_groups > 1 ? ws[7] : 0.0));
+        }
+        const float Kt = (float)(1.5 * a.gas_constant * a.count[g] * a.target_temperature);
+        const float Nf = 3.0f * N;
+        const float R = ok ? (float)randoms[(int64_t)s * a.stride + a.offset + 2 * g] : 0.0f;
+        const float S = ok ? (float)randoms[(int64_t)s * a.stride + a.offset + 2 * g + 1] : Nf - 1.0f;
+        const float c = (float)a.c;
+        const float q = Kt / (Nf * (float)K);
+        const float alpha2 = c + (1.0f - c) * (S + R * R) * q + 2.0f * R * sqrtf(c * (1.0f - c) * q);
+        state[4 * g] = (double)sqrtf(alpha2);
+        for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = (double)com[d];
+        state[8 + g] += K * ((double)alpha2 - 1.0);  // thermostat work (config.thermostat_work)
+    }
+    if (a.advance) *counter = s + 1;
+}
+
 // Isotropic SCR step (hymd/barostat_scr.py:34-132) run by one thread once all
 // sums are final.  The pressure components are added in FP64; with the k = 0
 // densities mean_t = m_t N_t / V the field part of p0 + p1 reduces to

@@ -126,42 +126,7 @@ __global__ void k_csvr_sums_alpha(float* __restrict__ v, const int32_t* __restri
         acc[4 * g + 3] += fmaf(x, x, fmaf(y, y, z * z));
     }
     if (!grid_reduce_store_f<8>(acc, ws_partials(ws), ws_ticket(ws), ws)) return;
-    const int s = *counter;
-    const bool ok = s >= 0 && s < a.n_steps;
-    if (!ok) hpf_flag(err, HPF_ERR_INDEX);
-    const bool act = !(a.every > 1 && (s + 1) % a.every != 0);
-    for (int g = 0; g < a.n_groups; ++g) {
-        state[4 * g] = 1.0;
-        for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = 0.0;
-        if (!act) continue;
-        // O(1) quantities without cancellation: FP32 (FP64 division and square
-        // root are long sequences on GB300's FP64 pipe, and this runs on one
-        // thread in the step's critical path)
-        const float N = (float)a.count[g];
-        const float iN = 1.0f / N;
-        float com[3] = {0, 0, 0};
-        double K;
-        if (a.remove_com && N > 1) {
-            for (int d = 0; d < 3; ++d) com[d] = (float)ws[4 * g + d] * iN;
-            K = 0.5 * a.mass * (ws[4 * g + 3] - (double)N * (double)(com[0] * com[0] +
-                                                                      com[1] * com[1] +
-                                                                      com[2] * com[2]));
-        } else {
-            // without COM removal the reference uses the whole system's K
-            K = 0.5 * a.mass * (ws[3] + (a.n_groups > 1 ? ws[7] : 0.0));
-        }
-        const float Kt = (float)(1.5 * a.gas_constant * a.count[g] * a.target_temperature);
-        const float Nf = 3.0f * N;
-        const float R = ok ? (float)randoms[(int64_t)s * a.stride + a.offset + 2 * g] : 0.0f;
-        const float S = ok ? (float)randoms[(int64_t)s * a.stride + a.offset + 2 * g + 1] : Nf - 1.0f;
-        const float c = (float)a.c;
-        const float q = Kt / (Nf * (float)K);
-        const float alpha2 = c + (1.0f - c) * (S + R * R) * q + 2.0f * R * sqrtf(c * (1.0f - c) * q);
-        state[4 * g] = (double)sqrtf(alpha2);
-        for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = (double)com[d];
-        state[8 + g] += K * ((double)alpha2 - 1.0);  // thermostat work (config.thermostat_work)
-    }
-    if (a.advance) *counter = s + 1;
+    csvr_update(a, ws, randoms, counter, state, err);
 }
 
 __global__ void k_csvr_scale(float* __restrict__ v, const int32_t* __restrict__ group, int64_t n,
@@ -260,6 +225,15 @@ int hpf_csvr(float* v, const int32_t* group, int64_t n, const float* const* kick
         v, group, n, fl, (float)(0.5 * kick_dt), ws, *args, randoms, counter, state, d_err);
     HPF_LAUNCH_CHECK();
     k_csvr_scale<<<grid_for(n), kThreads, 0, st>>>(v, group, n, state, args->remove_com);
+    HPF_LAUNCH_CHECK();
+    return HPF_OK;
+}
+
+int hpf_csvr_scale(float* v, const int32_t* group, int64_t n, const double* state,
+                   int remove_com, void* stream) {
+    if (!v || !state || n < 0) return HPF_ERR_ARG;
+    if (n == 0) return HPF_OK;
+    k_csvr_scale<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(v, group, n, state, remove_com);
     HPF_LAUNCH_CHECK();
     return HPF_OK;
 }

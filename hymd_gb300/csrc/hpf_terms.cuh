@@ -33,11 +33,13 @@ struct Box {
     float L[3], iL[3];
 };
 
+// The reciprocal only picks the periodic image (nint(r / L)), so FP32 is
+// enough; an FP64 division per thread would keep GB300's thin FP64 pipe busy.
 __device__ __forceinline__ Box load_box(const double* box) {
     Box b;
     for (int d = 0; d < 3; ++d) {
         b.L[d] = (float)box[d];
-        b.iL[d] = (float)(1.0 / box[d]);
+        b.iL[d] = 1.0f / b.L[d];
     }
     return b;
 }

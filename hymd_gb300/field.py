@@ -359,7 +359,7 @@ def update_field_force_q(charges, phi_q, phi_q_fourier, psi, psi_fourier, elec_f
         pm.pic_sums = torch.zeros(8, dtype=torch.float64, device=pm.device)
     _lib.call("hpf_pic_step", pm._h, _lib.ptr(pos), _lib.ptr(q), n, float(fac),
               _lib.ptr(elec_forces), _lib.ptr(phi_q), _lib.ptr(psi), _lib.ptr(ef_all),
-              _lib.ptr(psi_fourier), _lib.ptr(pm.pic_sums), _lib.stream_ptr())
+              _lib.ptr(psi_fourier), _lib.ptr(pm.pic_sums), None, _lib.stream_ptr())
     # the charges of this evaluation, for the FP64 energy / pressure
     pm.pic_charges = q
 

@@ -84,9 +84,9 @@ class RespaMD:
         # memsets not counted): field step = paint, finalize, k-space, readout
         field = 4 + (4 if charges is not None else 0)
         if self.plan is not None:
-            self.launches_per_step = 1 + field + 1
+            self.launches_per_step = 1 + field  # second kick fused into the readout
         else:
-            self.launches_per_step = 2 + self.respa * (1 + kinds) + 1 + field
+            self.launches_per_step = 1 + self.respa * (1 + kinds) + 1 + field
 
     def _make_plan(self, packed, max_block_beads):
         (b2a, b2b, b2r, b2k, b3a, b3b, b3c, b3t, b3k,
@@ -176,6 +176,7 @@ class RespaMD:
             self.launches_per_step += 1 if thermostat else 0
         else:
             self.launches_per_step += (1 if thermostat else 0) + (2 if barostat else 0)
+        # (the CSVR sums ride in the readout; its scaling is one more launch)
 
     def _thermostat(self, st, kick=False):
         """CSVR; with kick=True the second outer half kick runs in the same
@@ -252,14 +253,36 @@ class RespaMD:
                 _lib.ptr(self.f_angle) if t.n_angles else None,
                 _lib.ptr(self.f_dih) if t.n_dihedrals else None)
 
-    def _field(self, st, sums=None, pos_scale=None):
+    def _kick_args(self, thermostat):
+        """HpfKick for the second outer half kick fused into the last readout
+        (with the CSVR sums when the thermostat is on)."""
+        k = _lib.Kick()
+        k.v = self.v.data_ptr()
+        if self.charges is not None:
+            k.prev[0] = self.f_field.data_ptr()  # field first, then the electrostatic force
+            k.n_prev = 1
+        k.mass = self.mass
+        k.dt_outer = self.respa * self.dt
+        if thermostat:
+            k.thermo = _lib.ctypes.pointer(self.thermo_args)
+            k.group = self.group.data_ptr() if self.group is not None else None
+            k.randoms = self.randoms.data_ptr()
+            k.counter = self.counter.data_ptr()
+            k.state = self.state.data_ptr()
+            k.ws = self.ws_md.data_ptr()
+            k.d_err = self.err.data_ptr()
+        self._kick_keep = k
+        return _lib.ctypes.byref(k)
+
+    def _field(self, st, sums=None, pos_scale=None, kick=None):
+        last_kick = kick if self.charges is None else None
         _lib.call("hpf_field_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.types), self.n,
                   self.masses, _lib.ptr(self.f_field), _lib.ptr(sums),
-                  None if pos_scale is None else _lib.ctypes.c_void_p(pos_scale), st)
+                  None if pos_scale is None else _lib.ctypes.c_void_p(pos_scale), last_kick, st)
         if self.charges is not None:
             _lib.call("hpf_pic_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.charges),
                       self.n, float(self.elec_factor), _lib.ptr(self.f_elec), None, None, None,
-                      None, None, st)
+                      None, None, kick, st)
 
     def prime(self):
         """Bonded and slow forces at the initial positions (main.py:494-588)."""
@@ -316,11 +339,12 @@ class RespaMD:
                 self.bonded_out[0:4].copy_(self.ws_bond[:4])
                 self.bonded_out[4:8].copy_(self.ws_angle[:4])
                 self._barostat(st)
-        self._field(st, self.field_sums, pos_scale=scale)
-        if self.thermo_args is not None:
-            self._thermostat(st, kick=True)
-        else:
-            self._outer_kick(st)
+        # second outer half kick (and the CSVR sums) fused into the last readout
+        thermo = self.thermo_args is not None
+        self._field(st, self.field_sums, pos_scale=scale, kick=self._kick_args(thermo))
+        if thermo:
+            _lib.call("hpf_csvr_scale", _lib.ptr(self.v), _lib.ptr(self.group), self.n,
+                      _lib.ptr(self.state), int(self.thermo_args.remove_com), st)
 
     def capture(self):
         """Record one outer step in a CUDA graph (after a warm-up step)."""

@@ -51,6 +51,57 @@ typedef struct hpf_ctx hpf_ctx; /* mesh context: geometry, cuFFT plans, scratch 
 #define HPF_REDUCE_BLOCKS 1024
 #define HPF_OUT_DOUBLES (8 + 8 * HPF_REDUCE_BLOCKS + 8)
 
+/* ---- thermostat / barostat on the device -----------------------------------
+ * The random numbers are drawn on the host in the reference's order (numpy
+ * Generator: barostat normal(), then per thermostat group normal() and
+ * chisquare(N_f - 1)) into a device table with one row per outer step; a
+ * device step counter selects the row, so captured graphs replay them. */
+typedef struct {
+    int n_groups;       /* coupling groups, 1 or 2 (group ids from `group`)      */
+    int remove_com;     /* remove / restore each group's centre-of-mass velocity */
+    int n_steps;        /* rows in the random table                              */
+    int stride;         /* doubles per row                                       */
+    int offset;         /* row[offset + 2g] = R, row[offset + 2g + 1] = chi^2    */
+    int advance;        /* increment the step counter afterwards                 */
+    int every;          /* act when (step + 1) % every == 0 (n_b)                */
+    int pad;
+    double count[2];    /* particles per group                                   */
+    double mass, gas_constant, target_temperature;
+    double c;           /* exp(-dt_outer / tau)                                  */
+} HpfCsvrArgs;
+
+typedef struct {
+    int n_types, n_steps, stride, advance;
+    int every, pad[3];
+    double half_mQm;        /* 1/2 mc.Q.mc with mc_t = m_t N_t (paint mass x count),
+                               so the k = 0 densities are mc_t / V               */
+    double mass, gas_constant, target_temperature;
+    double target_pressure; /* bar                                              */
+    double beta;            /* isothermal compressibility (1/bar)               */
+    double tau_p, dt_outer, n_b;
+} HpfScrArgs;
+
+/* Optional outer half kick fused into the last readout of a field
+ * evaluation (hymd/main.py:1143-1169): v += 0.5 dt_outer F/mass for each of
+ * the n_prev slow forces already computed (in order), then for the force
+ * this readout produces.  With thermo != NULL the same pass accumulates the
+ * per-group velocity sums and the grid's last block forms the CSVR scale
+ * factors (as hpf_csvr does, without applying them: call hpf_csvr_scale). */
+typedef struct {
+    float* v;
+    const float* prev[4];
+    int n_prev;
+    int pad;
+    double mass, dt_outer;
+    const HpfCsvrArgs* thermo;
+    const int32_t* group;
+    const double* randoms;
+    int* counter;
+    double* state;
+    double* ws;     /* reduction workspace (HPF_OUT_DOUBLES) */
+    int* d_err;
+} HpfKick;
+
 /* ---- context ------------------------------------------------------------
  * Replaces initialize_pm (hymd/field.py:10-149): builds the mesh geometry and
  * the cuFFT plans for n_types densities.  Allocates the paint accumulators,
@@ -143,10 +194,12 @@ int hpf_readout(hpf_ctx* ctx, const float* force_mesh, const float* pos,
  * hpf_kspace_force (may be NULL). */
 int hpf_field_step(hpf_ctx* ctx, float* pos, const int32_t* types, int64_t n,
                    const double* type_mass, float* force, double* sums,
-                   const double* pos_scale, void* stream);
+                   const double* pos_scale, const HpfKick* kick, void* stream);
 /* pos_scale (device double, may be NULL): when given, positions are first
  * rescaled in place, pos = float(*pos_scale) * pos -- the position update of
- * a barostat step (hymd/barostat_scr.py:128) fused into the paint. */
+ * a barostat step (hymd/barostat_scr.py:128) fused into the paint.
+ * kick (may be NULL): the outer half kick (and CSVR sums) fused into the
+ * readout, see HpfKick. */
 
 /* ---- PIC_Spectral electrostatics ------------------------------------------
  * update_field_force_q (hymd/field.py:241-403): paint q/dV -> r2c -> H ->
@@ -157,7 +210,8 @@ int hpf_field_step(hpf_ctx* ctx, float* pos, const int32_t* types, int64_t n,
  * W_elec = V/2 sums[0] - E_self (field.py:698-699).  elec_factor = k_e/eps. */
 int hpf_pic_step(hpf_ctx* ctx, const float* pos, const float* charges, int64_t n,
                  double elec_factor, float* elec_forces, float* phi_q, float* psi,
-                 float* elec_field, void* psi_k, double* sums, void* stream);
+                 float* elec_field, void* psi_k, double* sums, const HpfKick* kick,
+                 void* stream);
 
 /* ---- bonded (f2py calling form, hymd/force.py:8-23, main.py:509-550) ------
  * All three zero their force array first, as the Fortran does.  Indices are
@@ -228,35 +282,6 @@ int hpf_respa_plan_info(const hpf_respa_plan* plan, int* n_mol_blocks, int* n_fr
 /* hpf_respa_step (the launch itself) is declared after the barostat
  * arguments below. */
 
-/* ---- thermostat / barostat on the device -----------------------------------
- * The random numbers are drawn on the host in the reference's order (numpy
- * Generator: barostat normal(), then per thermostat group normal() and
- * chisquare(N_f - 1)) into a device table with one row per outer step; a
- * device step counter selects the row, so captured graphs replay them. */
-typedef struct {
-    int n_groups;       /* coupling groups, 1 or 2 (group ids from `group`)      */
-    int remove_com;     /* remove / restore each group's centre-of-mass velocity */
-    int n_steps;        /* rows in the random table                              */
-    int stride;         /* doubles per row                                       */
-    int offset;         /* row[offset + 2g] = R, row[offset + 2g + 1] = chi^2    */
-    int advance;        /* increment the step counter afterwards                 */
-    int every;          /* act when (step + 1) % every == 0 (n_b)                */
-    int pad;
-    double count[2];    /* particles per group                                   */
-    double mass, gas_constant, target_temperature;
-    double c;           /* exp(-dt_outer / tau)                                  */
-} HpfCsvrArgs;
-
-typedef struct {
-    int n_types, n_steps, stride, advance;
-    int every, pad[3];
-    double half_mQm;        /* 1/2 mc.Q.mc with mc_t = m_t N_t (paint mass x count),
-                               so the k = 0 densities are mc_t / V               */
-    double mass, gas_constant, target_temperature;
-    double target_pressure; /* bar                                              */
-    double beta;            /* isothermal compressibility (1/bar)               */
-    double tau_p, dt_outer, n_b;
-} HpfScrArgs;
 
 /* csvr_thermostat (hymd/thermostat.py:111-219) for up to two coupling groups.
  * state: device double[16] ([4g] alpha, [4g+1..3] COM velocity, [8+g]
@@ -267,6 +292,10 @@ int hpf_csvr(float* v, const int32_t* group, int64_t n, const float* const* kick
 /* kick_forces (n_kick arrays, may be 0): the second outer half kick
  * v += 0.5 kick_dt F/mass (hymd/main.py:1143-1169) applied in the same pass,
  * before the kinetic energy is taken. */
+/* The scaling half of hpf_csvr: v = (v - com_g) alpha_g + com_g (or
+ * v alpha_g without COM removal) from state (hymd/thermostat.py:210-217). */
+int hpf_csvr_scale(float* v, const int32_t* group, int64_t n, const double* state,
+                   int remove_com, void* stream);
 /* Stochastic cell rescaling, isotropic (hymd/barostat_scr.py:34-132): the
  * pressure from field_sums (device double[4] = A, B_xyz of the last field
  * evaluation, see hpf_kspace_force), bonded_out (device double[9] of

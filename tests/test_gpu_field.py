@@ -113,7 +113,7 @@ def test_update_field_and_forces_match_oracle(kind):
     from hymd_gb300 import _lib
     F2 = torch.zeros_like(R)
     _lib.call("hpf_field_step", pm._h, _lib.ptr(R), _lib.ptr(Ty), R.shape[0], _lib.dvec(cfg.m),
-              _lib.ptr(F2), None, None, _lib.stream_ptr())
+              _lib.ptr(F2), None, None, None, _lib.stream_ptr())
     assert rel_rms(F2.cpu().numpy(), F.cpu().numpy()) < 1e-6
     pm.check_errors()
 
