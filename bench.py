@@ -190,6 +190,44 @@ def run_reference(args):
     return 0
 
 
+def step_breakdown(md, flush, torch, reps=10):
+    """Per-phase device time of one eager MD step (CUDA events on the
+    launching stream; L2 flushed once before each step, as in the timed
+    loop).  Diagnostic only; printed to stderr."""
+    from hymd_gb300 import _lib
+    st = torch.cuda.current_stream()
+    names = ["respa", "field", "pic", "thermostat_scale"]
+    tot = {k: 0.0 for k in names}
+    for _ in range(reps):
+        flush.zero_()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        s = _lib.stream_ptr()
+        ev[0].record(st)
+        md._inner_fused(s)
+        ev[1].record(st)
+        thermo = md.thermo_args is not None
+        scale = md.state.data_ptr() + 12 * 8 if md.baro_args is not None else None
+        kick = md._kick_args(thermo)
+        _lib.call("hpf_field_step", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n,
+                  md.masses, _lib.ptr(md.f_field), _lib.ptr(md.field_sums),
+                  None if scale is None else _lib.ctypes.c_void_p(scale),
+                  kick if md.charges is None else None, s)
+        ev[2].record(st)
+        if md.charges is not None:
+            _lib.call("hpf_pic_step", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.charges), md.n,
+                      float(md.elec_factor), _lib.ptr(md.f_elec), None, None, None, None, None,
+                      kick, s)
+        ev[3].record(st)
+        if thermo:
+            _lib.call("hpf_csvr_scale", _lib.ptr(md.v), _lib.ptr(md.group), md.n,
+                      _lib.ptr(md.state), int(md.thermo_args.remove_com), s)
+        ev[4].record(st)
+        ev[4].synchronize()
+        for k, (a, b) in zip(names, zip(ev[:-1], ev[1:])):
+            tot[k] += a.elapsed_time(b) * 1000.0 / reps
+    return tot
+
+
 def run_gpu(args):
     import torch
 
@@ -245,6 +283,8 @@ def run_gpu(args):
     ms_step = ms / args.steps
     sps = 1000.0 / ms_step
     md.check_errors()
+    if args.breakdown and rank == 0:
+        print(json.dumps({"breakdown_us": step_breakdown(md, flush, torch)}), file=sys.stderr)
 
     # ---- end to end through the public API with host buffers -------------
     r_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
@@ -322,6 +362,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="hpf", choices=["hpf", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--breakdown", action="store_true",
+                    help="also print per-phase step times (us) to stderr")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -108,11 +108,12 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                                           float* __restrict__ transfer, float (&acc)[kOut],
                                           Sync sync) {
     const int s0 = p.grp_bead[grp], nb = p.grp_bead[grp + 1] - s0;
+    const float inv_m = 1.0f / mass;
     for (int e = lane; e < 3 * nb; e += width) {
         const int i = e / 3, d = e - 3 * i;
         const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
         float x = v[g];
-        for (int q = 0; q < slow.n; ++q) x = x + h_out * (slow.f[q][g] / mass);
+        for (int q = 0; q < slow.n; ++q) x = x + h_out * div_m(slow.f[q][g], mass, inv_m);
         vs[e] = x;
         rs[e] = r[g];
         fs[e] = fb[g];
@@ -125,14 +126,18 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
         const bool last_it = it == respa - 1;
         // closing half kick of the previous inner step (same forces), the
         // opening half kick of this one, drift and wrap; clear forces
-        for (int e = lane; e < 3 * nb; e += width) {
-            const float a = fs[e] / mass;
-            float x = vs[e];
-            if (it > 0) x = x + hdt * a;
-            x = x + hdt * a;
-            vs[e] = x;
-            rs[e] = wrapf(rs[e] + dt * x, bx.L[e % 3]);
-            fs[e] = 0.0f;
+        for (int i = lane; i < nb; i += width) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const int e = 3 * i + d;
+                const float a = div_m(fs[e], mass, inv_m);
+                float x = vs[e];
+                if (it > 0) x = x + hdt * a;
+                x = x + hdt * a;
+                vs[e] = x;
+                rs[e] = wrapf(rs[e] + dt * x, bx.L[d]);
+                fs[e] = 0.0f;
+            }
         }
         sync();
         for (int t = b0 + lane; t < b1; t += width) {
@@ -216,7 +221,7 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
     for (int e = lane; e < 3 * nb; e += width) {
         const int i = e / 3, d = e - 3 * i;
         const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
-        const float a = fs[e] / mass;
+        const float a = div_m(fs[e], mass, inv_m);
         const float x = vs[e] + hdt * a;
         v[g] = x;
         r[g] = rs[e];
@@ -234,7 +239,8 @@ __device__ __forceinline__ void free_beads(const hpf_respa_plan& p, int fblock, 
         const int64_t g = 3 * (int64_t)p.free_ids[j];
         for (int d = 0; d < 3; ++d) {
             float x = v[g + d];
-            for (int q = 0; q < slow.n; ++q) x = x + h_out * (slow.f[q][g + d] / mass);
+            for (int q = 0; q < slow.n; ++q)
+                x = x + h_out * div_m(slow.f[q][g + d], mass, 1.0f / mass);
             float y = r[g + d];
             for (int it = 0; it < respa; ++it) y = wrapf(y + dt * x, bx.L[d]);
             v[g + d] = x;

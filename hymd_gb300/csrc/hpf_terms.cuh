@@ -53,13 +53,17 @@ __device__ __forceinline__ V3 min_image(V3 r, const Box& b) {
 }
 
 // Harmonic bond between a and b.  Returns the force on b (minus on a);
-// e = 1/2 k (|r|-r0)^2; vir = fa * rab (componentwise, bond_pr).
+// e = 1/2 k (|r|-r0)^2; vir = fa * rab (componentwise, bond_pr).  Lengths
+// and their reciprocals come from one rsqrt (<= 2 ulp), which keeps the term
+// free of divisions.
 __device__ __forceinline__ V3 bond_term(V3 pa, V3 pb, float r0, float k, const Box& bx,
                                         float& e, V3& vir) {
     const V3 rab = min_image(pb - pa, bx);
-    const float rn = norm(rab);
+    const float d2 = dot(rab, rab);
+    const float ir = rsqrtf(d2);
+    const float rn = d2 * ir;
     const float dr = rn - r0;
-    const V3 fa = (-k * dr / rn) * rab;
+    const V3 fa = (-k * dr * ir) * rab;
     e = 0.5f * k * dr * dr;
     vir = v3(fa.x * rab.x, fa.y * rab.y, fa.z * rab.z);
     return fa;
@@ -72,20 +76,32 @@ __device__ __forceinline__ bool angle_term(V3 pa, V3 pb, V3 pc, float t0, float 
                                            V3& ga, V3& gc, float& e, V3& vir) {
     const V3 ra = min_image(pa - pb, bx);
     const V3 rc = min_image(pc - pb, bx);
-    const float na_ = norm(ra), nc_ = norm(rc);
-    const V3 ea = (1.0f / na_) * ra, ec = (1.0f / nc_) * rc;
+    const float ia = rsqrtf(dot(ra, ra)), ic = rsqrtf(dot(rc, rc));
+    const V3 ea = ia * ra, ec = ic * rc;
     const float cosphi = dot(ea, ec);
-    const float sinphi = norm(cross(ea, ec));
-    if (!(sinphi > 0.0f)) return false;
+    const V3 cr = cross(ea, ec);
+    const float s2 = dot(cr, cr);
+    if (!(s2 > 0.0f)) return false;
+    const float is = rsqrtf(s2);
+    const float sinphi = s2 * is;
     const float theta = atan2f(sinphi, cosphi);
     const float d = theta - t0;
     const float ff = k * d;
-    ga = (-ff / (na_ * sinphi)) * (ec - cosphi * ea);
-    gc = (-ff / (nc_ * sinphi)) * (ea - cosphi * ec);
+    ga = (-ff * ia * is) * (ec - cosphi * ea);
+    gc = (-ff * ic * is) * (ea - cosphi * ec);
     e = 0.5f * ff * d;
     vir = v3(-(ga.x * ra.x) - (gc.x * rc.x), -(ga.y * ra.y) - (gc.y * rc.y),
              -(ga.z * ra.z) - (gc.z * rc.z));
     return true;
+}
+
+// f / m for a fixed m with a precomputed reciprocal: one product and one FMA
+// correction step (Markstein), which gives the correctly rounded quotient
+// except in rare ties -- the FP32 F/m of the reference's integrate_velocity.
+__device__ __forceinline__ float div_m(float f, float m, float inv_m) {
+    const float q = f * inv_m;
+    const float r = fmaf(-q, m, f);
+    return fmaf(r, inv_m, q);
 }
 
 __device__ __forceinline__ void cosine_series(const float* cn, const float* dn, float phi,
