@@ -191,40 +191,53 @@ def run_reference(args):
 
 
 def step_breakdown(md, flush, torch, reps=10):
-    """Per-phase device time of one eager MD step (CUDA events on the
-    launching stream; L2 flushed once before each step, as in the timed
-    loop).  Diagnostic only; printed to stderr."""
+    """Per-stage device time of one MD step (diagnostic, printed to stderr):
+    the fused rRESPA kernel timed as a captured graph, the field step by
+    hpf_field_step_profile (CUDA events between its stages), the thermostat
+    scaling as a graph.  L2 is flushed before each repetition."""
     from hymd_gb300 import _lib
     st = torch.cuda.current_stream()
-    names = ["respa", "field", "pic", "thermostat_scale"]
+
+    def graph(fn):
+        s = torch.cuda.Stream()
+        s.wait_stream(st)
+        with torch.cuda.stream(s):
+            fn()
+        st.wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            fn()
+        return g
+
+    thermo = md.thermo_args is not None
+    g_respa = graph(lambda: md._inner_fused(_lib.stream_ptr()))
+    g_scale = graph(lambda: _lib.call("hpf_csvr_scale", _lib.ptr(md.v), _lib.ptr(md.group),
+                                      md.n, _lib.ptr(md.state),
+                                      int(md.thermo_args.remove_com) if thermo else 1,
+                                      _lib.stream_ptr()))
+    names = ["respa", "paint", "r2c", "kspace", "c2r", "readout_kick", "thermostat_scale"]
     tot = {k: 0.0 for k in names}
+    us = (_lib.ctypes.c_float * 5)()
     for _ in range(reps):
         flush.zero_()
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
-        s = _lib.stream_ptr()
-        ev[0].record(st)
-        md._inner_fused(s)
-        ev[1].record(st)
-        thermo = md.thermo_args is not None
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        g_respa.replay()
+        b.record(st)
+        b.synchronize()
+        tot["respa"] += a.elapsed_time(b) * 1000.0 / reps
         scale = md.state.data_ptr() + 12 * 8 if md.baro_args is not None else None
-        kick = md._kick_args(thermo)
-        _lib.call("hpf_field_step", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n,
+        _lib.call("hpf_field_step_profile", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n,
                   md.masses, _lib.ptr(md.f_field), _lib.ptr(md.field_sums),
                   None if scale is None else _lib.ctypes.c_void_p(scale),
-                  kick if md.charges is None else None, s)
-        ev[2].record(st)
-        if md.charges is not None:
-            _lib.call("hpf_pic_step", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.charges), md.n,
-                      float(md.elec_factor), _lib.ptr(md.f_elec), None, None, None, None, None,
-                      kick, s)
-        ev[3].record(st)
-        if thermo:
-            _lib.call("hpf_csvr_scale", _lib.ptr(md.v), _lib.ptr(md.group), md.n,
-                      _lib.ptr(md.state), int(md.thermo_args.remove_com), s)
-        ev[4].record(st)
-        ev[4].synchronize()
-        for k, (a, b) in zip(names, zip(ev[:-1], ev[1:])):
-            tot[k] += a.elapsed_time(b) * 1000.0 / reps
+                  md._kick_args(thermo), _lib.stream_ptr(), us)
+        for k, x in zip(names[1:6], us):
+            tot[k] += x / reps
+        a.record(st)
+        g_scale.replay()
+        b.record(st)
+        b.synchronize()
+        tot["thermostat_scale"] += a.elapsed_time(b) * 1000.0 / reps
     return tot
 
 

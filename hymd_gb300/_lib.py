@@ -94,6 +94,8 @@ _SIGNATURES.update({
     "hpf_field_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P, ctypes.POINTER(Kick), P],
     "hpf_pic_step": [P, P, P, I64, D, P, P, P, P, P, P, ctypes.POINTER(Kick), P],
     "hpf_csvr_scale": [P, P, I64, P, I, P],
+    "hpf_field_step_profile": [P, P, P, I64, ctypes.POINTER(D), P, P, P, ctypes.POINTER(Kick), P,
+                               ctypes.POINTER(ctypes.c_float)],
     "hpf_csvr": [P, P, I64, ctypes.POINTER(P), I, D, ctypes.POINTER(CsvrArgs), P, P, P, P, P, P],
     "hpf_scr_isotropic": [P, P, P, I64, P, P, ctypes.POINTER(ScrArgs), P, P, P, P, P, P],
 })

@@ -988,6 +988,38 @@ int hpf_field_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
     return HPF_OK;
 }
 
+int hpf_field_step_profile(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
+                           const double* type_mass, float* force, double* sums,
+                           const double* pos_scale, const HpfKick* kick, void* stream,
+                           float* us_out) {
+    if (!c || !type_mass || !us_out || n <= 0 || !pos || !types || !force) return HPF_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    cudaEvent_t ev[6];
+    for (int i = 0; i < 6; ++i) HPF_CUDA_TRY(cudaEventCreate(&ev[i]));
+    TypeScale sc;
+    for (int t = 0; t < c->T; ++t) sc.s[t] = (float)type_mass[t];
+    int r = HPF_OK;
+    cudaEventRecord(ev[0], st);
+    if (!r) r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale);
+    cudaEventRecord(ev[1], st);
+    if (!r) r = exec_r2c(c, c->d_grid, c->d_spec_phi, c->T, st);
+    cudaEventRecord(ev[2], st);
+    if (!r) r = launch_kspace_force(c, c->d_spec_phi, c->d_spec, nullptr, nullptr, sums, st);
+    cudaEventRecord(ev[3], st);
+    if (!r) r = exec_c2r(c, c->d_spec, c->d_grid, 3 * c->T, st);
+    cudaEventRecord(ev[4], st);
+    if (!r) r = launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, kick, st);
+    cudaEventRecord(ev[5], st);
+    cudaEventSynchronize(ev[5]);
+    for (int i = 0; i < 5; ++i) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+        us_out[i] = 1000.0f * ms;
+    }
+    for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+    return r;
+}
+
 int hpf_pic_step(hpf_ctx* c, const float* pos, const float* charges, int64_t n,
                  double elec_factor, float* elec_forces, float* phi_q, float* psi,
                  float* elec_field, void* psi_k, double* sums, const HpfKick* kick,

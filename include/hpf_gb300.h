@@ -195,6 +195,14 @@ int hpf_readout(hpf_ctx* ctx, const float* force_mesh, const float* pos,
 int hpf_field_step(hpf_ctx* ctx, float* pos, const int32_t* types, int64_t n,
                    const double* type_mass, float* force, double* sums,
                    const double* pos_scale, const HpfKick* kick, void* stream);
+/* Diagnostic: hpf_field_step with CUDA events between its stages; writes the
+ * stage times in microseconds to the HOST array us_out[5] = {paint (incl.
+ * fixed-point finalise), r2c, k-space, c2r, readout}.  Synchronises; not for
+ * use inside a graph. */
+int hpf_field_step_profile(hpf_ctx* ctx, float* pos, const int32_t* types, int64_t n,
+                           const double* type_mass, float* force, double* sums,
+                           const double* pos_scale, const HpfKick* kick, void* stream,
+                           float* us_out);
 /* pos_scale (device double, may be NULL): when given, positions are first
  * rescaled in place, pos = float(*pos_scale) * pos -- the position update of
  * a barostat step (hymd/barostat_scr.py:128) fused into the paint.
