@@ -28,6 +28,20 @@ struct TypeScale {
     float s[HPF_MAX_TYPES + 1];
 };
 
+// Paint deposits are integers in units of 2^-24 of a particle's weight (a
+// charge of up to 2^7 e keeps a deposit inside int32).
+constexpr float kFixScale = 16777216.0f;          // 2^24
+constexpr float kFixInv = 5.9604644775390625e-8f;  // 2^-24
+
+// int64 -> float without the 64-bit conversion instruction (FP64 pipe on
+// GB300): magnitude split into 32-bit halves, one FMA.  Deterministic.
+__device__ __forceinline__ float fix_to_float(long long x) {
+    const bool neg = x < 0;
+    const unsigned long long a = neg ? (unsigned long long)(-x) : (unsigned long long)x;
+    const float f = fmaf((float)(unsigned)(a >> 32), 4294967296.0f, (float)(unsigned)a);
+    return neg ? -f : f;
+}
+
 struct TypeScaleD {
     double s[HPF_MAX_TYPES + 1];
 };
@@ -91,7 +105,10 @@ __global__ void k_paint(const float* pos, const int32_t* __restrict__ types,
                 const float wab = q * wx[a] * wy[b];
 #pragma unroll
                 for (int c = 0; c < 2; ++c) {
-                    const long long v = __float2ll_rn(wab * wz[c] * 4294967296.0f);
+                    // fixed point in units of 2^-24 via an FP32 -> int32
+                    // conversion (a 64-bit one runs on the FP64 pipe), summed
+                    // in 64 bits
+                    const long long v = (long long)__float2int_rn(wab * wz[c] * kFixScale);
                     if (v != 0) atomicAdd(base + row + zs[c], (unsigned long long)v);
                 }
             }
@@ -100,26 +117,26 @@ __global__ void k_paint(const float* pos, const int32_t* __restrict__ types,
 
 // Fixed-point accumulators -> float density (times mass/dV), then clear the
 // accumulators for the next paint (so no separate memset is needed).
+// Grid: blockIdx.y = grid index g (type), x strides over the mesh.
 __global__ void k_paint_finalize(unsigned long long* __restrict__ acc, float* __restrict__ out,
                                  int64_t M, int G, TypeScale sc,
                                  const BoxState* __restrict__ bs) {
-    const float inv_dV = bs->inv_dV;
-    const int64_t total4 = (int64_t)G * M / 4;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total4;
+    const int g = blockIdx.y;
+    const float s = sc.s[g] * bs->inv_dV * kFixInv;
+    ulonglong2* a = reinterpret_cast<ulonglong2*>(acc + (int64_t)g * M);
+    float4* o4 = reinterpret_cast<float4*>(out + (int64_t)g * M);
+    const int64_t M4 = M / 4;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < M4;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t e = 4 * q;
-        const int g = (int)(e / M);
-        const float s = sc.s[g] * inv_dV * 2.3283064365386963e-10f;  // 2^-32
-        ulonglong2* p = reinterpret_cast<ulonglong2*>(acc + e);
-        const ulonglong2 a0 = p[0], a1 = p[1];
+        const ulonglong2 a0 = a[2 * q], a1 = a[2 * q + 1];
         float4 o;
-        o.x = __ll2float_rn((long long)a0.x) * s;
-        o.y = __ll2float_rn((long long)a0.y) * s;
-        o.z = __ll2float_rn((long long)a1.x) * s;
-        o.w = __ll2float_rn((long long)a1.y) * s;
-        reinterpret_cast<float4*>(out)[q] = o;
-        p[0] = make_ulonglong2(0ull, 0ull);
-        p[1] = make_ulonglong2(0ull, 0ull);
+        o.x = fix_to_float((long long)a0.x) * s;
+        o.y = fix_to_float((long long)a0.y) * s;
+        o.z = fix_to_float((long long)a1.x) * s;
+        o.w = fix_to_float((long long)a1.y) * s;
+        o4[q] = o;
+        a[2 * q] = make_ulonglong2(0ull, 0ull);
+        a[2 * q + 1] = make_ulonglong2(0ull, 0ull);
     }
 }
 
@@ -127,12 +144,12 @@ __global__ void k_paint_finalize(unsigned long long* __restrict__ acc, float* __
 __global__ void k_paint_finalize1(unsigned long long* __restrict__ acc, float* __restrict__ out,
                                   int64_t M, int G, TypeScale sc,
                                   const BoxState* __restrict__ bs) {
-    const float inv_dV = bs->inv_dV;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)G * M;
+    const int g = blockIdx.y;
+    const float s = sc.s[g] * bs->inv_dV * kFixInv;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int g = (int)(e / M);
-        out[e] = __ll2float_rn((long long)acc[e]) * (sc.s[g] * inv_dV * 2.3283064365386963e-10f);
-        acc[e] = 0ull;
+        out[(int64_t)g * M + e] = fix_to_float((long long)acc[(int64_t)g * M + e]) * s;
+        acc[(int64_t)g * M + e] = 0ull;
     }
 }
 
@@ -406,7 +423,7 @@ __global__ void k_paint_finalize_f64(unsigned long long* __restrict__ acc,
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)G * M;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int g = (int)(e / M);
-        out[e] = (double)(long long)acc[e] * (sc.s[g] * inv_dV * 2.3283064365386963e-10);
+        out[e] = (double)(long long)acc[e] * (sc.s[g] * inv_dV * (double)kFixInv);
         acc[e] = 0ull;
     }
 }
@@ -568,12 +585,12 @@ int do_paint(hpf_ctx* c, const float* pos, const int32_t* types, const float* ch
                                                            c->M, c->d_err, scale);
         HPF_LAUNCH_CHECK();
     }
-    if (c->M % 4 == 0) {  // float4 groups never straddle two grids
-        k_paint_finalize<<<grid_for((int64_t)G * c->M / 4, kThreads), kThreads, 0, st>>>(
-            acc, out, c->M, G, sc, c->d_box);
+    if (c->M % 4 == 0) {
+        dim3 grid(grid_for(c->M / 4, kThreads), G);
+        k_paint_finalize<<<grid, kThreads, 0, st>>>(acc, out, c->M, G, sc, c->d_box);
     } else {
-        k_paint_finalize1<<<grid_for((int64_t)G * c->M, kThreads), kThreads, 0, st>>>(
-            acc, out, c->M, G, sc, c->d_box);
+        dim3 grid(grid_for(c->M, kThreads), G);
+        k_paint_finalize1<<<grid, kThreads, 0, st>>>(acc, out, c->M, G, sc, c->d_box);
     }
     HPF_LAUNCH_CHECK();
     return HPF_OK;

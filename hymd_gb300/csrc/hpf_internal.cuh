@@ -279,41 +279,61 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double* smem /* K*3
     }
 }
 
-// Same reduction for FP32 per-thread partial sums (a thread adds only a few
-// terms): the warp sums in FP32, everything above the warp in FP64.  GB300's
-// FP64 rate is a small fraction of its FP32 rate, so hot kernels keep FP64
-// arithmetic out of the per-element path.  Returns true on thread 0 of the
+// Compensated ("double-float") sum of two (hi, lo) FP32 pairs: TwoSum of the
+// high parts, then the low parts folded in and renormalised.  About 48
+// significant bits, using only the FP32 pipe.
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    const float hi = s + e;
+    return DF{hi, e - (hi - s)};
+}
+
+__device__ __forceinline__ DF df_shfl_down(DF v, int o) {
+    return DF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+// Deterministic grid-wide sum of FP32 per-thread values (a thread adds only a
+// few terms) with compensated double-float arithmetic above the thread: warp,
+// block and the last block's pass over the block partials (stored as (hi, lo)
+// pairs) all run on the FP32 pipe -- GB300's FP64 pipe is a small fraction of
+// its FP32 one, and FP64 shuffles/adds in every block were a visible share of
+// short kernels.  out[k] = hi + lo in FP64.  Returns true on thread 0 of the
 // last block, after out[] has been written (for a fused epilogue).
 template <int K>
 __device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* partials,
                                                     unsigned int* ticket, double* out) {
-    __shared__ double red[K * 32];
+    __shared__ float2 red[K * 32];
     __shared__ bool is_last;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) vf[k] += __shfl_down_sync(0xffffffffu, vf[k], o);
-    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (blockDim.x + 31) >> 5;
-    if (lane == 0) {
+    DF v[K];
 #pragma unroll
-        for (int k = 0; k < K; ++k) red[k * 32 + warp] = (double)vf[k];
+    for (int k = 0; k < K; ++k) {
+        v[k] = DF{vf[k], 0.0f};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = df_add(v[k], df_shfl_down(v[k], o));
+        if (lane == 0) red[k * 32 + warp] = make_float2(v[k].hi, v[k].lo);
     }
     __syncthreads();
-    double v[K];
+    float2* part = reinterpret_cast<float2*>(partials);
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            double x = lane < nw ? red[k * 32 + lane] : 0.0;
+            const float2 x = lane < nw ? red[k * 32 + lane] : make_float2(0.0f, 0.0f);
+            DF s{x.x, x.y};
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-            v[k] = x;
+            for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
+            if (lane == 0) part[(size_t)blockIdx.x * K + k] = make_float2(s.hi, s.lo);
         }
     }
     if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) partials[(size_t)blockIdx.x * K + k] = v[k];
         __threadfence();
         unsigned int t = atomicAdd(ticket, 1u);
         is_last = (t == gridDim.x - 1);
@@ -321,18 +341,35 @@ __device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* part
     __syncthreads();
     if (!is_last) return false;
     __threadfence();
-    double acc[K];
+    DF acc[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    for (int k = 0; k < K; ++k) acc[k] = DF{0.0f, 0.0f};
     for (unsigned int bI = threadIdx.x; bI < gridDim.x; bI += blockDim.x) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) acc[k] += ((volatile double*)partials)[(size_t)bI * K + k];
+        for (int k = 0; k < K; ++k) {
+            const float2 x = __ldcg(part + (size_t)bI * K + k);
+            acc[k] = df_add(acc[k], DF{x.x, x.y});
+        }
     }
     __syncthreads();
-    block_reduce<K>(acc, red);
-    if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) out[k] = acc[k];
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k] = df_add(acc[k], df_shfl_down(acc[k], o));
+        if (lane == 0) red[k * 32 + warp] = make_float2(acc[k].hi, acc[k].lo);
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float2 x = lane < nw ? red[k * 32 + lane] : make_float2(0.0f, 0.0f);
+            DF s{x.x, x.y};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
+            if (lane == 0) out[k] = (double)s.hi + (double)s.lo;
+        }
+    }
+    if (threadIdx.x == 0) {
         *ticket = 0u;
         return true;
     }
