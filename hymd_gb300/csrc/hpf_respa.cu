@@ -6,18 +6,23 @@
 // planner (host C++) finds the molecules as connected components of the
 // bonded terms, packs them into groups of at most `max_group_beads` beads and
 // rewrites every term with group-local bead indices.  One launch then:
-//   * molecule groups: load positions, velocities and bonded forces of the
-//     group's beads into shared memory, apply the first outer half kick with
+//   * molecule groups: stage positions, velocities, bonded forces and the
+//     group's topology in shared memory, apply the first outer half kick with
 //     the slow forces, run all inner steps on chip, write back.  Groups of up
-//     to 256 beads are run by one warp each (phases separated by __syncwarp);
+//     to 256 beads are run by one warp each (phases separated by __syncwarp),
 //     larger ones by a whole CTA (__syncthreads);
 //   * free beads (in no bonded term): per thread, the outer kick and
 //     respa_inner drift/wrap steps (their bonded force is zero).
+// Forces are accumulated without atomics: every term writes its force
+// vectors into its own shared-memory slots, then every bead adds the slots
+// that touch it in a fixed order (incidence lists built by the planner), so
+// the bonded forces are bit-deterministic.
 // Energies and virials of the last inner step (the ones the reference keeps,
-// main.py:964-973) and sum v^2 are reduced in FP64 by the grid's last block,
-// which can also run the isotropic SCR barostat (hymd/barostat_scr.py:34-132)
-// right there, since the barostat follows the inner loop (main.py:889-963).
+// main.py:964-973) and sum v^2 are reduced by the grid's last block, which can
+// also run the isotropic SCR barostat (hymd/barostat_scr.py:34-132) right
+// there, since the barostat follows the inner loop (main.py:889-963).
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 #include <vector>
 
@@ -28,19 +33,23 @@ struct hpf_respa_plan {
     int64_t n_beads;
     int n_groups;        // molecule groups
     int n_free;
-    int max_group_beads;
     int n_free_blocks;
     int warp_mode;       // 1: one warp per group, 0: one CTA per group
     int has_dih;
+    // per-group maxima (shared-memory layout)
+    int mx_beads, mx_slots, mx_inc, mx_bonds, mx_angles;
+    size_t smem_group;   // bytes per group
     size_t smem;         // dynamic shared memory per block
     // device arrays
     int* grp_bead;    // [n_groups+1]
     int* bead_ids;    // bonded beads, group-major
+    int* bead_inc;    // [n_bonded_beads+1] incidence list starts (group-major beads)
+    int* inc_list;    // (slot << 1) | negative, slot local to the group
     int* grp_bond;    // [n_groups+1]
-    short2* bond_ij;  // local indices
+    int* bond_ij;     // local indices, i | j << 16
     float2* bond_p;   // (r0, k)
     int* grp_ang;
-    short4* ang_ijk;
+    int2* ang_ijk;    // (i | j << 16, k)
     float2* ang_p;    // (t0, k)
     int* grp_dih;
     short4* dih_ijkl;
@@ -96,64 +105,153 @@ struct CtaSync {
     __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
+// Shared-memory layout of one group (offsets in bytes, 16-byte aligned).
+struct GroupSmem {
+    float2 *bond_p, *ang_p;
+    int2* ang_ijk;
+    float *rs, *vs, *fs, *slot;
+    int *bond_ij, *inc_start, *inc;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline size_t group_smem_bytes(int nb, int ns, int ni, int nbd, int na) {
+    size_t o = 0;
+    o += align16(sizeof(float2) * nbd);  // bond_p
+    o += align16(sizeof(float2) * na);   // ang_p
+    o += align16(sizeof(int2) * na);     // ang_ijk
+    o += align16(sizeof(float) * 9 * nb);
+    o += align16(sizeof(float) * 3 * ns);
+    o += align16(sizeof(int) * nbd);
+    o += align16(sizeof(int) * (nb + 1));
+    o += align16(sizeof(int) * ni);
+    return o;
+}
+
+__device__ __forceinline__ GroupSmem carve(char* base, const hpf_respa_plan& p) {
+    GroupSmem g;
+    size_t o = 0;
+    g.bond_p = reinterpret_cast<float2*>(base + o);
+    o += align16(sizeof(float2) * p.mx_bonds);
+    g.ang_p = reinterpret_cast<float2*>(base + o);
+    o += align16(sizeof(float2) * p.mx_angles);
+    g.ang_ijk = reinterpret_cast<int2*>(base + o);
+    o += align16(sizeof(int2) * p.mx_angles);
+    g.rs = reinterpret_cast<float*>(base + o);
+    g.vs = g.rs + 3 * p.mx_beads;
+    g.fs = g.rs + 6 * p.mx_beads;
+    o += align16(sizeof(float) * 9 * p.mx_beads);
+    g.slot = reinterpret_cast<float*>(base + o);
+    o += align16(sizeof(float) * 3 * p.mx_slots);
+    g.bond_ij = reinterpret_cast<int*>(base + o);
+    o += align16(sizeof(int) * p.mx_bonds);
+    g.inc_start = reinterpret_cast<int*>(base + o);
+    o += align16(sizeof(int) * (p.mx_beads + 1));
+    g.inc = reinterpret_cast<int*>(base + o);
+    return g;
+}
+
+__device__ __forceinline__ void put3(float* s, int slot, V3 v) {
+    s[3 * slot] = v.x;
+    s[3 * slot + 1] = v.y;
+    s[3 * slot + 2] = v.z;
+}
+
 // Group-local work shared by the warp and CTA variants.  `lane`/`width`
-// enumerate the threads of the group; `sync()` separates the phases.
+// enumerate the threads of the group; `sync()` separates the phases.  A
+// bead is always handled by the same lane, so the gather of its forces and
+// its next kick need no barrier in between.
 template <bool DIH, typename Sync>
 __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int lane, int width,
-                                          float* rs, float* vs, float* fs, float* __restrict__ r,
+                                          char* smem_base, float* __restrict__ r,
                                           float* __restrict__ v, float* __restrict__ fb,
                                           const SlowForces& slow, float mass, float h_out,
                                           float hdt, float dt, int respa, const Box& bx,
                                           float* __restrict__ dipoles,
                                           float* __restrict__ transfer, float (&acc)[kOut],
                                           Sync sync) {
+    const GroupSmem s = carve(smem_base, p);
     const int s0 = p.grp_bead[grp], nb = p.grp_bead[grp + 1] - s0;
+    const int b0 = p.grp_bond[grp], nbd = p.grp_bond[grp + 1] - b0;
+    const int a0 = p.grp_ang[grp], na = p.grp_ang[grp + 1] - a0;
+    const int d0 = DIH ? p.grp_dih[grp] : 0, nd = DIH ? p.grp_dih[grp + 1] - d0 : 0;
+    const int i0 = p.bead_inc[s0];
     const float inv_m = 1.0f / mass;
+    // stage the group: beads (with the first outer half kick), topology
     for (int e = lane; e < 3 * nb; e += width) {
         const int i = e / 3, d = e - 3 * i;
         const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
         float x = v[g];
         for (int q = 0; q < slow.n; ++q) x = x + h_out * div_m(slow.f[q][g], mass, inv_m);
-        vs[e] = x;
-        rs[e] = r[g];
-        fs[e] = fb[g];
+        s.vs[e] = x;
+        s.rs[e] = r[g];
+        s.fs[e] = fb[g];
     }
+    for (int t = lane; t < nbd; t += width) {
+        s.bond_ij[t] = p.bond_ij[b0 + t];
+        s.bond_p[t] = p.bond_p[b0 + t];
+    }
+    for (int t = lane; t < na; t += width) {
+        s.ang_ijk[t] = p.ang_ijk[a0 + t];
+        s.ang_p[t] = p.ang_p[a0 + t];
+    }
+    for (int i = lane; i <= nb; i += width) s.inc_start[i] = p.bead_inc[s0 + i] - i0;
+    const int ninc = p.bead_inc[s0 + nb] - i0;
+    for (int t = lane; t < ninc; t += width) s.inc[t] = p.inc_list[i0 + t];
     sync();
-    const int b0 = p.grp_bond[grp], b1 = p.grp_bond[grp + 1];
-    const int a0 = p.grp_ang[grp], a1 = p.grp_ang[grp + 1];
-    const int d0 = DIH ? p.grp_dih[grp] : 0, d1 = DIH ? p.grp_dih[grp + 1] : 0;
-    for (int it = 0; it < respa; ++it) {
+    for (int it = 0; it <= respa; ++it) {
         const bool last_it = it == respa - 1;
-        // closing half kick of the previous inner step (same forces), the
-        // opening half kick of this one, drift and wrap; clear forces
+        // per bead: gather the bonded force of the previous inner step (in
+        // the fixed incidence order), closing half kick of that step; then,
+        // unless all steps are done, the opening half kick, drift and wrap
         for (int i = lane; i < nb; i += width) {
+            float F[3];
+            if (it == 0) {
+                F[0] = s.fs[3 * i];
+                F[1] = s.fs[3 * i + 1];
+                F[2] = s.fs[3 * i + 2];
+            } else {
+                F[0] = F[1] = F[2] = 0.0f;
+                for (int q = s.inc_start[i]; q < s.inc_start[i + 1]; ++q) {
+                    const int en = s.inc[q];
+                    const float* sl = s.slot + 3 * (en >> 1);
+                    if (en & 1) {
+                        F[0] -= sl[0];
+                        F[1] -= sl[1];
+                        F[2] -= sl[2];
+                    } else {
+                        F[0] += sl[0];
+                        F[1] += sl[1];
+                        F[2] += sl[2];
+                    }
+                }
+                s.fs[3 * i] = F[0];
+                s.fs[3 * i + 1] = F[1];
+                s.fs[3 * i + 2] = F[2];
+            }
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                const int e = 3 * i + d;
-                const float a = div_m(fs[e], mass, inv_m);
-                float x = vs[e];
+                const float a = div_m(F[d], mass, inv_m);
+                float x = s.vs[3 * i + d];
                 if (it > 0) x = x + hdt * a;
-                x = x + hdt * a;
-                vs[e] = x;
-                rs[e] = wrapf(rs[e] + dt * x, bx.L[d]);
-                fs[e] = 0.0f;
+                if (it < respa) {
+                    x = x + hdt * a;
+                    s.rs[3 * i + d] = wrapf(s.rs[3 * i + d] + dt * x, bx.L[d]);
+                }
+                s.vs[3 * i + d] = x;
             }
         }
+        if (it == respa) break;
         sync();
-        for (int t = b0 + lane; t < b1; t += width) {
-            const short2 ij = p.bond_ij[t];
-            const float2 pr = p.bond_p[t];
+        for (int t = lane; t < nbd; t += width) {
+            const int ij = s.bond_ij[t];
+            const int bi = ij & 0xffff, bj = ij >> 16;
+            const float2 pr = s.bond_p[t];
             float e;
             V3 vir;
-            const V3 pa = v3(rs[3 * ij.x], rs[3 * ij.x + 1], rs[3 * ij.x + 2]);
-            const V3 pb = v3(rs[3 * ij.y], rs[3 * ij.y + 1], rs[3 * ij.y + 2]);
-            const V3 fa = bond_term(pa, pb, pr.x, pr.y, bx, e, vir);
-            atomicAdd(fs + 3 * ij.x, -fa.x);
-            atomicAdd(fs + 3 * ij.x + 1, -fa.y);
-            atomicAdd(fs + 3 * ij.x + 2, -fa.z);
-            atomicAdd(fs + 3 * ij.y, fa.x);
-            atomicAdd(fs + 3 * ij.y + 1, fa.y);
-            atomicAdd(fs + 3 * ij.y + 2, fa.z);
+            const V3 pa = v3(s.rs[3 * bi], s.rs[3 * bi + 1], s.rs[3 * bi + 2]);
+            const V3 pb = v3(s.rs[3 * bj], s.rs[3 * bj + 1], s.rs[3 * bj + 2]);
+            put3(s.slot, t, bond_term(pa, pb, pr.x, pr.y, bx, e, vir));
             if (last_it) {
                 acc[0] += e;
                 acc[1] += vir.x;
@@ -161,24 +259,22 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                 acc[3] += vir.z;
             }
         }
-        for (int t = a0 + lane; t < a1; t += width) {
-            const short4 q = p.ang_ijk[t];
-            const float2 pr = p.ang_p[t];
-            const V3 pa = v3(rs[3 * q.x], rs[3 * q.x + 1], rs[3 * q.x + 2]);
-            const V3 pb = v3(rs[3 * q.y], rs[3 * q.y + 1], rs[3 * q.y + 2]);
-            const V3 pc = v3(rs[3 * q.z], rs[3 * q.z + 1], rs[3 * q.z + 2]);
+        for (int t = lane; t < na; t += width) {
+            const int2 q = s.ang_ijk[t];
+            const int ai = q.x & 0xffff, aj = q.x >> 16, ak = q.y;
+            const float2 pr = s.ang_p[t];
+            const V3 pa = v3(s.rs[3 * ai], s.rs[3 * ai + 1], s.rs[3 * ai + 2]);
+            const V3 pb = v3(s.rs[3 * aj], s.rs[3 * aj + 1], s.rs[3 * aj + 2]);
+            const V3 pc = v3(s.rs[3 * ak], s.rs[3 * ak + 1], s.rs[3 * ak + 2]);
             V3 ga, gc, vir;
             float e;
-            if (!angle_term(pa, pb, pc, pr.x, pr.y, bx, ga, gc, e, vir)) continue;
-            atomicAdd(fs + 3 * q.x, -ga.x);
-            atomicAdd(fs + 3 * q.x + 1, -ga.y);
-            atomicAdd(fs + 3 * q.x + 2, -ga.z);
-            atomicAdd(fs + 3 * q.z, -gc.x);
-            atomicAdd(fs + 3 * q.z + 1, -gc.y);
-            atomicAdd(fs + 3 * q.z + 2, -gc.z);
-            atomicAdd(fs + 3 * q.y, ga.x + gc.x);
-            atomicAdd(fs + 3 * q.y + 1, ga.y + gc.y);
-            atomicAdd(fs + 3 * q.y + 2, ga.z + gc.z);
+            if (!angle_term(pa, pb, pc, pr.x, pr.y, bx, ga, gc, e, vir)) {
+                ga = gc = v3(0.f, 0.f, 0.f);
+                e = 0.0f;
+                vir = ga;
+            }
+            put3(s.slot, nbd + 2 * t, ga);
+            put3(s.slot, nbd + 2 * t + 1, gc);
             if (last_it) {
                 acc[4] += e;
                 acc[5] += vir.x;
@@ -187,17 +283,17 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
             }
         }
         if (DIH) {
-            for (int t = d0 + lane; t < d1; t += width) {
-                const short4 q = p.dih_ijkl[t];
-                const int2 tl = p.dih_tl[t];
+            for (int t = lane; t < nd; t += width) {
+                const short4 q = p.dih_ijkl[d0 + t];
+                const int2 tl = p.dih_tl[d0 + t];
                 const int li[4] = {q.x, q.y, q.z, q.w};
                 V3 pos[4];
                 for (int j = 0; j < 4; ++j)
-                    pos[j] = v3(rs[3 * li[j]], rs[3 * li[j] + 1], rs[3 * li[j] + 2]);
+                    pos[j] = v3(s.rs[3 * li[j]], s.rs[3 * li[j] + 1], s.rs[3 * li[j] + 2]);
                 float* dip = nullptr;
                 float* tmx = nullptr;
                 if (last_it && dipoles) {
-                    const int64_t gd = p.dih_gid[t];
+                    const int64_t gd = p.dih_gid[d0 + t];
                     dip = dipoles + 12 * gd;
                     tmx = transfer + 54 * gd;
                     for (int j = 0; j < 12; ++j) dip[j] = 0.0f;
@@ -205,28 +301,25 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                 }
                 V3 F[4];
                 float e;
-                dihedral_term(pos[0], pos[1], pos[2], pos[3], p.dih_coeff + 30 * (int64_t)t, tl.x,
-                              tl.y, (last_it && dipoles) ? 1 : 0, bx, F, e, dip, tmx);
-                for (int j = 0; j < 4; ++j) {
-                    atomicAdd(fs + 3 * li[j], F[j].x);
-                    atomicAdd(fs + 3 * li[j] + 1, F[j].y);
-                    atomicAdd(fs + 3 * li[j] + 2, F[j].z);
-                }
+                dihedral_term(pos[0], pos[1], pos[2], pos[3],
+                              p.dih_coeff + 30 * (int64_t)(d0 + t), tl.x, tl.y,
+                              (last_it && dipoles) ? 1 : 0, bx, F, e, dip, tmx);
+                for (int j = 0; j < 4; ++j) put3(s.slot, nbd + 2 * na + 4 * t + j, F[j]);
                 if (last_it) acc[8] += e;
             }
         }
         sync();
     }
-    // closing half kick of the last inner step, write back
-    for (int e = lane; e < 3 * nb; e += width) {
-        const int i = e / 3, d = e - 3 * i;
-        const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
-        const float a = div_m(fs[e], mass, inv_m);
-        const float x = vs[e] + hdt * a;
-        v[g] = x;
-        r[g] = rs[e];
-        fb[g] = fs[e];
-        acc[9] = fmaf(x, x, acc[9]);
+    // write back (each bead by the lane that owns it)
+    for (int i = lane; i < nb; i += width) {
+        const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i];
+        for (int d = 0; d < 3; ++d) {
+            const float x = s.vs[3 * i + d];
+            v[g + d] = x;
+            r[g + d] = s.rs[3 * i + d];
+            fb[g + d] = s.fs[3 * i + d];
+            acc[9] = fmaf(x, x, acc[9]);
+        }
     }
 }
 
@@ -235,12 +328,12 @@ __device__ __forceinline__ void free_beads(const hpf_respa_plan& p, int fblock, 
                                            float mass, float h_out, float dt, int respa,
                                            const Box& bx, float (&acc)[kOut]) {
     const int stride = p.n_free_blocks * kThreads;
+    const float inv_m = 1.0f / mass;
     for (int j = fblock * kThreads + threadIdx.x; j < p.n_free; j += stride) {
         const int64_t g = 3 * (int64_t)p.free_ids[j];
         for (int d = 0; d < 3; ++d) {
             float x = v[g + d];
-            for (int q = 0; q < slow.n; ++q)
-                x = x + h_out * div_m(slow.f[q][g + d], mass, 1.0f / mass);
+            for (int q = 0; q < slow.n; ++q) x = x + h_out * div_m(slow.f[q][g + d], mass, inv_m);
             float y = r[g + d];
             for (int it = 0; it < respa; ++it) y = wrapf(y + dt * x, bx.L[d]);
             v[g + d] = x;
@@ -260,7 +353,7 @@ k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
              float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
              int respa, const double* __restrict__ box, float* __restrict__ dipoles,
              float* __restrict__ transfer, double* out, BaroFuse baro, int* err) {
-    extern __shared__ float smem[];
+    extern __shared__ __align__(16) char smem[];
     const Box bx = load_box(box);
     float acc[kOut];
 #pragma unroll
@@ -269,12 +362,9 @@ k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     if ((int)blockIdx.x < n_grp_blocks) {
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
         const int grp = blockIdx.x * kWarps + warp;
-        if (grp < p.n_groups) {
-            float* base = smem + (size_t)warp * 9 * p.max_group_beads;
-            run_group<DIH>(p, grp, lane, 32, base, base + 3 * p.max_group_beads,
-                           base + 6 * p.max_group_beads, r, v, fb, slow, mass, h_out, hdt, dt,
-                           respa, bx, dipoles, transfer, acc, WarpSync());
-        }
+        if (grp < p.n_groups)
+            run_group<DIH>(p, grp, lane, 32, smem + (size_t)warp * p.smem_group, r, v, fb, slow,
+                           mass, h_out, hdt, dt, respa, bx, dipoles, transfer, acc, WarpSync());
     } else {
         free_beads(p, blockIdx.x - n_grp_blocks, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
@@ -289,16 +379,14 @@ k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
             float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
             int respa, const double* __restrict__ box, float* __restrict__ dipoles,
             float* __restrict__ transfer, double* out, BaroFuse baro, int* err) {
-    extern __shared__ float smem[];
+    extern __shared__ __align__(16) char smem[];
     const Box bx = load_box(box);
     float acc[kOut];
 #pragma unroll
     for (int k = 0; k < kOut; ++k) acc[k] = 0.0f;
     if ((int)blockIdx.x < p.n_groups) {
-        const int nb = p.max_group_beads;
-        run_group<DIH>(p, blockIdx.x, threadIdx.x, kThreads, smem, smem + 3 * nb, smem + 6 * nb,
-                       r, v, fb, slow, mass, h_out, hdt, dt, respa, bx, dipoles, transfer, acc,
-                       CtaSync());
+        run_group<DIH>(p, blockIdx.x, threadIdx.x, kThreads, smem, r, v, fb, slow, mass, h_out,
+                       hdt, dt, respa, bx, dipoles, transfer, acc, CtaSync());
     } else {
         free_beads(p, blockIdx.x - p.n_groups, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
@@ -346,9 +434,10 @@ extern "C" {
 
 int hpf_respa_plan_destroy(hpf_respa_plan* p) {
     if (!p) return HPF_OK;
-    void* ptrs[] = {p->grp_bead, p->bead_ids, p->grp_bond, p->bond_ij, p->bond_p, p->grp_ang,
-                    p->ang_ijk, p->ang_p, p->grp_dih, p->dih_ijkl, p->dih_coeff, p->dih_tl,
-                    p->dih_gid, p->free_ids, p->partials, p->ticket};
+    void* ptrs[] = {p->grp_bead, p->bead_ids, p->bead_inc, p->inc_list, p->grp_bond,
+                    p->bond_ij,  p->bond_p,   p->grp_ang,  p->ang_ijk,  p->ang_p,
+                    p->grp_dih,  p->dih_ijkl, p->dih_coeff, p->dih_tl,  p->dih_gid,
+                    p->free_ids, p->partials, p->ticket};
     for (void* q : ptrs) cudaFree(q);
     delete p;
     return HPF_OK;
@@ -395,11 +484,9 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
         else free_ids.push_back((int)i);
     }
     for (int64_t i = 0; i < n; ++i) largest = std::max(largest, comp_size[i]);
-    // a group must fit in shared memory (36 bytes per bead); a warp takes
-    // groups of up to kWarpMaxBeads beads, a CTA up to ~6400
-    const int hard = (227 * 1024) / 36;
-    if (largest > hard) return HPF_ERR_NOT_IMPLEMENTED;
-    int cap = std::max(max_group_beads, largest);
+    // local bead indices are 16-bit; a CTA group must fit in shared memory
+    if (largest > 32767) return HPF_ERR_NOT_IMPLEMENTED;
+    const int cap = std::max(max_group_beads, largest);
     const int warp_mode = cap <= kWarpMaxBeads ? 1 : 0;
     std::vector<int> comp_grp(n, -1);
     std::vector<int> grp_beads;
@@ -442,18 +529,18 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
     bucket(nb, [&](int64_t t) { return ba[t]; }, sb, ob);
     bucket(na, [&](int64_t t) { return aa[t]; }, sa, oa);
     bucket(nd, [&](int64_t t) { return da[t]; }, sd, od);
-    std::vector<short2> bond_ij(nb);
+    std::vector<int> bond_ij(nb);
     std::vector<float2> bond_p(nb);
     for (int64_t k = 0; k < nb; ++k) {
         const int64_t t = ob[k];
-        bond_ij[k] = make_short2((short)local[ba[t]], (short)local[bb[t]]);
+        bond_ij[k] = local[ba[t]] | (local[bb[t]] << 16);
         bond_p[k] = make_float2(br0[t], bk[t]);
     }
-    std::vector<short4> ang_ijk(na);
+    std::vector<int2> ang_ijk(na);
     std::vector<float2> ang_p(na);
     for (int64_t k = 0; k < na; ++k) {
         const int64_t t = oa[k];
-        ang_ijk[k] = make_short4((short)local[aa[t]], (short)local[ab[t]], (short)local[ac[t]], 0);
+        ang_ijk[k] = make_int2(local[aa[t]] | (local[ab[t]] << 16), local[ac[t]]);
         ang_p[k] = make_float2(at0[t], ak[t]);
     }
     std::vector<short4> dih_ijkl(nd);
@@ -468,6 +555,45 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
         dih_tl[k] = make_int2(dtype[t], dlast[t]);
         dih_gid[k] = (int)t;
     }
+    // incidence lists: per bead the (slot, sign) entries of the terms that
+    // touch it; slots per group: bonds, then 2 per angle, then 4 per dihedral
+    std::vector<std::vector<int>> inc(grp_bead[G]);
+    int mx_slots = 0, mx_bonds = 0, mx_angles = 0, mx_beads = 0, mx_inc = 0;
+    for (int g = 0; g < G; ++g) {
+        const int base = grp_bead[g];
+        const int nbd_g = sb[g + 1] - sb[g], na_g = sa[g + 1] - sa[g], nd_g = sd[g + 1] - sd[g];
+        for (int k = 0; k < nbd_g; ++k) {
+            const int ij = bond_ij[sb[g] + k];
+            inc[base + (ij & 0xffff)].push_back((k << 1) | 1);
+            inc[base + (ij >> 16)].push_back(k << 1);
+        }
+        for (int k = 0; k < na_g; ++k) {
+            const int2 q = ang_ijk[sa[g] + k];
+            const int s0 = nbd_g + 2 * k;
+            inc[base + (q.x & 0xffff)].push_back((s0 << 1) | 1);
+            inc[base + (q.x >> 16)].push_back(s0 << 1);
+            inc[base + (q.x >> 16)].push_back((s0 + 1) << 1);
+            inc[base + q.y].push_back(((s0 + 1) << 1) | 1);
+        }
+        for (int k = 0; k < nd_g; ++k) {
+            const short4 q = dih_ijkl[sd[g] + k];
+            const int s0 = nbd_g + 2 * na_g + 4 * k;
+            const int li[4] = {q.x, q.y, q.z, q.w};
+            for (int j = 0; j < 4; ++j) inc[base + li[j]].push_back((s0 + j) << 1);
+        }
+        int ng = 0;
+        for (int i = grp_bead[g]; i < grp_bead[g + 1]; ++i) ng += (int)inc[i].size();
+        mx_inc = std::max(mx_inc, ng);
+        mx_slots = std::max(mx_slots, nbd_g + 2 * na_g + 4 * nd_g);
+        mx_bonds = std::max(mx_bonds, nbd_g);
+        mx_angles = std::max(mx_angles, na_g);
+        mx_beads = std::max(mx_beads, grp_beads[g]);
+    }
+    std::vector<int> bead_inc(grp_bead[G] + 1, 0), inc_list;
+    for (int i = 0; i < grp_bead[G]; ++i) {
+        bead_inc[i + 1] = bead_inc[i] + (int)inc[i].size();
+        inc_list.insert(inc_list.end(), inc[i].begin(), inc[i].end());
+    }
     hpf_respa_plan* p = new hpf_respa_plan();
     memset(p, 0, sizeof(*p));
     p->n_beads = n;
@@ -475,10 +601,18 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
     p->n_free = (int)free_ids.size();
     p->warp_mode = warp_mode;
     p->has_dih = nd > 0;
-    int mx = 0;
-    for (int g = 0; g < G; ++g) mx = std::max(mx, grp_beads[g]);
-    p->max_group_beads = std::max(mx, 1);
-    p->smem = sizeof(float) * 9 * (size_t)p->max_group_beads * (warp_mode ? kWarps : 1);
+    p->mx_beads = std::max(mx_beads, 1);
+    p->mx_slots = std::max(mx_slots, 1);
+    p->mx_inc = std::max(mx_inc, 1);
+    p->mx_bonds = std::max(mx_bonds, 1);
+    p->mx_angles = std::max(mx_angles, 1);
+    p->smem_group = group_smem_bytes(p->mx_beads, p->mx_slots, p->mx_inc, p->mx_bonds,
+                                     p->mx_angles);
+    p->smem = p->smem_group * (warp_mode ? kWarps : 1);
+    if (p->smem > 227 * 1024) {
+        delete p;
+        return HPF_ERR_NOT_IMPLEMENTED;
+    }
     const int grp_blocks = warp_mode ? (G + kWarps - 1) / kWarps : G;
     int nfb = (p->n_free + kThreads - 1) / kThreads;
     nfb = std::min(nfb, std::max(1, 152 * 8 - grp_blocks));
@@ -486,6 +620,7 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
     p->n_free_blocks = nfb;
     int st = HPF_OK;
     if ((st = upload(&p->grp_bead, grp_bead)) || (st = upload(&p->bead_ids, bead_ids)) ||
+        (st = upload(&p->bead_inc, bead_inc)) || (st = upload(&p->inc_list, inc_list)) ||
         (st = upload(&p->grp_bond, sb)) || (st = upload(&p->bond_ij, bond_ij)) ||
         (st = upload(&p->bond_p, bond_p)) || (st = upload(&p->grp_ang, sa)) ||
         (st = upload(&p->ang_ijk, ang_ijk)) || (st = upload(&p->ang_p, ang_p)) ||
@@ -522,7 +657,7 @@ int hpf_respa_plan_info(const hpf_respa_plan* p, int* n_groups, int* n_free,
     if (!p) return HPF_ERR_ARG;
     if (n_groups) *n_groups = p->n_groups;
     if (n_free) *n_free = p->n_free;
-    if (max_group_beads) *max_group_beads = p->max_group_beads;
+    if (max_group_beads) *max_group_beads = p->mx_beads;
     return HPF_OK;
 }
 
