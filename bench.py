@@ -30,6 +30,23 @@ sys.path.insert(0, ROOT)
 METRIC = "MD steps/s & ns/day per GB300 vs plain GPU form at <=1e-5 force rel-RMS vs FP64"
 WORKLOAD = "membrane162k"
 
+# workload -> description and coupling (thermostat / barostat)
+WORKLOADS = {
+    "membrane162k": ("lipid membrane 162k beads (6000 x 12-bead lipids + 90k W), box 27 nm, "
+                     "mesh 64^3, 5 types",
+                     dict(thermostat=True, barostat="isotropic"),
+                     "NPT: SCR barostat (isotropic, 1 bar, tau_p 1 ps, every step) + "
+                     "CSVR thermostat (323 K, tau 0.1 ps)"),
+    "melt10k": ("binary homopolymer melt 10k beads (1000 x 10-bead chains), box 10 nm, "
+                "mesh 32^3, 2 types",
+                dict(thermostat=True, barostat=None), "NVT: CSVR thermostat (323 K, tau 0.1 ps)"),
+    "peptide500k": ("charged peptides 500k beads (200 x 50-residue BB+SC chains, 20% charged "
+                    "side chains + counter-ions, W), box 40 nm, mesh 128^3, 3 types, "
+                    "PIC_Spectral eps_r 80, CBT dihedrals",
+                    dict(thermostat=True, barostat=None),
+                    "NVT: CSVR thermostat (323 K, tau 0.1 ps)"),
+}
+
 
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -37,15 +54,12 @@ def _dist():
     return ws, rank
 
 
-def _config_block(cfg, n, extra=None):
-    d = {"workload": "lipid membrane 162k beads (6000 x 12-bead lipids + 90k W), "
-                     "box 27 nm, mesh 64^3, 5 types",
-         "n_beads": int(n), "mesh": list(cfg.mesh()), "respa_inner": int(cfg.respa_inner),
+def _config_block(cfg, n, workload=WORKLOAD, extra=None):
+    desc, _, ensemble = WORKLOADS[workload]
+    d = {"workload": desc, "n_beads": int(n), "mesh": list(cfg.mesh()), "respa_inner": int(cfg.respa_inner),
          "time_step_ps": float(cfg.time_step), "sigma": cfg.sigma, "kappa": cfg.kappa,
          "l2": "flushed between timed steps (256 MB write, outside the timed windows)",
-         "parallelism": "replicas only",
-         "ensemble": "NPT: SCR barostat (isotropic, 1 bar, tau_p 1 ps, every step) + "
-                     "CSVR thermostat (323 K, tau 0.1 ps)"}
+         "parallelism": "replicas only", "ensemble": ensemble}
     if extra:
         d.update(extra)
     return d
@@ -161,7 +175,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     from hymd_gb300 import systems
-    s = systems.BUILDERS[WORKLOAD]()
+    s = systems.BUILDERS[args.workload]()
     cfg = s["config"]
     workers = os.cpu_count() or 1
     cpu_baseline(s, steps=1, workers=workers)  # warm-up (one step)
@@ -180,7 +194,7 @@ def run_reference(args):
             "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64 field / f32 bonded", "data": "synthetic",
             "ns_per_day": ns_day,
-            "config": _config_block(cfg, len(s["positions"])),
+            "config": _config_block(cfg, len(s["positions"]), args.workload),
             "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": workers, "kind": "port",
                              "sample": f"{done} outer steps of the full workload "
                                        f"({secs:.1f} s); FFTs threaded over {workers} cores"},
@@ -255,15 +269,15 @@ def run_gpu(args):
     from hymd_gb300.hamiltonian import get_hamiltonian
     from hymd_gb300.md import RespaMD
 
-    s = systems.BUILDERS[WORKLOAD](seed=2 + rank)
+    s = systems.BUILDERS[args.workload](seed=2 + rank)
     cfg = s["config"]
     n = len(s["positions"])
     ham = get_hamiltonian(cfg)
     md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"],
-                 device=dev)
-    # the membrane workload runs NPT: SCR barostat at 1 bar every step and the
-    # CSVR thermostat at 323 K; their random numbers come from a seeded table
-    md.couple(thermostat=True, barostat="isotropic", seed=100 + rank, n_steps=20000)
+                 charges=s.get("charges"), device=dev)
+    # coupling of the workload (the membrane runs NPT: SCR barostat at 1 bar
+    # every step and CSVR at 323 K); random numbers come from a seeded table
+    md.couple(seed=100 + rank, n_steps=20000, **WORKLOADS[args.workload][1])
     md.prime()
     md.capture()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
@@ -351,7 +365,7 @@ def run_gpu(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 (f64 energies/virial)", "data": "synthetic",
                 "ns_per_day": ns_day * ws,
-                "config": _config_block(cfg, n),
+                "config": _config_block(cfg, n, args.workload),
                 "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "steps/s",
                         "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 12 * n},
                 "gpu_launches": md.launches_per_step * args.steps,
@@ -374,6 +388,7 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="hpf", choices=["hpf", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--breakdown", action="store_true",
                     help="also print per-phase step times (us) to stderr")
