@@ -93,3 +93,30 @@ def test_fused_inner_loop_matches_per_term_path():
         assert x == pytest.approx(y, rel=1e-5)
     a.check_errors()
     b.check_errors()
+
+
+def test_integrator_matches_reference_kat(golden):
+    """integrate_velocity / integrate_position against the known answers of the
+    reference's test/test_integrator.py (three_atoms fixture), at FP32."""
+    from hymd_gb300.integrator import integrate_position, integrate_velocity
+    m = golden("misc.npz")
+    dt = float(m["integrator/dt"])
+    v0 = torch.tensor(m["integrator/v0"], dtype=torch.float32, device="cuda")
+    r0 = torch.tensor(m["integrator/r0"], dtype=torch.float32, device="cuda")
+    acc = torch.tensor(m["integrator_kat/accelerations"], dtype=torch.float32, device="cuda")
+    v1 = integrate_velocity(v0, acc, dt)
+    r1 = integrate_position(r0, v0, dt)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(v1.cpu().numpy(), m["integrator_kat/expected_velocities"],
+                               rtol=2e-6, atol=1e-6)
+    np.testing.assert_allclose(r1.cpu().numpy(), m["integrator_kat/expected_positions"],
+                               rtol=2e-6, atol=1e-6)
+    # the inputs are not changed in place (hymd/integrator.py:9-73 returns new arrays)
+    assert torch.equal(v0.cpu(), torch.tensor(m["integrator/v0"], dtype=torch.float32))
+    # within one FP32 rounding of the reference's expressions evaluated in FP32
+    v0n = m["integrator/v0"].astype(np.float32)
+    an = m["integrator_kat/accelerations"].astype(np.float32)
+    want_v = v0n + np.float32(0.5 * dt) * an
+    want_r = m["integrator/r0"].astype(np.float32) + np.float32(dt) * v0n
+    assert np.all(np.abs(v1.cpu().numpy() - want_v) <= 2 * np.spacing(np.abs(want_v)))
+    assert np.all(np.abs(r1.cpu().numpy() - want_r) <= 2 * np.spacing(np.abs(want_r)))

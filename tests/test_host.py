@@ -174,3 +174,16 @@ def test_synthetic_workloads_shapes():
     assert np.all((s["positions"] >= 0) & (s["positions"] < 27.0))
     s = systems.homopolymer_melt()
     assert s["positions"].shape == (10000, 3) and len(s["topology"][0]) == 9000
+
+
+def test_integrator_formula_matches_reference_kat(golden):
+    """The velocity-Verlet pieces used by oracle/md.py against the known answers
+    of the reference's test/test_integrator.py."""
+    m = golden("misc.npz")
+    dt = float(m["integrator/dt"])
+    v0, r0 = m["integrator/v0"], m["integrator/r0"]
+    acc = m["integrator_kat/accelerations"]
+    np.testing.assert_allclose(v0 + 0.5 * dt * acc, m["integrator_kat/expected_velocities"],
+                               rtol=0, atol=1e-13)
+    np.testing.assert_allclose(r0 + dt * v0, m["integrator_kat/expected_positions"], rtol=0,
+                               atol=1e-13)
