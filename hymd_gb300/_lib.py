@@ -21,7 +21,7 @@ HPF_OUT_DOUBLES = 8 + 8 * HPF_REDUCE_BLOCKS + 8
 STATUS = {
     0: "HPF_OK", 1: "HPF_ERR_ARG", 2: "HPF_ERR_CUDA", 3: "HPF_ERR_CUFFT",
     4: "HPF_ERR_INDEX", 5: "HPF_ERR_NONFINITE", 6: "HPF_ERR_TIMEOUT",
-    7: "HPF_ERR_NOT_IMPLEMENTED",
+    7: "HPF_ERR_NOT_IMPLEMENTED", 8: "HPF_ERR_SCRATCH_LIMIT",
 }
 
 
@@ -98,6 +98,7 @@ _SIGNATURES.update({
                                ctypes.POINTER(ctypes.c_float)],
     "hpf_csvr": [P, P, I64, ctypes.POINTER(P), I, D, ctypes.POINTER(CsvrArgs), P, P, P, P, P, P],
     "hpf_scr_isotropic": [P, P, P, I64, P, P, ctypes.POINTER(ScrArgs), P, P, P, P, P, P],
+    "hpf_paint_static": [P, P, I64, I, I, I, I, ctypes.POINTER(D), ctypes.POINTER(D), P, P, P],
 })
 
 _LIB = None

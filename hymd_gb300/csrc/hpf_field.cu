@@ -680,6 +680,7 @@ const char* hpf_status_string(int s) {
         case HPF_ERR_NONFINITE: return "HPF_ERR_NONFINITE";
         case HPF_ERR_TIMEOUT: return "HPF_ERR_TIMEOUT";
         case HPF_ERR_NOT_IMPLEMENTED: return "HPF_ERR_NOT_IMPLEMENTED";
+        case HPF_ERR_SCRATCH_LIMIT: return "HPF_ERR_SCRATCH_LIMIT";
         default: return "HPF_ERR_UNKNOWN";
     }
 }
@@ -1074,3 +1075,82 @@ int hpf_pic_step(hpf_ctx* c, const float* pos, const float* charges, int64_t n,
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- paint without allocation ---
+// Variant of hpf_paint for callers that hold no mesh context and must not
+// allocate device memory: the fixed-point accumulators live in one
+// file-scope device array, and the box state in the first 256 bytes of it.
+// The scratch is shared by every call on a device, so calls that overlap (on
+// two streams or two host threads) race.  The first call on a device loads
+// the module and looks up the array's address, so it should come before any
+// stream capture.
+namespace {
+
+constexpr int64_t kStaticPaintCells = (int64_t)1 << 21;  // T * n0 * n1 * n2 at most (16 MiB)
+constexpr int64_t kStaticBoxBytes = 256;
+static_assert(sizeof(BoxState) <= kStaticBoxBytes, "box state exceeds its scratch slot");
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned long long
+    g_paint_static_scratch[kStaticBoxBytes / 8 + kStaticPaintCells];
+
+char* g_paint_static_addr[kStaticMaxDevices];  // per device, set by the first call
+
+__global__ void k_store_box(BoxState bs, BoxState* dst) { *dst = bs; }
+
+int paint_static_scratch(char** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kStaticMaxDevices)
+        return HPF_ERR_CUDA;
+    if (!g_paint_static_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_paint_static_scratch) != cudaSuccess || !p)
+            return HPF_ERR_CUDA;
+        g_paint_static_addr[dev] = static_cast<char*>(p);
+    }
+    *out = g_paint_static_addr[dev];
+    return HPF_OK;
+}
+
+}  // namespace
+
+extern "C" int hpf_paint_static(const float* pos, const int32_t* types, int64_t n, int T, int n0,
+                                int n1, int n2, const double box[3], const double* type_mass,
+                                float* phi_out, int* d_err, void* stream) {
+    if ((n > 0 && (!pos || !types)) || n < 0 || !box || !type_mass || !phi_out || T < 1 ||
+        T > HPF_MAX_TYPES || n0 < 2 || n1 < 2 || n2 < 2)
+        return HPF_ERR_ARG;
+    if (!(box[0] > 0 && box[1] > 0 && box[2] > 0)) return HPF_ERR_ARG;
+    const int64_t M = (int64_t)n0 * n1 * n2;
+    if (M > kStaticPaintCells || (int64_t)T * M > kStaticPaintCells) return HPF_ERR_SCRATCH_LIMIT;
+    char* base = nullptr;
+    int r = paint_static_scratch(&base);
+    if (r != HPF_OK) return r;
+    BoxState* bs = reinterpret_cast<BoxState*>(base);
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(base + kStaticBoxBytes);
+    cudaStream_t st = as_stream(stream);
+    BoxState h;
+    memset(&h, 0, sizeof(h));
+    const int nn[3] = {n0, n1, n2};
+    fill_box_state(h, box[0], box[1], box[2], nn);
+    k_store_box<<<1, 1, 0, st>>>(h, bs);
+    HPF_LAUNCH_CHECK();
+    // the accumulators must start at zero
+    HPF_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * (size_t)T * M, st));
+    TypeScale sc;
+    for (int t = 0; t < T; ++t) sc.s[t] = (float)type_mass[t];
+    if (n > 0) {
+        k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, types, nullptr, n, T, bs, acc, M,
+                                                           d_err, nullptr);
+        HPF_LAUNCH_CHECK();
+    }
+    if (M % 4 == 0) {
+        dim3 grid(grid_for(M / 4, kThreads), T);
+        k_paint_finalize<<<grid, kThreads, 0, st>>>(acc, phi_out, M, T, sc, bs);
+    } else {
+        dim3 grid(grid_for(M, kThreads), T);
+        k_paint_finalize1<<<grid, kThreads, 0, st>>>(acc, phi_out, M, T, sc, bs);
+    }
+    HPF_LAUNCH_CHECK();
+    return HPF_OK;
+}

@@ -386,3 +386,30 @@ def domain_decomposition(positions, pm, *args, molecules=None, bonds=None, topol
     """hymd/field.py:1115-1178.  One GPU holds the whole system, so there is
     nothing to exchange: the arrays are returned unchanged."""
     return (positions, *args)
+
+
+def paint_static(positions, types, masses, mesh_size, box_size, out=None, err=None):
+    """Per-type CIC densities without a mesh context or any device allocation
+    by the library (hpf_paint_static): the same grids as the paint inside
+    `update_field` (hymd/field.py:573-575), bit for bit.
+
+    For callers that own no `ParticleMesh` and may not allocate device memory
+    themselves.  The library's scratch is a fixed 16 MiB static array per
+    device, so n_types * prod(mesh_size) is limited to 2**21 cells
+    (HPFError HPF_ERR_SCRATCH_LIMIT beyond).  Calls that overlap in time on
+    one device race on that scratch.  `out` (float32, (T, n0, n1, n2)) and
+    `err` (int32 device word) are caller-owned; without `out` a tensor is
+    allocated here by torch.
+    """
+    pos = _lib.require_cuda(positions, "positions", torch.float32)
+    n = pos.shape[0]
+    typ = _types32(types, n)
+    T = len(masses)
+    n0, n1, n2 = (int(x) for x in mesh_size)
+    if out is None:
+        out = torch.empty((T, n0, n1, n2), dtype=torch.float32, device=pos.device)
+    _lib.require_cuda(out, "out", torch.float32, (T, n0, n1, n2))
+    _lib.call("hpf_paint_static", _lib.ptr(pos), _lib.ptr(typ), n, T, n0, n1, n2,
+              _lib.dvec([float(x) for x in box_size]), _lib.dvec(_masses(masses, T)),
+              _lib.ptr(out), _lib.ptr(err), _lib.stream_ptr())
+    return out

@@ -38,7 +38,8 @@ enum {
     HPF_ERR_INDEX = 4,        /* device saw a particle/type index out of range   */
     HPF_ERR_NONFINITE = 5,    /* device saw a non-finite position                */
     HPF_ERR_TIMEOUT = 6,      /* a bounded device wait ran out                   */
-    HPF_ERR_NOT_IMPLEMENTED = 7
+    HPF_ERR_NOT_IMPLEMENTED = 7,
+    HPF_ERR_SCRATCH_LIMIT = 8 /* request exceeds a fixed-size static scratch     */
 };
 
 typedef struct hpf_ctx hpf_ctx; /* mesh context: geometry, cuFFT plans, scratch */
@@ -340,6 +341,21 @@ int hpf_respa_step(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
 /* Sum over particles of v^2 into out[0] (device workspace, HPF_OUT_DOUBLES);
  * KE = mass/2 * out[0]. */
 int hpf_sum_v2(const float* v, int64_t n, double* out, void* stream);
+
+/* ---- paint without allocation --------------------------------------------
+ * No counterpart in the reference: a variant of hpf_paint (same densities,
+ * bit for bit) for callers that hold no hpf_ctx and may not allocate device
+ * memory.  Its scratch is one static device array per device of 16 MiB:
+ * T * n0 * n1 * n2 <= 2^21 cells, beyond which it returns
+ * HPF_ERR_SCRATCH_LIMIT.  It clears the accumulators itself on every call.
+ * All calls on a device share that scratch, so calls that overlap in time (two
+ * streams, two host threads) race; the first call on a device looks up the
+ * array's address and should come before any stream capture.
+ * box: host double[3]; type_mass: host double[T]; phi_out: float[T][M];
+ * d_err: device int (may be NULL).                                         */
+int hpf_paint_static(const float* pos, const int32_t* types, int64_t n, int T, int n0, int n1,
+                     int n2, const double box[3], const double* type_mass, float* phi_out,
+                     int* d_err, void* stream);
 
 #ifdef __cplusplus
 }
