@@ -5,7 +5,8 @@ Workload (default): the 162k-bead lipid membrane -- 6000 twelve-bead lipids +
 recipe, bonds + angles, time_step 0.03 ps, respa_inner 10.  One step = one
 outer rRESPA step (10 inner bonded steps + one field evaluation), run from a
 CUDA graph.  Inputs (the system state) are resident in HBM; the working set
-(~70 MB) fits in L2, so L2 is flushed (256 MB write) between timed steps,
+(~70 MB) fits in L2, so L2 is flushed between timed steps (a 256 MB write, then
+a 256 MB read so that the evicted lines are clean),
 outside the per-step CUDA-event windows.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl hpf|reference]
@@ -58,7 +59,8 @@ def _config_block(cfg, n, workload=WORKLOAD, extra=None):
     desc, _, ensemble = WORKLOADS[workload]
     d = {"workload": desc, "n_beads": int(n), "mesh": list(cfg.mesh()), "respa_inner": int(cfg.respa_inner),
          "time_step_ps": float(cfg.time_step), "sigma": cfg.sigma, "kappa": cfg.kappa,
-         "l2": "flushed between timed steps (256 MB write, outside the timed windows)",
+         "l2": "flushed between timed steps (256 MB write, then 256 MB read so the evicted "
+               "lines are clean; outside the timed windows)",
          "parallelism": "replicas only", "ensemble": ensemble}
     if extra:
         d.update(extra)
@@ -128,21 +130,13 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _time_kernel(fn, reps, flush, torch):
-    """Average device time of fn() (CUDA events on the current stream), with
-    an L2 flush before each launch outside the timed window."""
-    st = torch.cuda.current_stream()
-    tot = 0.0
-    for _ in range(reps):
-        flush.zero_()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(st)
-        fn()
-        b.record(st)
-        b.synchronize()
-        tot += a.elapsed_time(b)
-    return tot / reps
+def _traffic(workload):
+    """Per-launch DRAM bytes (read + write) of the step's kernels from one ncu
+    capture of this workload, if recorded under profiles/."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if not os.path.exists(p):
+        return {}
+    return json.load(open(p)).get(workload, {})
 
 
 def cpu_baseline(sys_, steps=2, workers=1):
@@ -204,11 +198,27 @@ def run_reference(args):
     return 0
 
 
+class L2Flush:
+    """Evicts L2 (129 MB) between timed steps: a 256 MB write, then a 256 MB
+    read, so that the lines left in L2 are clean and the next step's misses
+    do not first write back the flush's own data."""
+
+    def __init__(self, torch, dev):
+        self.w = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+        self.r = torch.ones(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+        self.sink = torch.empty(1, dtype=torch.float32, device=dev)
+
+    def zero_(self):
+        self.w.zero_()
+        self.sink.copy_(self.r.sum().reshape(1))
+
+
 def step_breakdown(md, flush, torch, reps=10):
     """Per-stage device time of one MD step (diagnostic, printed to stderr):
     the fused rRESPA kernel timed as a captured graph, the field step by
     hpf_field_step_profile (CUDA events between its stages), the thermostat
-    scaling as a graph.  L2 is flushed before each repetition."""
+    scaling as a graph.  L2 is flushed before each timed stage group (which
+    also keeps the GPU busy while the host enqueues the stages)."""
     from hymd_gb300 import _lib
     st = torch.cuda.current_stream()
 
@@ -231,6 +241,17 @@ def step_breakdown(md, flush, torch, reps=10):
                                       _lib.stream_ptr()))
     names = ["respa", "paint", "r2c", "kspace", "c2r", "readout_kick", "thermostat_scale"]
     tot = {k: 0.0 for k in names}
+    # the fused kernel with its data left in L2 (back-to-back replays), for
+    # comparison with the flushed figure
+    flush.zero_()
+    g_respa.replay()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(reps):
+        g_respa.replay()
+    b.record(st)
+    b.synchronize()
+    tot["respa_l2_resident"] = a.elapsed_time(b) * 1000.0 / reps
     us = (_lib.ctypes.c_float * 5)()
     for _ in range(reps):
         flush.zero_()
@@ -241,12 +262,16 @@ def step_breakdown(md, flush, torch, reps=10):
         b.synchronize()
         tot["respa"] += a.elapsed_time(b) * 1000.0 / reps
         scale = md.state.data_ptr() + 12 * 8 if md.baro_args is not None else None
+        # the flush also keeps the GPU busy while the host enqueues the
+        # stages, so the events see no host launch gaps
+        flush.zero_()
         _lib.call("hpf_field_step_profile", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n,
                   md.masses, _lib.ptr(md.f_field), _lib.ptr(md.field_sums),
                   None if scale is None else _lib.ctypes.c_void_p(scale),
                   md._kick_args(thermo), _lib.stream_ptr(), us)
         for k, x in zip(names[1:6], us):
             tot[k] += x / reps
+        flush.zero_()
         a.record(st)
         g_scale.replay()
         b.record(st)
@@ -279,8 +304,10 @@ def run_gpu(args):
     # every step and CSVR at 323 K); random numbers come from a seeded table
     md.couple(seed=100 + rank, n_steps=20000, **WORKLOADS[args.workload][1])
     md.prime()
-    md.capture()
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
+    # two graphs per step (fused inner loop | field step + thermostat) so that
+    # an event between them times the dominant kernel inside the timed region
+    md.capture(split=True)
+    flush = L2Flush(torch, dev)
     for _ in range(max(3, args.warmup)):
         md.run(1)
     torch.cuda.synchronize()
@@ -290,19 +317,26 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     st = torch.cuda.current_stream()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3))
            for _ in range(args.steps)]
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for a, b in evs:
+        for a, m, b in evs:
             flush.zero_()
             a.record(st)
-            md.graph.replay()
+            if md.graph_inner is not None:
+                md.graph_inner.replay()
+                m.record(st)
+                md.graph_field.replay()
+            else:
+                md.graph.replay()
+                m.record(st)
             b.record(st)
         torch.cuda.synchronize()
     barrier()
-    ms = sum(a.elapsed_time(b) for a, b in evs)
+    ms = sum(a.elapsed_time(b) for a, m, b in evs)
+    respa_ms = sum(a.elapsed_time(m) for a, m, b in evs) / args.steps
     if ws > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -310,8 +344,6 @@ def run_gpu(args):
     ms_step = ms / args.steps
     sps = 1000.0 / ms_step
     md.check_errors()
-    if args.breakdown and rank == 0:
-        print(json.dumps({"breakdown_us": step_breakdown(md, flush, torch)}), file=sys.stderr)
 
     # ---- end to end through the public API with host buffers -------------
     r_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
@@ -332,24 +364,34 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_evs) / args.steps
 
-    # ---- roofline of the dominant field kernel (paint) --------------------
+    # ---- roofline -------------------------------------------------------------
+    # dominant kernel: the fused rRESPA inner loop.  Algorithmic bytes are
+    # those of the unfused inner step (read r, v, F; write r, v, F; bonded
+    # term data: 72 N + 16 B + 20 A + 144 D) times respa_inner; the fused
+    # kernel keeps the loop on chip, so its DRAM traffic is far lower.
     peak, peak_kind = _peaks()
     T = cfg.n_types
     M = int(np.prod(cfg.mesh()))
-    phi = md.pm.real_field(T)
-    masses = _lib.dvec(cfg.m)
-
-    def paint():
-        _lib.call("hpf_paint", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), n, masses,
-                  _lib.ptr(phi), _lib.stream_ptr())
-
-    paint_ms = _time_kernel(paint, 20, flush, torch)
-    paint_bytes = 16 * n + 4 * T * M
-    achieved = paint_bytes / (paint_ms * 1e-3) / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "paint_traffic.json")
-    if os.path.exists(tp):
-        traffic = json.load(open(tp)).get("bytes_per_launch")
+    Mc = cfg.mesh()[0] * cfg.mesh()[1] * (cfg.mesh()[2] // 2 + 1)
+    topo = md.topo
+    nb = topo.n_bonds if topo else 0
+    na = topo.n_angles if topo else 0
+    nd = topo.n_dihedrals if topo else 0
+    respa_bytes = cfg.respa_inner * (72 * n + 16 * nb + 20 * na + 144 * nd)
+    respa_gbs = respa_bytes / (respa_ms * 1e-3) / 1e9
+    traffic = _traffic(args.workload)
+    # the other kernels of the step, timed stage by stage (graphs + events,
+    # L2 flushed before each repetition)
+    bd = step_breakdown(md, flush, torch)
+    if args.breakdown and rank == 0:
+        print(json.dumps({"breakdown_us": bd}), file=sys.stderr)
+    stage_bytes = {"paint": 16 * n + 4 * T * M, "kspace": 32 * T * Mc,
+                   "readout_kick": 28 * n + 12 * T * M + 36 * n}
+    kernels = {}
+    for k, b_ in stage_bytes.items():
+        gbs = b_ / (bd[k] * 1e-6) / 1e9
+        kernels[k] = {"algorithmic_bytes": b_, "us": bd[k], "achieved": gbs, "frac": gbs / peak,
+                      "traffic": traffic.get(k)}
 
     ns_day = sps * cfg.respa_inner * cfg.time_step * 86400 / 1000.0
     # CPU baseline (rank 0, N=1 only): bounded oracle sample
@@ -365,20 +407,64 @@ def run_gpu(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 (f64 energies/virial)", "data": "synthetic",
                 "ns_per_day": ns_day * ws,
-                "config": _config_block(cfg, n, args.workload),
+                "config": _config_block(cfg, n, args.workload,
+                                        {"respa_groups": md.plan_info(),
+                                         "respa_group_tuning_us": md.block_timings}),
                 "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "steps/s",
                         "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 12 * n},
                 "gpu_launches": md.launches_per_step * args.steps,
-                "roofline": {"kernel": "paint (k_paint + k_paint_finalize)", "bound": "hbm",
-                             "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic,
-                             "peak_kind": peak_kind, "ms_per_launch": paint_ms,
-                             "algorithmic_bytes": paint_bytes},
+                "roofline": {"kernel": "k_respa_warp (fused rRESPA inner loop, "
+                                       f"{cfg.respa_inner} inner steps per launch)",
+                             "bound": "hbm", "achieved": respa_gbs, "peak": peak, "unit": "GB/s",
+                             "frac": respa_gbs / peak, "traffic": traffic.get("respa"),
+                             "peak_kind": peak_kind, "ms_per_launch": respa_ms,
+                             "algorithmic_bytes": respa_bytes,
+                             "bytes_basis": "respa_inner x (72 N + 16 B + 20 A + 144 D), "
+                                            "the unfused inner step's reads and writes",
+                             "note": "latency-bound in practice: the loop runs on chip and "
+                                     "touches DRAM once per bead per launch (traffic)"},
+                "roofline_kernels": kernels,
                 "clocks": clk.summary(),
                 "cpu_baseline": cpu}
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def profile_stage(args):
+    """Run one stage of the step eagerly (no graph, no timing) `--reps` times
+    on the workload and exit: a small program for kernel profilers.
+    Stages: paint, field (paint -> r2c -> k-space -> c2r -> readout), respa
+    (the fused inner loop), step (a whole outer step)."""
+    import torch
+    from hymd_gb300 import _lib, systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+
+    s = systems.BUILDERS[args.workload](seed=2)
+    cfg = s["config"]
+    md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, get_hamiltonian(cfg),
+                 topology=s["topology"], charges=s.get("charges"))
+    md.couple(seed=100, n_steps=max(16, 4 * args.reps), **WORKLOADS[args.workload][1])
+    md.prime()
+    phi = md.pm.real_field(cfg.n_types)
+    masses = _lib.dvec(cfg.m)
+    st = _lib.stream_ptr()
+    for _ in range(args.reps):
+        if args.profile_stage == "paint":
+            _lib.call("hpf_paint", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n, masses,
+                      _lib.ptr(phi), st)
+        elif args.profile_stage == "field":
+            md._field(st, md.field_sums)
+        elif args.profile_stage == "respa":
+            md._inner_fused(st)
+        else:
+            md.step()
+    torch.cuda.synchronize()
+    md.check_errors()
+    print(json.dumps({"profile_stage": args.profile_stage, "workload": args.workload,
+                      "reps": args.reps, "status": "ok"}))
     return 0
 
 
@@ -392,7 +478,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--breakdown", action="store_true",
                     help="also print per-phase step times (us) to stderr")
+    ap.add_argument("--profile-stage", choices=["paint", "field", "respa", "step"],
+                    help="run one stage eagerly --reps times for a profiler, print no bench line")
+    ap.add_argument("--reps", type=int, default=4)
     args = ap.parse_args()
+    if args.profile_stage:
+        return profile_stage(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

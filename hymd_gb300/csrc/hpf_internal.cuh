@@ -23,6 +23,7 @@ struct BoxState {
     float inv_dV;
     int n[3];
     int pad;
+    double inv_M;     // 1 / (n0 n1 n2)
 };
 
 // Quadratic functional w = 1/2 phi.Q.phi + b.phi + c (per context).
@@ -97,6 +98,7 @@ __host__ __device__ inline void fill_box_state(BoxState& s, double L0, double L1
         s.kf[d] = (float)(2.0 * 3.14159265358979323846 / Ls[d]);
     }
     s.inv_dV = (float)(1.0 / s.dV);
+    s.inv_M = 1.0 / ((double)n[0] * (double)n[1] * (double)n[2]);
 }
 
 // Record the first device-side error code (out-of-range index, non-finite
@@ -115,22 +117,25 @@ __device__ __forceinline__ double rcp_d(double x) {
     return r;
 }
 
-// Device-side box update (barostat): the same quantities as fill_box_state.
-__device__ __forceinline__ void fill_box_state_dev(BoxState& s, double L0, double L1, double L2) {
-    const double Ls[3] = {L0, L1, L2};
-    s.V = L0 * L1 * L2;
-    const double M = (double)s.n[0] * (double)s.n[1] * (double)s.n[2];
-    s.dV = s.V * rcp_d(M);
+// Device-side box update (barostat) from the new float box lengths: the same
+// quantities as fill_box_state.  Run by one thread on the critical path of a
+// step, so only V and dV are formed in FP64 (GB300's FP64 pipe is narrow);
+// n/L is the double-float quotient hi + lo from FP32 operations (FMA
+// residual), equal to the host's split to within an ulp of lo.
+__device__ __forceinline__ void fill_box_state_dev(BoxState& s, float L0, float L1, float L2) {
+    const float Ls[3] = {L0, L1, L2};
+    s.V = (double)L0 * (double)L1 * (double)L2;
+    s.dV = s.V * s.inv_M;
     for (int d = 0; d < 3; ++d) {
-        const double iL = rcp_d(Ls[d]);
-        s.L[d] = Ls[d];
-        s.Lf[d] = (float)Ls[d];
-        const double ih = (double)s.n[d] * iL;
-        s.ih_hi[d] = (float)ih;
-        s.ih_lo[d] = (float)(ih - (double)s.ih_hi[d]);
-        s.kf[d] = (float)(2.0 * 3.14159265358979323846 * iL);
+        const float L = Ls[d], nd = (float)s.n[d];
+        s.L[d] = (double)L;
+        s.Lf[d] = L;
+        const float hi = nd / L;
+        s.ih_hi[d] = hi;
+        s.ih_lo[d] = fmaf(-hi, L, nd) / L;
+        s.kf[d] = 6.28318530717958647692f / L;
     }
-    s.inv_dV = (float)(M * rcp_d(s.V));
+    s.inv_dV = ((float)s.n[0] * (float)s.n[1] * (float)s.n[2]) / (float)s.V;
 }
 
 // CSVR scale factors (hymd/thermostat.py:167-219, Bussi-Parrinello 2008 form)
@@ -205,13 +210,13 @@ __device__ __forceinline__ void scr_update(const HpfScrArgs& a, double sum_v2,
         const double P = 0.5 * (ptot[0] + ptot[1]) * 16.61;
         const float R = ok ? (float)randoms[(int64_t)s * a.stride] : 0.0f;
         const float itau = 1.0f / (float)a.tau_p;
-        const float noise = sqrtf((float)(2.0 * a.n_b * a.gas_constant * a.target_temperature *
-                                          a.beta * a.dt_outer * a.n_b * iV) * itau) * R;
-        const float log_alpha =
-            -(float)(a.n_b * a.dt_outer * a.beta) * itau * (float)(a.target_pressure - P) + noise;
+        const float nb = (float)a.n_b, bdt = (float)a.beta * (float)a.dt_outer;
+        const float noise = sqrtf(2.0f * nb * (float)a.gas_constant *
+                                  (float)a.target_temperature * bdt * nb * (float)iV * itau) * R;
+        const float log_alpha = -(nb * bdt) * itau * (float)(a.target_pressure - P) + noise;
         const double alpha = (double)expf(log_alpha / 3.0f);
-        fill_box_state_dev(*bs, (double)(float)(bs->L[0] * alpha),
-                           (double)(float)(bs->L[1] * alpha), (double)(float)(bs->L[2] * alpha));
+        fill_box_state_dev(*bs, (float)(bs->L[0] * alpha), (float)(bs->L[1] * alpha),
+                           (float)(bs->L[2] * alpha));
         state[12] = alpha;
         state[13] = P;
     }
@@ -299,40 +304,93 @@ __device__ __forceinline__ DF df_shfl_down(DF v, int o) {
     return DF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
 }
 
-// Deterministic grid-wide sum of FP32 per-thread values (a thread adds only a
-// few terms) with compensated double-float arithmetic above the thread: warp,
-// block and the last block's pass over the block partials (stored as (hi, lo)
-// pairs) all run on the FP32 pipe -- GB300's FP64 pipe is a small fraction of
-// its FP32 one, and FP64 shuffles/adds in every block were a visible share of
-// short kernels.  out[k] = hi + lo in FP64.  Returns true on thread 0 of the
-// last block, after out[] has been written (for a fused epilogue).
+// Block sum of K float values in double-float (TwoSum) arithmetic, written
+// value-major as partials[k * G + blockIdx.x] (float2 hi/lo); G = number of
+// partial slots per value (the grid size).  All threads must call it.
 template <int K>
-__device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* partials,
-                                                    unsigned int* ticket, double* out) {
-    __shared__ float2 red[K * 32];
-    __shared__ bool is_last;
+__device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partials, unsigned int G) {
+    __shared__ float2 red_p[K * 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (blockDim.x + 31) >> 5;
-    DF v[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        v[k] = DF{vf[k], 0.0f};
+        DF v{vf[k], 0.0f};
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] = df_add(v[k], df_shfl_down(v[k], o));
-        if (lane == 0) red[k * 32 + warp] = make_float2(v[k].hi, v[k].lo);
+        for (int o = 16; o > 0; o >>= 1) v = df_add(v, df_shfl_down(v, o));
+        if (lane == 0) red_p[k * 32 + warp] = make_float2(v.hi, v.lo);
     }
     __syncthreads();
     float2* part = reinterpret_cast<float2*>(partials);
     if (warp == 0) {
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            const float2 x = lane < nw ? red[k * 32 + lane] : make_float2(0.0f, 0.0f);
-            DF s{x.x, x.y};
+            const float2 x = lane < nw ? red_p[k * 32 + lane] : make_float2(0.0f, 0.0f);
+            DF t{x.x, x.y};
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
-            if (lane == 0) part[(size_t)blockIdx.x * K + k] = make_float2(s.hi, s.lo);
+            for (int o = 16; o > 0; o >>= 1) t = df_add(t, df_shfl_down(t, o));
+            // value-major: the final pass's loads of one value are coalesced
+            if (lane == 0) part[(size_t)k * G + blockIdx.x] = make_float2(t.hi, t.lo);
         }
     }
+}
+
+// Sum of the G block partials of each of K values (written by
+// block_partials_f) by one block, in a fixed order: out[k] (double).
+// All threads of the block must call it; thread 0 writes out.
+template <int K>
+__device__ __forceinline__ void final_partials_f(const double* partials, unsigned int G,
+                                                 double* out) {
+    __shared__ float2 red_f[K * 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    const float2* part = reinterpret_cast<const float2*>(partials);
+    DF acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = DF{0.0f, 0.0f};
+    // two blocks' partials per thread and round trip
+    const unsigned int step = 2u * blockDim.x;
+    for (unsigned int b0 = threadIdx.x; b0 < G; b0 += step) {
+        const unsigned int b1 = b0 + blockDim.x;
+        float2 x0[K], x1[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            x0[k] = __ldcg(part + (size_t)k * G + b0);
+            x1[k] = b1 < G ? __ldcg(part + (size_t)k * G + b1) : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            acc[k] = df_add(acc[k], DF{x0[k].x, x0[k].y});
+            acc[k] = df_add(acc[k], DF{x1[k].x, x1[k].y});
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[k] = df_add(acc[k], df_shfl_down(acc[k], o));
+        if (lane == 0) red_f[k * 32 + warp] = make_float2(acc[k].hi, acc[k].lo);
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float2 x = lane < nw ? red_f[k * 32 + lane] : make_float2(0.0f, 0.0f);
+            DF t{x.x, x.y};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t = df_add(t, df_shfl_down(t, o));
+            if (lane == 0) out[k] = (double)t.hi + (double)t.lo;
+        }
+    }
+}
+
+// Grid-wide deterministic sum of K float values per thread: block partials,
+// then the last block to finish (ticket) sums them in a fixed order into
+// out[0..K).  Returns true on thread 0 of that last block (out is final
+// there); the ticket is reset for the next launch.
+template <int K>
+__device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* partials,
+                                                    unsigned int* ticket, double* out) {
+    __shared__ bool is_last;
+    block_partials_f<K>(vf, partials, gridDim.x);
     if (threadIdx.x == 0) {
         __threadfence();
         unsigned int t = atomicAdd(ticket, 1u);
@@ -341,34 +399,7 @@ __device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* part
     __syncthreads();
     if (!is_last) return false;
     __threadfence();
-    DF acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = DF{0.0f, 0.0f};
-    for (unsigned int bI = threadIdx.x; bI < gridDim.x; bI += blockDim.x) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const float2 x = __ldcg(part + (size_t)bI * K + k);
-            acc[k] = df_add(acc[k], DF{x.x, x.y});
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[k] = df_add(acc[k], df_shfl_down(acc[k], o));
-        if (lane == 0) red[k * 32 + warp] = make_float2(acc[k].hi, acc[k].lo);
-    }
-    __syncthreads();
-    if (warp == 0) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const float2 x = lane < nw ? red[k * 32 + lane] : make_float2(0.0f, 0.0f);
-            DF s{x.x, x.y};
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
-            if (lane == 0) out[k] = (double)s.hi + (double)s.lo;
-        }
-    }
+    final_partials_f<K>(partials, gridDim.x, out);
     if (threadIdx.x == 0) {
         *ticket = 0u;
         return true;
@@ -376,11 +407,6 @@ __device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* part
     return false;
 }
 
-// Deterministic grid-wide sum: each block stores its K partials; the last
-// block to finish (ticket) adds them -- thread j takes blocks j, j+B, ...,
-// then a fixed tree -- and writes out[k] (overwrite or accumulate).  The
-// order never depends on scheduling, and the ticket resets itself, so the
-// pattern is graph-replay safe.
 template <int K>
 __device__ __forceinline__ void grid_reduce_store(double (&v)[K], double* partials,
                                                   unsigned int* ticket, double* out,

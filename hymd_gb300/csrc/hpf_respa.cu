@@ -9,7 +9,7 @@
 //   * molecule groups: stage positions, velocities, bonded forces and the
 //     group's topology in shared memory, apply the first outer half kick with
 //     the slow forces, run all inner steps on chip, write back.  Groups of up
-//     to 256 beads are run by one warp each (phases separated by __syncwarp),
+//     to 64 beads are run by one warp each (phases separated by __syncwarp),
 //     larger ones by a whole CTA (__syncthreads);
 //   * free beads (in no bonded term): per thread, the outer kick and
 //     respa_inner drift/wrap steps (their bonded force is zero).
@@ -18,9 +18,10 @@
 // that touch it in a fixed order (incidence lists built by the planner), so
 // the bonded forces are bit-deterministic.
 // Energies and virials of the last inner step (the ones the reference keeps,
-// main.py:964-973) and sum v^2 are reduced by the grid's last block, which can
-// also run the isotropic SCR barostat (hymd/barostat_scr.py:34-132) right
-// there, since the barostat follows the inner loop (main.py:889-963).
+// main.py:964-973) and sum v^2 are written as block partials and summed by a
+// one-block finish kernel, which can also run the isotropic SCR barostat
+// (hymd/barostat_scr.py:34-132) there, since the barostat follows the inner
+// loop (main.py:889-963).
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -57,8 +58,7 @@ struct hpf_respa_plan {
     int2* dih_tl;      // (type, last)
     int* dih_gid;      // global dihedral index (dipole / transfer rows)
     int* free_ids;
-    double* partials;
-    unsigned int* ticket;
+    double* partials;   // [kOut][grid] block partials (float2 hi/lo per slot)
 };
 
 namespace {
@@ -67,14 +67,17 @@ constexpr int kThreads = 128;  // 4 warps
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxSlow = 4;
 constexpr int kOut = 10;  // E_bond, pr_bond[3], E_angle, pr_angle[3], E_dihedral, sum v^2
-constexpr int kWarpMaxBeads = 256;
+// Groups of up to this many beads run one per warp (about two beads and two
+// terms of each kind per lane); larger ones one per CTA, so that a long chain
+// gets one thread per bead and per term instead of a serial loop per lane.
+constexpr int kWarpMaxBeads = 64;
 
 struct SlowForces {
     const float* f[kMaxSlow];
     int n;
 };
 
-// Optional barostat run by the last block (all inner steps are done then).
+// Optional barostat run by the finish kernel (all inner steps are done then).
 struct BaroFuse {
     int on;
     HpfScrArgs a;
@@ -368,9 +371,7 @@ k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     } else {
         free_beads(p, blockIdx.x - n_grp_blocks, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
-    if (!out) return;
-    if (grid_reduce_store_f<kOut>(acc, p.partials, p.ticket, out) && baro.on)
-        scr_epilogue(baro, out, err);
+    if (out) block_partials_f<kOut>(acc, p.partials, gridDim.x);
 }
 
 template <bool DIH>
@@ -390,9 +391,18 @@ k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     } else {
         free_beads(p, blockIdx.x - p.n_groups, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
-    if (!out) return;
-    if (grid_reduce_store_f<kOut>(acc, p.partials, p.ticket, out) && baro.on)
-        scr_epilogue(baro, out, err);
+    if (out) block_partials_f<kOut>(acc, p.partials, gridDim.x);
+}
+
+// Sum of the block partials (fixed order) into out[0..kOut), then the
+// barostat when coupled.  A separate one-block launch: a last-block reduction
+// inside the main kernel (fence + ticket on every block, then a serial pass
+// at the end) cost more than this launch.
+__global__ void __launch_bounds__(256)
+k_respa_finish(const double* __restrict__ partials, unsigned int G, double* out, BaroFuse baro,
+               int* err) {
+    final_partials_f<kOut>(partials, G, out);
+    if (threadIdx.x == 0 && baro.on) scr_epilogue(baro, out, err);
 }
 
 // ------------------------------------------------------------- planner ---
@@ -437,7 +447,7 @@ int hpf_respa_plan_destroy(hpf_respa_plan* p) {
     void* ptrs[] = {p->grp_bead, p->bead_ids, p->bead_inc, p->inc_list, p->grp_bond,
                     p->bond_ij,  p->bond_p,   p->grp_ang,  p->ang_ijk,  p->ang_p,
                     p->grp_dih,  p->dih_ijkl, p->dih_coeff, p->dih_tl,  p->dih_gid,
-                    p->free_ids, p->partials, p->ticket};
+                    p->free_ids, p->partials};
     for (void* q : ptrs) cudaFree(q);
     delete p;
     return HPF_OK;
@@ -614,8 +624,10 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
         return HPF_ERR_NOT_IMPLEMENTED;
     }
     const int grp_blocks = warp_mode ? (G + kWarps - 1) / kWarps : G;
+    // free beads: a few per thread, over at least the SMs' worth of blocks
+    // that the molecule groups leave (grid-stride loop inside)
     int nfb = (p->n_free + kThreads - 1) / kThreads;
-    nfb = std::min(nfb, std::max(1, 152 * 8 - grp_blocks));
+    nfb = std::min(nfb, std::max(2 * 152, 152 * 8 - grp_blocks));
     if (p->n_free == 0) nfb = 0;
     p->n_free_blocks = nfb;
     int st = HPF_OK;
@@ -631,9 +643,7 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
         return st;
     }
     const int grid = grid_size(p);
-    if (cudaMalloc(&p->partials, sizeof(double) * kOut * (size_t)std::max(grid, 1)) != cudaSuccess ||
-        cudaMalloc(&p->ticket, sizeof(unsigned int)) != cudaSuccess ||
-        cudaMemset(p->ticket, 0, sizeof(unsigned int)) != cudaSuccess) {
+    if (cudaMalloc(&p->partials, sizeof(double) * kOut * (size_t)std::max(grid, 1)) != cudaSuccess) {
         hpf_respa_plan_destroy(p);
         return HPF_ERR_CUDA;
     }
@@ -709,6 +719,10 @@ int hpf_respa_step(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
     }
 #undef HPF_RESPA
     HPF_LAUNCH_CHECK();
+    if (out) {
+        k_respa_finish<<<1, 256, 0, st>>>(p->partials, (unsigned int)grid, out, bf, d_err);
+        HPF_LAUNCH_CHECK();
+    }
     return HPF_OK;
 }
 

@@ -26,7 +26,7 @@ from .force import BondedTopology
 
 class RespaMD:
     def __init__(self, positions, velocities, types, config, hamiltonian, topology=None,
-                 charges=None, device="cuda", fused=True, max_block_beads=36):
+                 charges=None, device="cuda", fused=True, max_block_beads="auto"):
         self.device = torch.device(device)
         self.config = config
         self.r = torch.as_tensor(np.asarray(positions, np.float32), device=self.device).contiguous()
@@ -67,9 +67,14 @@ class RespaMD:
             self.dipoles = torch.zeros((nd, 4, 3), dtype=torch.float32, device=self.device)
             self.transfer = torch.zeros((nd, 6, 3, 3), dtype=torch.float32, device=self.device)
         self.plan = None
+        self.block_timings = None
         if fused and self.topo is not None and packed is not None:
-            self.plan = self._make_plan(packed, max_block_beads)
+            if max_block_beads == "auto":
+                self.plan = self._tune_plan(packed)
+            else:
+                self.plan = self._make_plan(packed, max_block_beads)
         self.graph = None
+        self.graph_inner = self.graph_field = None
         self.field_sums = torch.zeros(8, dtype=torch.float64, device=self.device)
         self.thermo_args = None
         self.baro_args = None
@@ -84,7 +89,9 @@ class RespaMD:
         # memsets not counted): field step = paint, finalize, k-space, readout
         field = 4 + (4 if charges is not None else 0)
         if self.plan is not None:
-            self.launches_per_step = 1 + field  # second kick fused into the readout
+            # fused inner kernel + its one-block finish (sums, barostat); the
+            # second kick is fused into the readout
+            self.launches_per_step = 2 + field
         else:
             self.launches_per_step = 1 + self.respa * (1 + kinds) + 1 + field
 
@@ -107,6 +114,57 @@ class RespaMD:
         if code:
             raise _lib.HPFError("hpf_respa_plan_create", code)
         return h
+
+    # group sizes tried by the autotuner (beads per molecule group)
+    BLOCK_CANDIDATES = (12, 16, 24, 32, 36, 48, 64)
+
+    def _tune_plan(self, packed, reps=4):
+        """Molecule-group size of the fused inner kernel picked by timing it on
+        this system: each candidate plan runs `reps` launches (CUDA events) on
+        a copy of the state; the fastest is kept.  Candidates that give the
+        same grouping are timed once.  Timings (us) are kept in
+        `block_timings`."""
+        r, v = self.r.clone(), self.v.clone()
+        fb, slow = torch.zeros_like(self.r), torch.zeros_like(self.r)
+        arr = (_lib.P * 1)(_lib.ptr(slow))
+        st = _lib.stream_ptr()
+        best, seen, timings = None, set(), {}
+        for c in self.BLOCK_CANDIDATES:
+            plan = self._make_plan(packed, c)
+            if plan is None:
+                continue
+            a, b, m = _lib.I(), _lib.I(), _lib.I()
+            _lib.call("hpf_respa_plan_info", plan, _lib.ctypes.byref(a), _lib.ctypes.byref(b),
+                      _lib.ctypes.byref(m))
+            key = (a.value, m.value)
+            if key in seen:
+                _lib.lib().hpf_respa_plan_destroy(plan)
+                continue
+            seen.add(key)
+
+            def launch():
+                _lib.call("hpf_respa_step", plan, _lib.ptr(r), _lib.ptr(v), _lib.ptr(fb), arr, 1,
+                          self.mass, self.dt, self.respa, _lib.ptr(self.box), None, None, None,
+                          None, None, None, None, None, None, _lib.ptr(self.err), st)
+
+            launch()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                launch()
+            e1.record()
+            e1.synchronize()
+            t = e0.elapsed_time(e1) * 1000.0 / reps
+            timings[c] = t
+            if best is None or t < best[0]:
+                if best is not None:
+                    _lib.lib().hpf_respa_plan_destroy(best[1])
+                best = (t, plan)
+            else:
+                _lib.lib().hpf_respa_plan_destroy(plan)
+        self.err.zero_()
+        self.block_timings = timings
+        return None if best is None else best[1]
 
     def couple(self, thermostat=True, barostat=None, seed=0, n_steps=100000, groups=None,
                remove_com=True, target_pressure=1.0, beta=7.6e-4):
@@ -172,7 +230,7 @@ class RespaMD:
             self.baro_args = b
         if self.plan is not None:
             # CSVR: sums (with the fused second kick) + scale; the barostat runs
-            # in the respa kernel's last block and the paint
+            # in the rRESPA finish kernel and the paint
             self.launches_per_step += 1 if thermostat else 0
         else:
             self.launches_per_step += (1 if thermostat else 0) + (2 if barostat else 0)
@@ -328,42 +386,71 @@ class RespaMD:
     def step(self):
         """One outer rRESPA step (launch sequence only; no host sync)."""
         st = _lib.stream_ptr()
-        scale = None
         if self.plan is not None:
             self._inner_fused(st)  # includes the barostat's box update
-            if self.baro_args is not None:
-                scale = self.state.data_ptr() + 12 * 8  # alpha, applied in the paint
-        else:
-            self._inner_unfused(st)
-            if self.baro_args is not None:
-                self.bonded_out[0:4].copy_(self.ws_bond[:4])
-                self.bonded_out[4:8].copy_(self.ws_angle[:4])
-                self._barostat(st)
-        # second outer half kick (and the CSVR sums) fused into the last readout
+            self._outer_rest(st)
+            return
+        self._inner_unfused(st)
+        if self.baro_args is not None:
+            self.bonded_out[0:4].copy_(self.ws_bond[:4])
+            self.bonded_out[4:8].copy_(self.ws_angle[:4])
+            self._barostat(st)
+        self._outer_rest(st, fused=False)
+
+    def _outer_rest(self, st, fused=True):
+        """The part of the outer step after the inner loop: field forces with
+        the second outer half kick (and the CSVR sums) fused into the last
+        readout, then the thermostat's scaling."""
+        scale = None
+        if fused and self.baro_args is not None:
+            scale = self.state.data_ptr() + 12 * 8  # alpha, applied in the paint
         thermo = self.thermo_args is not None
         self._field(st, self.field_sums, pos_scale=scale, kick=self._kick_args(thermo))
         if thermo:
             _lib.call("hpf_csvr_scale", _lib.ptr(self.v), _lib.ptr(self.group), self.n,
                       _lib.ptr(self.state), int(self.thermo_args.remove_com), st)
 
-    def capture(self):
-        """Record one outer step in a CUDA graph (after a warm-up step)."""
+    def capture(self, split=False):
+        """Record one outer step in a CUDA graph (after a warm-up step).
+
+        With split=True (fused inner loop only) the step is recorded as two
+        graphs replayed back to back -- `graph_inner` (the fused rRESPA kernel)
+        and `graph_field` (field step, kick, thermostat) -- so that a caller
+        can put timing events between them."""
         s = torch.cuda.Stream(device=self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):
             self.step()
         torch.cuda.current_stream(self.device).wait_stream(s)
         torch.cuda.synchronize(self.device)
+        self.graph_inner = self.graph_field = None
+        if split and self.plan is not None:
+            gi, gf = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gi):
+                self._inner_fused(_lib.stream_ptr())
+            with torch.cuda.graph(gf, pool=gi.pool()):
+                self._outer_rest(_lib.stream_ptr())
+            self.graph_inner, self.graph_field = gi, gf
+            self.graph = None
+            return gi, gf
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
             self.step()
         self.graph = g
         return g
 
+    def replay(self):
+        """One outer step from the captured graph(s)."""
+        if self.graph_inner is not None:
+            self.graph_inner.replay()
+            self.graph_field.replay()
+        else:
+            self.graph.replay()
+
     def run(self, steps):
         for _ in range(steps):
-            if self.graph is not None:
-                self.graph.replay()
+            if self.graph is not None or self.graph_inner is not None:
+                self.replay()
             else:
                 self.step()
 

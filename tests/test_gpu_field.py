@@ -84,6 +84,53 @@ def test_paint_matches_oracle_and_is_deterministic():
         assert torch.equal(out, out2)
 
 
+@pytest.mark.parametrize("mesh,T,cluster", [
+    ((128, 128, 128), 1, 0.0),
+    ((64, 64, 64), 3, 0.6),      # clustered: hundreds of particles per cell
+    ((25, 21, 18), 3, 0.0),      # odd sizes, M not a multiple of 4
+    ((8, 6, 4), 2, 0.0),         # coarse: ~300 particles per cell
+])
+def test_paint_mesh_shapes_and_charge_paint(mesh, T, cluster):
+    """Density paint (hpf_paint) and charge paint (hpf_paint_charge) against
+    the oracle over mesh shapes and occupancies, and bit-identical to the
+    context-free paint."""
+    from hymd_gb300 import _lib
+    from hymd_gb300.field import ParticleMesh, paint_static
+    rng = np.random.default_rng(sum(mesh) + T)
+    box = np.array([9.0, 8.0, 7.5])
+    n = 60000
+    r = (rng.uniform(0, 1, (n, 3)) * box).astype(np.float32)
+    k = int(cluster * n)
+    r[:k] = np.mod(box / 3 + rng.normal(0, 0.15, (k, 3)), box).astype(np.float32)
+    types = rng.integers(0, T, n).astype(np.int32)
+    masses = list(rng.uniform(0.5, 2.0, T))
+    pm = ParticleMesh(mesh, box, T)
+    R = torch.as_tensor(r, device="cuda")
+    Ty = torch.as_tensor(types, device="cuda")
+    out = pm.real_field(T)
+    _lib.call("hpf_paint", pm._h, _lib.ptr(R), _lib.ptr(Ty), n, _lib.dvec(masses), _lib.ptr(out),
+              _lib.stream_ptr())
+    ref = paint_static(R, Ty, masses, mesh, box)
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
+    dV = np.prod(box) / np.prod(mesh)
+    g = out.cpu().numpy()
+    for t in range(T):
+        want = of.cic_paint(r[types == t].astype(np.float64), masses[t], mesh, box) / dV
+        assert np.max(np.abs(g[t] - want)) <= 2e-6 * np.max(np.abs(want))
+    q = np.zeros(n, np.float32)
+    qi = rng.permutation(n)[: n // 5]
+    q[qi] = rng.choice([-1.0, 1.0], len(qi)).astype(np.float32)
+    Q = torch.as_tensor(q, device="cuda")
+    rho = pm.real_field()
+    _lib.call("hpf_paint_charge", pm._h, _lib.ptr(R), _lib.ptr(Q), n, _lib.ptr(rho),
+              _lib.stream_ptr())
+    want = of.cic_paint(r.astype(np.float64), q.astype(np.float64), mesh, box) / dV
+    got = rho.cpu().numpy()
+    assert np.max(np.abs(got - want)) <= 2e-6 * np.max(np.abs(want))
+    pm.check_errors()
+
+
 @pytest.mark.parametrize("kind", ["DefaultWithChi", "DefaultNoChi", "SquaredPhi"])
 def test_update_field_and_forces_match_oracle(kind):
     cfg, ham, fun, r, types = make_system(2, kind=kind)

@@ -64,22 +64,29 @@ def test_graph_replay_matches_eager():
     assert rel_rms(a.v.cpu().numpy(), b.v.cpu().numpy()) < 1e-5
 
 
-def test_fused_inner_loop_matches_per_term_path():
+@pytest.mark.parametrize("n_res,max_block_beads", [(40, 256), (40, 36), (10, 36)])
+def test_fused_inner_loop_matches_per_term_path(n_res, max_block_beads):
     """Molecule-blocked fused kernel vs the per-term launch sequence on a
-    peptide system with CBT dihedrals, dipoles and PIC electrostatics."""
+    peptide system with CBT dihedrals, dipoles and PIC electrostatics: chains
+    of 80 beads (one CTA per group, groups of 3 or 1 chains) and of 20 beads
+    (one warp per group of 36 beads at most)."""
     from hymd_gb300 import systems
     from hymd_gb300.hamiltonian import get_hamiltonian
     from hymd_gb300.md import RespaMD
-    s = systems.charged_peptides(seed=7, n_chains=30, n_res=40, n_total=6000, box=8.0, mesh=32)
+    s = systems.charged_peptides(seed=7, n_chains=30, n_res=n_res, n_total=6000, box=8.0,
+                                 mesh=32)
     cfg = s["config"]
     ham = get_hamiltonian(cfg)
     kw = dict(topology=s["topology"], charges=s["charges"])
     a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, fused=True,
-                max_block_beads=256, **kw)
+                max_block_beads=max_block_beads, **kw)
     b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, fused=False, **kw)
     assert a.plan is not None and b.plan is None
     info = a.plan_info()
-    assert info["mol_blocks"] >= 10 and info["free_beads"] == 6000 - 30 * 80
+    per = 2 * n_res
+    assert info["free_beads"] == 6000 - 30 * per
+    assert info["max_block_beads"] <= max(max_block_beads, per)
+    assert info["mol_blocks"] >= 30 * per // max(max_block_beads, per)
     for m in (a, b):
         m.prime()
         m.run(2)
