@@ -280,6 +280,54 @@ def step_breakdown(md, flush, torch, reps=10):
     return tot
 
 
+def adjoint_cost(md, flush, torch, reps=10):
+    """Device time (us) of one forward field-force evaluation (hpf_field_step:
+    paint, r2c, k-space, c2r, readout) against the adjoint (hpf_field_adjoint)
+    giving dW/d(chi, kappa, sigma), and with dW/dx as well; each as a captured
+    graph, L2 flushed before each repetition."""
+    from hymd_gb300 import _lib
+    st = torch.cuda.current_stream()
+    T = md.T
+    sums = torch.zeros(T * (T + 1) // 2 + 1 + T, dtype=torch.float64, device=md.r.device)
+    grad = torch.empty_like(md.r)
+    f = torch.empty_like(md.r)
+
+    def fwd():
+        _lib.call("hpf_field_step", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n, md.masses,
+                  _lib.ptr(f), None, None, None, _lib.stream_ptr())
+
+    def adj(with_x):
+        def fn():
+            _lib.call("hpf_field_adjoint", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n,
+                      md.masses, _lib.ptr(grad) if with_x else None, _lib.ptr(sums),
+                      _lib.stream_ptr())
+        return fn
+
+    out = {}
+    for name, fn in (("forward_force_us", fwd), ("dW_dparams_us", adj(False)),
+                     ("dW_dx_and_params_us", adj(True))):
+        s = torch.cuda.Stream()
+        s.wait_stream(st)
+        with torch.cuda.stream(s):
+            fn()
+        st.wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            fn()
+        tot = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            g.replay()
+            b.record(st)
+            b.synchronize()
+            tot += a.elapsed_time(b) * 1000.0 / reps
+        out[name] = tot
+    out["params_over_forward"] = out["dW_dparams_us"] / out["forward_force_us"]
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -385,6 +433,7 @@ def run_gpu(args):
     bd = step_breakdown(md, flush, torch)
     if args.breakdown and rank == 0:
         print(json.dumps({"breakdown_us": bd}), file=sys.stderr)
+    adj = adjoint_cost(md, flush, torch)
     stage_bytes = {"paint": 16 * n + 4 * T * M, "kspace": 32 * T * Mc,
                    "readout_kick": 28 * n + 12 * T * M + 36 * n}
     kernels = {}
@@ -424,6 +473,7 @@ def run_gpu(args):
                              "note": "latency-bound in practice: the loop runs on chip and "
                                      "touches DRAM once per bead per launch (traffic)"},
                 "roofline_kernels": kernels,
+                "adjoint": adj,
                 "clocks": clk.summary(),
                 "cpu_baseline": cpu}
         print(json.dumps(line))

@@ -99,6 +99,7 @@ _SIGNATURES.update({
     "hpf_csvr": [P, P, I64, ctypes.POINTER(P), I, D, ctypes.POINTER(CsvrArgs), P, P, P, P, P, P],
     "hpf_scr_isotropic": [P, P, P, I64, P, P, ctypes.POINTER(ScrArgs), P, P, P, P, P, P],
     "hpf_paint_static": [P, P, I64, I, I, I, I, ctypes.POINTER(D), ctypes.POINTER(D), P, P, P],
+    "hpf_field_adjoint": [P, P, P, I64, ctypes.POINTER(D), P, P, P],
 })
 
 _LIB = None

@@ -517,6 +517,148 @@ __global__ void k_laplacian(const float2* __restrict__ phi_f, float2* __restrict
     }
 }
 
+// ---------------------------------------------------------------- adjoint ---
+// dW/dx: the filtered potential V_t = H * (Q phi~)_t read out with the
+// gradient of the CIC weights (phi_t = m_t/dV sum_i W(g - x_i), so
+// dW/dx_i = m_t sum_g V_t(g) grad W(g - x_i)); the constant b_t of
+// v_t = (Q phi~ + b)_t drops out of a gradient.
+// V_t(k) = H(k)^2 sum_j Q_tj phi_j(k) / M  (phi_j(k): raw r2c spectra).
+template <int TT>
+__global__ void k_kspace_pot(const float2* __restrict__ phi_raw, float2* __restrict__ out,
+                             int T_rt, int64_t Mc, KGeom g, const BoxState* __restrict__ bs,
+                             const Functional* __restrict__ fun) {
+    constexpr int TM = TT > 0 ? TT : HPF_MAX_TYPES;
+    const int T = TT > 0 ? TT : T_rt;
+    const float s2h = fun->sigma2_half;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        float kx, ky, kz, gx, gy, gz, wk;
+        mode_k(idx, g, bs, kx, ky, kz, gx, gy, gz, wk);
+        const float H = expf(-s2h * (kx * kx + ky * ky + kz * kz));
+        const float h2m = H * H * g.invM;
+        float2 ph[TM];
+#pragma unroll
+        for (int j = 0; j < TM; ++j)
+            ph[j] = j < T ? phi_raw[(int64_t)j * Mc + idx] : make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int t = 0; t < TM; ++t) {
+            if (t >= T) break;
+            float ux = 0.0f, uy = 0.0f;
+#pragma unroll
+            for (int j = 0; j < TM; ++j) {
+                if (j >= T) break;
+                const float q = fun->Q[t * T + j];
+                ux = fmaf(q, ph[j].x, ux);
+                uy = fmaf(q, ph[j].y, uy);
+            }
+            out[(int64_t)t * Mc + idx] = make_float2(ux * h2m, uy * h2m);
+        }
+    }
+}
+
+__global__ void k_readout_grad(const float* __restrict__ vg, const float* __restrict__ pos,
+                               const int32_t* __restrict__ types, int64_t n, int T, int64_t M,
+                               const BoxState* __restrict__ bs, TypeScale sc,
+                               float* __restrict__ grad, int* err) {
+    const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
+    const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
+    const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
+    const float i0 = h0 + l0, i1 = h1 + l1, i2 = h2 + l2;  // d(frac)/dx = n/L
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        const int t = types[i];
+        float gr[3] = {0.0f, 0.0f, 0.0f};
+        const bool ok = isfinite(x) && isfinite(y) && isfinite(z) && t >= 0 && t < T;
+        if (!ok) hpf_flag(err, (t >= 0 && t < T) ? HPF_ERR_NONFINITE : HPF_ERR_INDEX);
+        if (ok) {
+            int ix, iy, iz;
+            float fx, fy, fz;
+            grid_coord(x, h0, l0, n0, ix, fx);
+            grid_coord(y, h1, l1, n1, iy, fy);
+            grid_coord(z, h2, l2, n2, iz, fz);
+            const int xs[2] = {ix, ix + 1 == n0 ? 0 : ix + 1};
+            const int ys[2] = {iy, iy + 1 == n1 ? 0 : iy + 1};
+            const int zs[2] = {iz, iz + 1 == n2 ? 0 : iz + 1};
+            const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy}, wz[2] = {1.0f - fz, fz};
+            const float dx[2] = {-i0, i0}, dy[2] = {-i1, i1}, dz[2] = {-i2, i2};
+            const float* base = vg + (int64_t)t * M;
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    const int64_t row = ((int64_t)xs[a] * n1 + ys[b]) * n2;
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const float v = __ldg(base + row + zs[c]);
+                        gr[0] = fmaf(dx[a] * wy[b] * wz[c], v, gr[0]);
+                        gr[1] = fmaf(wx[a] * dy[b] * wz[c], v, gr[1]);
+                        gr[2] = fmaf(wx[a] * wy[b] * dz[c], v, gr[2]);
+                    }
+                }
+            const float m = sc.s[t];
+            gr[0] *= m;
+            gr[1] *= m;
+            gr[2] *= m;
+        }
+        grad[3 * i] = gr[0];
+        grad[3 * i + 1] = gr[1];
+        grad[3 * i + 2] = gr[2];
+    }
+}
+
+// Parseval sums for the parameter gradients over the raw FP32 spectra of
+// the densities (the forward path's r2c): for t <= j,
+// s_tj = sum_{k != 0} w_k Re(p_t^* p_j) and
+// r = sum_{k != 0} w_k k^2 sum_tj Q_tj Re(p_t^* p_j), p_t = H phi_t(k)/M,
+// into out[0..P) (row-major t <= j) and out[P]; out[P+1+t] = mean of phi_t.
+// FP32 products, per-thread FP32 sums over a few modes, double-float
+// (compensated) block and grid reduction.  With V these give
+// sum_g phi~_t phi~_j dV = V (s_tj + mean_t mean_j) and
+// sum_tj Q_tj sum_g phi~_j (-lap phi~_t) dV = V r.
+template <int TT>
+__global__ void k_adjoint_sums(const float2* __restrict__ spec, int64_t Mc, KGeom g,
+                               const BoxState* __restrict__ bs,
+                               const Functional* __restrict__ fun, double* out, double* partials,
+                               unsigned int* ticket) {
+    constexpr int P = TT * (TT + 1) / 2;
+    float acc[P + 1];
+#pragma unroll
+    for (int k = 0; k <= P; ++k) acc[k] = 0.0f;
+    const float s2h = fun->sigma2_half;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        if (idx == 0) {
+#pragma unroll
+            for (int j = 0; j < TT; ++j) out[P + 1 + j] = (double)spec[(int64_t)j * Mc].x * g.invM;
+            continue;
+        }
+        float kx, ky, kz, gx, gy, gz, wk;
+        mode_k(idx, g, bs, kx, ky, kz, gx, gy, gz, wk);
+        const float k2 = kx * kx + ky * ky + kz * kz;
+        const float Hm = expf(-s2h * k2) * g.invM;
+        float2 ph[TT];
+#pragma unroll
+        for (int j = 0; j < TT; ++j) {
+            const float2 r = spec[(int64_t)j * Mc + idx];
+            ph[j] = make_float2(r.x * Hm, r.y * Hm);
+        }
+        float q = 0.0f;
+        int p = 0;
+#pragma unroll
+        for (int t = 0; t < TT; ++t) {
+#pragma unroll
+            for (int j = t; j < TT; ++j) {
+                const float st = fmaf(ph[t].x, ph[j].x, ph[t].y * ph[j].y);
+                acc[p++] += wk * st;
+                q = fmaf((j == t ? 1.0f : 2.0f) * fun->Q[t * TT + j], st, q);
+            }
+        }
+        acc[P] = fmaf(wk * k2, q, acc[P]);
+    }
+    grid_reduce_store_f<P + 1>(acc, partials, ticket, out);
+}
+
 // ------------------------------------------------------------ host glue ---
 int make_plan(hpf_ctx* c, cufftHandle* plan, cufftType type, int batch, size_t* ws) {
     int n[3] = {c->n0, c->n1, c->n2};
@@ -547,6 +689,57 @@ int grid_for(int64_t work, int threads) {
     const int64_t cap = 152 * 32;
     return (int)(b < cap ? b : cap);
 }
+
+// The FP64 buffers and the D2Z plan (batch T+1: densities + charges) are
+// only needed for energies and gradients: created on first use.
+int ensure_d2z(hpf_ctx* c) {
+    if (c->has_d2z) return HPF_OK;
+    const int T = c->T;
+    HPF_CUDA_TRY(cudaMalloc(&c->d_grid64, sizeof(double) * (size_t)(T + 1) * c->M));
+    HPF_CUDA_TRY(cudaMalloc(&c->d_spec64, sizeof(double2) * (size_t)(T + 1) * c->Mc));
+    long long nn[3] = {c->n0, c->n1, c->n2};
+    size_t ws = 0;
+    if (cufftCreate(&c->plan_d2z) != CUFFT_SUCCESS) return HPF_ERR_CUFFT;
+    if (cufftMakePlanMany64(c->plan_d2z, 3, nn, NULL, 1, c->M, NULL, 1, c->Mc, CUFFT_D2Z, T + 1,
+                            &ws) != CUFFT_SUCCESS) {
+        cufftDestroy(c->plan_d2z);
+        return HPF_ERR_CUFFT;
+    }
+    c->has_d2z = true;
+    return HPF_OK;
+}
+
+// Densities (fixed-point paint) as FP64 grids and their D2Z spectra in
+// d_spec64 (slots 0..T-1; slot T holds the charges when given, else zeros).
+int density_spectra_f64(hpf_ctx* c, const float* pos, const int32_t* types, int64_t n,
+                        const double* type_mass, const float* charges, cudaStream_t st) {
+    int r = ensure_d2z(c);
+    if (r != HPF_OK) return r;
+    const int T = c->T;
+    TypeScaleD sc;
+    for (int t = 0; t < T; ++t) sc.s[t] = type_mass[t];
+    sc.s[T] = 1.0;
+    if (n > 0) {
+        k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, types, nullptr, n, T, c->d_box,
+                                                           c->d_acc, c->M, c->d_err, nullptr);
+        HPF_LAUNCH_CHECK();
+        if (charges) {
+            k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(
+                pos, nullptr, charges, n, 1, c->d_box, c->d_acc + (int64_t)T * c->M, c->M,
+                c->d_err, nullptr);
+            HPF_LAUNCH_CHECK();
+        }
+    }
+    k_paint_finalize_f64<<<grid_for((int64_t)(T + 1) * c->M, kThreads), kThreads, 0, st>>>(
+        c->d_acc, c->d_grid64, c->M, T + 1, sc, c->d_box);
+    HPF_LAUNCH_CHECK();
+    if (cufftSetStream(c->plan_d2z, st) != CUFFT_SUCCESS) return HPF_ERR_CUFFT;
+    if (cufftExecD2Z(c->plan_d2z, c->d_grid64, reinterpret_cast<cufftDoubleComplex*>(c->d_spec64)) !=
+        CUFFT_SUCCESS)
+        return HPF_ERR_CUFFT;
+    return HPF_OK;
+}
+
 
 int launch_kspace_force(hpf_ctx* c, const float2* phi_raw, float2* force_k, float2* phi_f,
                         float2* v_k, double* sums, cudaStream_t st) {
@@ -908,42 +1101,8 @@ int hpf_energy_fp64(hpf_ctx* c, const float* pos, const int32_t* types, int64_t 
     if (!c || !type_mass || !out || n < 0 || (n > 0 && (!pos || !types))) return HPF_ERR_ARG;
     cudaStream_t st = as_stream(stream);
     const int T = c->T;
-    if (!c->has_d2z) {
-        // lazily: the FP64 buffers and the D2Z plan are only needed for energies
-        HPF_CUDA_TRY(cudaMalloc(&c->d_grid64, sizeof(double) * (size_t)(T + 1) * c->M));
-        HPF_CUDA_TRY(cudaMalloc(&c->d_spec64, sizeof(double2) * (size_t)(T + 1) * c->Mc));
-        long long nn[3] = {c->n0, c->n1, c->n2};
-        size_t ws = 0;
-        if (cufftCreate(&c->plan_d2z) != CUFFT_SUCCESS) return HPF_ERR_CUFFT;
-        if (cufftMakePlanMany64(c->plan_d2z, 3, nn, NULL, 1, c->M, NULL, 1, c->Mc, CUFFT_D2Z,
-                                T + 1, &ws) != CUFFT_SUCCESS) {
-            cufftDestroy(c->plan_d2z);
-            return HPF_ERR_CUFFT;
-        }
-        c->has_d2z = true;
-    }
-    TypeScaleD sc;
-    for (int t = 0; t < T; ++t) sc.s[t] = type_mass[t];
-    sc.s[T] = 1.0;
-    // densities into accumulator slots 0..T-1, charges into slot T
-    if (n > 0) {
-        k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, types, nullptr, n, T, c->d_box,
-                                                           c->d_acc, c->M, c->d_err, nullptr);
-        HPF_LAUNCH_CHECK();
-        if (charges) {
-            k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(
-                pos, nullptr, charges, n, 1, c->d_box, c->d_acc + (int64_t)T * c->M, c->M,
-                c->d_err, nullptr);
-            HPF_LAUNCH_CHECK();
-        }
-    }
-    k_paint_finalize_f64<<<grid_for((int64_t)(T + 1) * c->M, kThreads), kThreads, 0, st>>>(
-        c->d_acc, c->d_grid64, c->M, T + 1, sc, c->d_box);
-    HPF_LAUNCH_CHECK();
-    if (cufftSetStream(c->plan_d2z, st) != CUFFT_SUCCESS) return HPF_ERR_CUFFT;
-    if (cufftExecD2Z(c->plan_d2z, c->d_grid64, reinterpret_cast<cufftDoubleComplex*>(c->d_spec64)) !=
-        CUFFT_SUCCESS)
-        return HPF_ERR_CUFFT;
+    int r0 = density_spectra_f64(c, pos, types, n, type_mass, charges, st);
+    if (r0 != HPF_OK) return r0;
     TypeScale qt;
     for (int t = 0; t < T; ++t) qt.s[t] = type_charges ? (float)type_charges[t] : 0.0f;
     KGeom g = kgeom(c);
@@ -1152,5 +1311,72 @@ extern "C" int hpf_paint_static(const float* pos, const int32_t* types, int64_t 
         k_paint_finalize1<<<grid, kThreads, 0, st>>>(acc, phi_out, M, T, sc, bs);
     }
     HPF_LAUNCH_CHECK();
+    return HPF_OK;
+}
+
+// ---------------------------------------------------------------- adjoint ---
+extern "C" int hpf_field_adjoint(hpf_ctx* c, const float* pos, const int32_t* types, int64_t n,
+                                 const double* type_mass, float* grad_pos, double* sums,
+                                 void* stream) {
+    if (!c || !type_mass || n < 0 || (n > 0 && (!pos || !types)) || (!grad_pos && !sums))
+        return HPF_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    const int T = c->T;
+    if (sums && T > 8) return HPF_ERR_NOT_IMPLEMENTED;
+    int r;
+    // densities and their raw spectra, shared by both parts
+    TypeScale sc;
+    for (int t = 0; t < T; ++t) sc.s[t] = (float)type_mass[t];
+    if ((r = do_paint(c, pos, types, nullptr, n, T, sc, c->d_grid, st)) != HPF_OK) return r;
+    if ((r = exec_r2c(c, c->d_grid, c->d_spec_phi, T, st)) != HPF_OK) return r;
+    if (grad_pos && n > 0) {
+        const KGeom g = kgeom(c);
+        const int grid = grid_for(c->Mc, kThreads);
+#define HPF_KP(TT)                                                                       \
+    k_kspace_pot<TT><<<grid, kThreads, 0, st>>>(c->d_spec_phi, c->d_spec, T, c->Mc, g, c->d_box, \
+                                                c->d_fun)
+        switch (T) {
+            case 1: HPF_KP(1); break;
+            case 2: HPF_KP(2); break;
+            case 3: HPF_KP(3); break;
+            case 4: HPF_KP(4); break;
+            case 5: HPF_KP(5); break;
+            case 6: HPF_KP(6); break;
+            case 7: HPF_KP(7); break;
+            case 8: HPF_KP(8); break;
+            default: HPF_KP(0); break;
+        }
+#undef HPF_KP
+        HPF_LAUNCH_CHECK();
+        if ((r = exec_c2r(c, c->d_spec, c->d_grid, T, st)) != HPF_OK) return r;
+        k_readout_grad<<<grid_for(n, kThreads), kThreads, 0, st>>>(c->d_grid, pos, types, n, T,
+                                                                   c->M, c->d_box, sc, grad_pos,
+                                                                   c->d_err);
+        HPF_LAUNCH_CHECK();
+    }
+    if (sums) {
+        const KGeom g = kgeom(c);
+        const int K = T * (T + 1) / 2 + 1;
+        int grid = reduce_grid(c->Mc, kThreads);
+        // K partials (float2) per block must fit the workspace's 8 * HPF_REDUCE_BLOCKS slots
+        if (grid > 8 * HPF_REDUCE_BLOCKS / K) grid = 8 * HPF_REDUCE_BLOCKS / K;
+        double* part = ws_partials(c->d_ws);
+        unsigned int* tick = ws_ticket(c->d_ws);
+#define HPF_KA(TT)                                                                          \
+    k_adjoint_sums<TT><<<grid, kThreads, 0, st>>>(c->d_spec_phi, c->Mc, g, c->d_box, c->d_fun, \
+                                                  sums, part, tick)
+        switch (T) {
+            case 1: HPF_KA(1); break;
+            case 2: HPF_KA(2); break;
+            case 3: HPF_KA(3); break;
+            case 4: HPF_KA(4); break;
+            case 5: HPF_KA(5); break;
+            case 6: HPF_KA(6); break;
+            case 7: HPF_KA(7); break;
+            default: HPF_KA(8); break;
+        }
+#undef HPF_KA
+        HPF_LAUNCH_CHECK();
+    }
     return HPF_OK;
 }

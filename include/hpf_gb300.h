@@ -178,6 +178,26 @@ int hpf_energy_fp64(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_
                     const double* type_mass, const float* charges, const double* type_charges,
                     double elec_factor, double* out, void* stream);
 
+/* ---- adjoint of the field energy ------------------------------------------
+ * Gradients of W = sum_g w(phi~(g)) dV (hymd/field.py:688-703 with the
+ * functional set by hpf_ctx_set_functional), for fitting the functional's
+ * parameters; the reference has no gradient code (it uses the force, the
+ * spectral readout of -grad V, which agrees with -dW/dx up to O(h^2)).
+ * grad_pos (device float[n][3], or NULL): dW/dx, the exact derivative of the
+ *   discrete W (CIC-weight gradient readout of H * Q phi~), FP32.
+ * sums (device double[P + 1 + T], P = T(T+1)/2, or NULL): Parseval sums
+ *   over the FP32 density spectra (FP32 products, compensated double-float
+ *   reduction); with p_t = H phi_t(k) / M over the half spectrum:
+ *   sums[p]   s_tj = sum_{k!=0} w_k Re(p_t conj p_j), p enumerating t <= j
+ *             row-major, so sum_g phi~_t phi~_j dV = V (s_tj + mean_t mean_j);
+ *   sums[P]   r = sum_{k!=0} w_k k^2 sum_tj Q_tj Re(p_t conj p_j), so that
+ *             dW/dsigma = -sigma V r;
+ *   sums[P+1+t] mean of phi_t.
+ * Both parts share one paint and one r2c.  T <= 8 for sums
+ * (HPF_ERR_NOT_IMPLEMENTED above). */
+int hpf_field_adjoint(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_t n,
+                      const double* type_mass, float* grad_pos, double* sums, void* stream);
+
 /* comp_laplacian (hymd/field.py:406-425): lap_out[t][d] = c2r(-k_d^2
  * phi_fourier[t]) for all T types and d = 0..2.  lap_out: float[T][3][M]. */
 int hpf_laplacian(hpf_ctx* ctx, const void* phi_fourier, float* lap_out, void* stream);

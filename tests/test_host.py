@@ -187,3 +187,19 @@ def test_integrator_formula_matches_reference_kat(golden):
                                rtol=0, atol=1e-13)
     np.testing.assert_allclose(r0 + dt * v0, m["integrator_kat/expected_positions"], rtol=0,
                                atol=1e-13)
+
+
+def test_adjoint_functional_coefficients_match_oracle():
+    """The (Q, b, c) the adjoint differentiates are those of the three
+    reference functionals (oracle/hamiltonian.py restates hymd/hamiltonian.py)."""
+    from hymd_gb300.adjoint import functional_coefficients
+    from oracle import hamiltonian as oh
+    rng = np.random.default_rng(1)
+    T = 4
+    chi = rng.uniform(0, 20, (T, T))
+    chi = 0.5 * (chi + chi.T)
+    for kind in ("DefaultWithChi", "DefaultNoChi", "SquaredPhi"):
+        Q, b, c = functional_coefficients(kind, chi, 0.05, 8.3, 8.0)
+        ref = oh.quadratic_from_params(kind, T, 0.05, 8.3, 8.0, chi)
+        assert np.allclose(Q, ref.Q, rtol=1e-14) and np.allclose(b, ref.b, rtol=1e-14)
+        assert c == pytest.approx(ref.c, rel=1e-14)
