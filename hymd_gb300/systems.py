@@ -54,7 +54,7 @@ def _config(**kw):
     return c
 
 
-def homopolymer_melt(seed=1, n_chains=1000, length=10, box=10.0, mesh=32):
+def homopolymer_melt(seed=1, n_chains=1000, length=10, box=10.0, mesh=32, chi_ab=15.0):
     rng = np.random.default_rng(seed)
     L = np.full(3, box)
     N = n_chains * length
@@ -72,7 +72,7 @@ def homopolymer_melt(seed=1, n_chains=1000, length=10, box=10.0, mesh=32):
                   respa_inner=10, time_step=0.03, target_temperature=323.0, tau=0.1,
                   hamiltonian="DefaultWithChi", unique_names=["A", "B"],
                   type_to_name_map={0: "A", 1: "B"}, m=[1.0, 1.0],
-                  chi=[Chi("A", "B", 15.0)],
+                  chi=[Chi("A", "B", float(chi_ab))],
                   bonds=[Bond("A", "A", 0.47, 1250.0), Bond("B", "B", 0.47, 1250.0)])
     # A and B chains have the same bond parameters, so one template serves both
     tmpl = prepare_bonds(np.zeros(length, int), np.full(length, b"A"), conn, idx, cfg)
@@ -92,7 +92,7 @@ _LIPID_DEPTH = np.array([0, 1, 2, 2, 3, 4, 5, 6, 3, 4, 5, 6], dtype=np.float64)
 _LIPID_SIDE = np.array([0, 0, -1, 1, -1, -1, -1, -1, 1, 1, 1, 1], dtype=np.float64)
 
 
-def lipid_membrane(seed=2, n_lipids=6000, n_water=90000, box=27.0, mesh=64):
+def lipid_membrane(seed=2, n_lipids=6000, n_water=90000, box=27.0, mesh=64, chi_cw=30.0):
     rng = np.random.default_rng(seed)
     L = np.full(3, box)
     zc = box / 2
@@ -125,7 +125,7 @@ def lipid_membrane(seed=2, n_lipids=6000, n_water=90000, box=27.0, mesh=64):
     N = len(r)
     molecules = np.concatenate([np.repeat(np.arange(n_lipids), 12),
                                 n_lipids + np.arange(n_water)])
-    chi = [Chi("C", "W", 30.0), Chi("C", "N", 15.0), Chi("C", "P", 15.0), Chi("C", "G", 6.0),
+    chi = [Chi("C", "W", float(chi_cw)), Chi("C", "N", 15.0), Chi("C", "P", 15.0), Chi("C", "G", 6.0),
            Chi("G", "W", 4.0)]
     bonds = [Bond(a, b, 0.47, 1250.0) for a, b in
              (("N", "P"), ("P", "G"), ("G", "G"), ("G", "C"), ("C", "C"))]
@@ -217,3 +217,37 @@ def charged_peptides(seed=3, n_chains=200, n_res=50, n_total=500_000, box=40.0, 
 
 BUILDERS = {"melt10k": homopolymer_melt, "membrane162k": lipid_membrane,
             "peptide500k": charged_peptides}
+
+REPLICA_MESHES = (32, 48, 64, 96)
+
+
+def replica_set(n_replicas=64, seed=5, n_min=5_000, n_max=200_000, density=8.3, spacing=0.4):
+    """Independent replicas mixing the melt and membrane recipes: bead counts
+    log-uniform in [n_min, n_max], cubic box for `density` beads/nm^3, mesh
+    from REPLICA_MESHES closest to box/spacing, chi_AB (melt) or chi_CW
+    (membrane) uniform in [5, 40] kJ/mol.  Even indices are melts, odd ones
+    membranes (44% of the beads in 12-bead lipids, as in the 162k membrane)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_replicas):
+        n = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        chi = float(rng.uniform(5.0, 40.0))
+        sub = int(rng.integers(1 << 30))
+        if i % 2 == 0:
+            n_chains = max(2, int(round(n / 10)))
+            N = 10 * n_chains
+        else:
+            n_lipids = max(2, int(round(0.44 * n / 12)))
+            n_water = max(1, int(round(n)) - 12 * n_lipids)
+            N = 12 * n_lipids + n_water
+        box = (N / density) ** (1.0 / 3.0)
+        mesh = min(REPLICA_MESHES, key=lambda m: abs(m - box / spacing))
+        if i % 2 == 0:
+            s = homopolymer_melt(seed=sub, n_chains=n_chains, box=box, mesh=mesh, chi_ab=chi)
+        else:
+            s = lipid_membrane(seed=sub, n_lipids=n_lipids, n_water=n_water, box=box, mesh=mesh,
+                               chi_cw=chi)
+        s["recipe"] = "melt" if i % 2 == 0 else "membrane"
+        s["chi"] = chi
+        out.append(s)
+    return out
