@@ -78,9 +78,10 @@ class CsvrArgs(ctypes.Structure):
 class ScrArgs(ctypes.Structure):
     """HpfScrArgs of include/hpf_gb300.h."""
     _fields_ = [("n_types", I), ("n_steps", I), ("stride", I), ("advance", I), ("every", I),
-                ("pad", I * 3), ("half_mQm", D), ("mass", D), ("gas_constant", D),
-                ("target_temperature", D), ("target_pressure", D), ("beta", D), ("tau_p", D),
-                ("dt_outer", D), ("n_b", D)]
+                ("mode", I), ("couple_l", I), ("couple_n", I), ("half_mQm", D), ("mass", D),
+                ("gas_constant", D), ("target_temperature", D), ("target_pressure", D),
+                ("beta", D), ("tau_p", D), ("dt_outer", D), ("n_b", D),
+                ("target_pressure_n", D)]
 
 
 class Kick(ctypes.Structure):
@@ -100,6 +101,8 @@ _SIGNATURES.update({
     "hpf_scr_isotropic": [P, P, P, I64, P, P, ctypes.POINTER(ScrArgs), P, P, P, P, P, P],
     "hpf_paint_static": [P, P, I64, I, I, I, I, ctypes.POINTER(D), ctypes.POINTER(D), P, P, P],
     "hpf_field_adjoint": [P, P, P, I64, ctypes.POINTER(D), P, P, P],
+    "hpf_scr_scale_positions": [P, I64, P, I, P],
+    "hpf_respa_forces": [P, P, P, P, P, P, P],
 })
 
 _LIB = None

@@ -182,12 +182,16 @@ __device__ __forceinline__ void csvr_update(const HpfCsvrArgs& a, const double* 
     if (a.advance) *counter = s + 1;
 }
 
-// Isotropic SCR step (hymd/barostat_scr.py:34-132) run by one thread once all
-// sums are final.  The pressure components are added in FP64; with the k = 0
-// densities mean_t = m_t N_t / V the field part of p0 + p1 reduces to
+// SCR barostat step run by one thread once all sums are final: isotropic
+// (hymd/barostat_scr.py:34-132) or semi-isotropic with z normal (:133-284).
+// The pressure components are added in FP64; with the k = 0 densities
+// mean_t = m_t N_t / V the field part of p0 + p1 reduces to
 //   -W/V + A + (Q mean + b).mean = A/2 + (1/2 mc.Q.mc) / V^2 - c.
 // `bonded` holds {E_bond, bond_pr[3], E_angle, angle_pr[3]}.  The box is kept
 // in float32 values, as the reference's float32 box_size array.
+// state[12] = alpha (semi-isotropic: lateral alpha_L), state[13] = P
+// (semi-isotropic: P_L), state[14] = alpha_N, state[15] = P_N,
+// state[10] = surface tension L_z/2 (P_N - P_L) (bar nm).
 __device__ __forceinline__ void scr_update(const HpfScrArgs& a, double sum_v2,
                                            const double* field, const double* bonded,
                                            const double* randoms, int* counter, BoxState* bs,
@@ -196,6 +200,7 @@ __device__ __forceinline__ void scr_update(const HpfScrArgs& a, double sum_v2,
     const bool ok = s >= 0 && s < a.n_steps;
     if (!ok) hpf_flag(err, HPF_ERR_INDEX);
     state[12] = 1.0;
+    state[14] = 1.0;
     if (!(a.every > 1 && (s + 1) % a.every != 0)) {
         const double V = bs->V;
         const double iV = rcp_d(V);
@@ -203,22 +208,56 @@ __device__ __forceinline__ void scr_update(const HpfScrArgs& a, double sum_v2,
         const double p_kin = (2.0 / 3.0) * iV * (0.5 * a.mass * sum_v2);
         const double p01 = 0.5 * A + a.half_mQm * iV * iV - fun->c;
         const double sig2 = 2.0 * fun->sigma2_half_d;
-        double ptot[2];
-        for (int d = 0; d < 2; ++d)
+        double ptot[3];
+        for (int d = 0; d < 3; ++d)
             ptot[d] = p_kin + p01 - sig2 * field[1 + d] + (bonded[1 + d] + bonded[5 + d]) * iV;
-        // the reference averages p_tot[-3:-1], i.e. the x and y components
-        const double P = 0.5 * (ptot[0] + ptot[1]) * 16.61;
-        const float R = ok ? (float)randoms[(int64_t)s * a.stride] : 0.0f;
         const float itau = 1.0f / (float)a.tau_p;
         const float nb = (float)a.n_b, bdt = (float)a.beta * (float)a.dt_outer;
-        const float noise = sqrtf(2.0f * nb * (float)a.gas_constant *
-                                  (float)a.target_temperature * bdt * nb * (float)iV * itau) * R;
-        const float log_alpha = -(nb * bdt) * itau * (float)(a.target_pressure - P) + noise;
-        const double alpha = (double)expf(log_alpha / 3.0f);
-        fill_box_state_dev(*bs, (float)(bs->L[0] * alpha), (float)(bs->L[1] * alpha),
-                           (float)(bs->L[2] * alpha));
-        state[12] = alpha;
-        state[13] = P;
+        const float kT = (float)a.gas_constant * (float)a.target_temperature;
+        if (a.mode == 0) {
+            // the reference averages p_tot[-3:-1], i.e. the x and y components
+            const double P = 0.5 * (ptot[0] + ptot[1]) * 16.61;
+            const float R = ok ? (float)randoms[(int64_t)s * a.stride] : 0.0f;
+            const float noise = sqrtf(2.0f * nb * kT * bdt * nb * (float)iV * itau) * R;
+            const float log_alpha = -(nb * bdt) * itau * (float)(a.target_pressure - P) + noise;
+            const double alpha = (double)expf(log_alpha / 3.0f);
+            fill_box_state_dev(*bs, (float)(bs->L[0] * alpha), (float)(bs->L[1] * alpha),
+                               (float)(bs->L[2] * alpha));
+            state[12] = alpha;
+            state[13] = P;
+        } else {
+            const double PL = 0.5 * (ptot[0] + ptot[1]) * 16.61, PN = ptot[2] * 16.61;
+            double L[3] = {bs->L[0], bs->L[1], bs->L[2]};
+            const double gamma = 0.5 * L[2] * (PN - PL);
+            const float Rxy = ok ? (float)randoms[(int64_t)s * a.stride] : 0.0f;
+            const float Rz = ok ? (float)randoms[(int64_t)s * a.stride + 1] : 0.0f;
+            double aL = 1.0, aN = 1.0;
+            if (a.couple_l) {
+                const float iVf = (float)rcp_d(L[0] * L[1] * L[2]);
+                const float noise = sqrtf(4.0f * nb * kT * bdt * nb * iVf * itau / 3.0f) * Rxy;
+                const float log_alpha =
+                    -2.0f * nb * bdt * itau / 3.0f *
+                        (float)(a.target_pressure - PL - gamma / L[2]) + noise;
+                aL = (double)expf(log_alpha / 2.0f);
+                L[0] = (double)(float)(L[0] * aL);
+                L[1] = (double)(float)(L[1] * aL);
+            }
+            if (a.couple_n) {
+                // the volume after the lateral rescale, as in the reference
+                const float iVf = (float)rcp_d(L[0] * L[1] * L[2]);
+                const float noise = sqrtf(2.0f * nb * kT * bdt * nb * iVf * itau / 3.0f) * Rz;
+                const float log_alpha =
+                    -nb * bdt * itau / 3.0f * (float)(a.target_pressure_n - PN) + noise;
+                aN = (double)expf(log_alpha);
+                L[2] = (double)(float)(L[2] * aN);
+            }
+            fill_box_state_dev(*bs, (float)L[0], (float)L[1], (float)L[2]);
+            state[10] = gamma;
+            state[12] = aL;
+            state[13] = PL;
+            state[14] = aN;
+            state[15] = PN;
+        }
     }
     if (a.advance) *counter = s + 1;
 }

@@ -5,7 +5,7 @@
 //   integrate_velocity / integrate_position   hymd/integrator.py:9-73
 //   outer kick, inner loop, wrap              hymd/main.py:802-887, 1143-1169
 //   csvr_thermostat                           hymd/thermostat.py:111-219
-//   isotropic SCR barostat                    hymd/barostat_scr.py:34-132
+//   SCR barostat, isotropic / semi-isotropic  hymd/barostat_scr.py:34-132, :133-284
 // Each reference call `v = v + 0.5 * dt * (F / m)` is one FP32 rounding of
 // F/m and one of the update; the kernels repeat exactly those roundings so
 // that trajectories follow the reference's FP32 arithmetic.
@@ -174,6 +174,21 @@ __global__ void k_scale_positions(float* __restrict__ r, int64_t n3, const doubl
         r[e] = r[e] * al;
 }
 
+// Semi-isotropic position update as the reference performs it
+// (hymd/barostat_scr.py:249, :280): `positions[:][0:2] *= alpha_L` and
+// `positions[:][2] *= alpha_N` index ROWS, so all three coordinates of
+// particles 0 and 1 are scaled by alpha_L and those of particle 2 by
+// alpha_N; every other particle keeps its coordinates.  float32 values times
+// a float64 factor, rounded back to float32.
+__global__ void k_scale_positions_semi(float* __restrict__ r, int64_t n,
+                                       const double* __restrict__ state) {
+    const int e = threadIdx.x;  // one block of 9 threads
+    const int p = e / 3;
+    if (e >= 9 || p >= n) return;
+    const double al = p < 2 ? state[12] : state[14];
+    r[e] = (float)((double)r[e] * al);
+}
+
 }  // namespace
 
 extern "C" {
@@ -238,6 +253,8 @@ int hpf_csvr_scale(float* v, const int32_t* group, int64_t n, const double* stat
     return HPF_OK;
 }
 
+int hpf_scr_scale_positions(float* r, int64_t n, const double* state, int mode, void* stream);
+
 int hpf_scr_isotropic(hpf_ctx* ctx, float* r, const float* v, int64_t n,
                       const double* field_sums, const double* bonded_out,
                       const HpfScrArgs* args, const double* randoms, int* counter,
@@ -250,7 +267,17 @@ int hpf_scr_isotropic(hpf_ctx* ctx, float* r, const float* v, int64_t n,
         v, 3 * n, ws, field_sums, bonded_out, *args, randoms, counter, ctx->d_box, ctx->d_fun,
         state, d_err);
     HPF_LAUNCH_CHECK();
-    k_scale_positions<<<grid_for(3 * n), kThreads, 0, st>>>(r, 3 * n, state);
+    return hpf_scr_scale_positions(r, n, state, args->mode, stream);
+}
+
+int hpf_scr_scale_positions(float* r, int64_t n, const double* state, int mode, void* stream) {
+    if (!r || !state || n < 0 || mode < 0 || mode > 1) return HPF_ERR_ARG;
+    if (n == 0) return HPF_OK;
+    cudaStream_t st = as_stream(stream);
+    if (mode == 0)
+        k_scale_positions<<<grid_for(3 * n), kThreads, 0, st>>>(r, 3 * n, state);
+    else
+        k_scale_positions_semi<<<1, 9, 0, st>>>(r, n, state);
     HPF_LAUNCH_CHECK();
     return HPF_OK;
 }

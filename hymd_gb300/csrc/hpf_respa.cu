@@ -172,7 +172,9 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                                           float hdt, float dt, int respa, const Box& bx,
                                           float* __restrict__ dipoles,
                                           float* __restrict__ transfer, float (&acc)[kOut],
-                                          Sync sync) {
+                                          Sync sync, bool forces_only) {
+    // forces_only: bonded forces (and energies) at the current positions
+    // only -- no kicks, no drift, v and r untouched (respa is 1 then)
     const GroupSmem s = carve(smem_base, p);
     const int s0 = p.grp_bead[grp], nb = p.grp_bead[grp + 1] - s0;
     const int b0 = p.grp_bond[grp], nbd = p.grp_bond[grp + 1] - b0;
@@ -184,7 +186,7 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
     for (int e = lane; e < 3 * nb; e += width) {
         const int i = e / 3, d = e - 3 * i;
         const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
-        float x = v[g];
+        float x = forces_only ? 0.0f : v[g];
         for (int q = 0; q < slow.n; ++q) x = x + h_out * div_m(slow.f[q][g], mass, inv_m);
         s.vs[e] = x;
         s.rs[e] = r[g];
@@ -232,6 +234,7 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                 s.fs[3 * i + 1] = F[1];
                 s.fs[3 * i + 2] = F[2];
             }
+            if (forces_only) continue;
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 const float a = div_m(F[d], mass, inv_m);
@@ -316,6 +319,10 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
     // write back (each bead by the lane that owns it)
     for (int i = lane; i < nb; i += width) {
         const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i];
+        if (forces_only) {
+            for (int d = 0; d < 3; ++d) fb[g + d] = s.fs[3 * i + d];
+            continue;
+        }
         for (int d = 0; d < 3; ++d) {
             const float x = s.vs[3 * i + d];
             v[g + d] = x;
@@ -355,7 +362,7 @@ __global__ void __launch_bounds__(kThreads)
 k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
              float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
              int respa, const double* __restrict__ box, float* __restrict__ dipoles,
-             float* __restrict__ transfer, double* out, BaroFuse baro, int* err) {
+             float* __restrict__ transfer, double* out, int forces_only) {
     extern __shared__ __align__(16) char smem[];
     const Box bx = load_box(box);
     float acc[kOut];
@@ -367,8 +374,9 @@ k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
         const int grp = blockIdx.x * kWarps + warp;
         if (grp < p.n_groups)
             run_group<DIH>(p, grp, lane, 32, smem + (size_t)warp * p.smem_group, r, v, fb, slow,
-                           mass, h_out, hdt, dt, respa, bx, dipoles, transfer, acc, WarpSync());
-    } else {
+                           mass, h_out, hdt, dt, respa, bx, dipoles, transfer, acc, WarpSync(),
+                           forces_only != 0);
+    } else if (!forces_only) {
         free_beads(p, blockIdx.x - n_grp_blocks, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
     if (out) block_partials_f<kOut>(acc, p.partials, gridDim.x);
@@ -379,7 +387,7 @@ __global__ void __launch_bounds__(kThreads)
 k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
             float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
             int respa, const double* __restrict__ box, float* __restrict__ dipoles,
-            float* __restrict__ transfer, double* out, BaroFuse baro, int* err) {
+            float* __restrict__ transfer, double* out, int forces_only) {
     extern __shared__ __align__(16) char smem[];
     const Box bx = load_box(box);
     float acc[kOut];
@@ -387,8 +395,8 @@ k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     for (int k = 0; k < kOut; ++k) acc[k] = 0.0f;
     if ((int)blockIdx.x < p.n_groups) {
         run_group<DIH>(p, blockIdx.x, threadIdx.x, kThreads, smem, r, v, fb, slow, mass, h_out,
-                       hdt, dt, respa, bx, dipoles, transfer, acc, CtaSync());
-    } else {
+                       hdt, dt, respa, bx, dipoles, transfer, acc, CtaSync(), forces_only != 0);
+    } else if (!forces_only) {
         free_beads(p, blockIdx.x - p.n_groups, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
     if (out) block_partials_f<kOut>(acc, p.partials, gridDim.x);
@@ -708,8 +716,7 @@ int hpf_respa_step(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
     const float h_out = (float)(0.5 * respa_inner * dt), hdt = (float)(0.5 * dt);
 #define HPF_RESPA(K)                                                                          \
     K<<<grid, kThreads, p->smem, st>>>(*p, r, v, f_bonded, sf, (float)mass, h_out, hdt,        \
-                                       (float)dt, respa_inner, box, dipoles, transfer, out, bf, \
-                                       d_err)
+                                       (float)dt, respa_inner, box, dipoles, transfer, out, 0)
     if (p->warp_mode) {
         if (p->has_dih) HPF_RESPA(k_respa_warp<true>);
         else HPF_RESPA(k_respa_warp<false>);
@@ -721,6 +728,37 @@ int hpf_respa_step(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
     HPF_LAUNCH_CHECK();
     if (out) {
         k_respa_finish<<<1, 256, 0, st>>>(p->partials, (unsigned int)grid, out, bf, d_err);
+        HPF_LAUNCH_CHECK();
+    }
+    return HPF_OK;
+}
+
+int hpf_respa_forces(hpf_respa_plan* p, const float* r, float* f_bonded, const double* box,
+                     double* out, int* d_err, void* stream) {
+    if (!p || !r || !f_bonded || !box) return HPF_ERR_ARG;
+    const int grid = p->warp_mode ? (p->n_groups + kWarps - 1) / kWarps : p->n_groups;
+    if (grid == 0) return HPF_OK;
+    cudaStream_t st = as_stream(stream);
+    SlowForces sf;
+    sf.n = 0;
+    // v is neither read nor written in this mode; r is only read
+    float* rr = const_cast<float*>(r);
+#define HPF_RESPA_F(K)                                                                       \
+    K<<<grid, kThreads, p->smem, st>>>(*p, rr, nullptr, f_bonded, sf, 1.0f, 0.0f, 0.0f, 0.0f, \
+                                       1, box, nullptr, nullptr, out, 1)
+    if (p->warp_mode) {
+        if (p->has_dih) HPF_RESPA_F(k_respa_warp<true>);
+        else HPF_RESPA_F(k_respa_warp<false>);
+    } else {
+        if (p->has_dih) HPF_RESPA_F(k_respa_cta<true>);
+        else HPF_RESPA_F(k_respa_cta<false>);
+    }
+#undef HPF_RESPA_F
+    HPF_LAUNCH_CHECK();
+    if (out) {
+        BaroFuse none;
+        memset(&none, 0, sizeof(none));
+        k_respa_finish<<<1, 256, 0, st>>>(p->partials, (unsigned int)grid, out, none, d_err);
         HPF_LAUNCH_CHECK();
     }
     return HPF_OK;

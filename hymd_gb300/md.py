@@ -78,6 +78,7 @@ class RespaMD:
         self.field_sums = torch.zeros(8, dtype=torch.float64, device=self.device)
         self.thermo_args = None
         self.baro_args = None
+        self.baro_mode = 0
         self.counter = torch.zeros(4, dtype=torch.int32, device=self.device)
         self.state = torch.zeros(16, dtype=torch.float64, device=self.device)
         self.ws_md = _lib.new_workspace(self.device)
@@ -169,13 +170,17 @@ class RespaMD:
     def couple(self, thermostat=True, barostat=None, seed=0, n_steps=100000, groups=None,
                remove_com=True, target_pressure=1.0, beta=7.6e-4):
         """Enable the CSVR thermostat (hymd/thermostat.py:111-219) and/or the
-        isotropic SCR barostat (hymd/barostat_scr.py:34-132) on the device.
+        SCR barostat on the device: barostat="isotropic"
+        (hymd/barostat_scr.py:34-132, target_pressure in bar) or
+        "semiisotropic" (:133-284, target_pressure = (P_L, P_N) in bar; a
+        direction with a zero target is not coupled, as in the reference).
 
         The random numbers of `n_steps` outer steps are drawn now with
         numpy's default_rng(seed), in the reference's order per step: the
-        barostat's normal(), then for each thermostat group normal() and
-        chisquare(3 N_g - 1).  groups: optional int array (0/1) of coupling
-        groups (default: one group of all particles)."""
+        barostat's normal() (semi-isotropic: lateral, then normal), then for
+        each thermostat group normal() and chisquare(3 N_g - 1).  groups:
+        optional int array (0/1) of coupling groups (default: one group of all
+        particles)."""
         cfg = self.config
         every = int(cfg.n_b or 1)
         ng = 1
@@ -188,33 +193,42 @@ class RespaMD:
                 raise NotImplementedError("at most two thermostat coupling groups")
             self.group = torch.as_tensor(g, device=self.device)
             counts = [float(np.sum(g == 0)), float(np.sum(g == 1))]
-        stride = 1 + 2 * ng
+        if barostat not in (None, False, "isotropic", "semiisotropic"):
+            raise NotImplementedError(f"device barostat {barostat!r}")
+        nbar = 2 if barostat == "semiisotropic" else 1
+        stride = nbar + 2 * ng
         rng = np.random.default_rng(seed)
         table = np.zeros((n_steps, stride))
         for s in range(n_steps):
             if (s + 1) % every:
                 continue
             if barostat:
-                table[s, 0] = rng.normal()
+                for q in range(nbar):
+                    table[s, q] = rng.normal()
             if thermostat:
                 for gi in range(ng):
-                    table[s, 1 + 2 * gi] = rng.normal()
-                    table[s, 2 + 2 * gi] = rng.chisquare(3 * int(counts[gi]) - 1)
+                    table[s, nbar + 2 * gi] = rng.normal()
+                    table[s, nbar + 1 + 2 * gi] = rng.chisquare(3 * int(counts[gi]) - 1)
         self.randoms = torch.as_tensor(table.reshape(-1), device=self.device)
         dt_o = self.respa * self.dt
         if thermostat:
             a = _lib.CsvrArgs()
             a.n_groups, a.remove_com, a.n_steps, a.stride = ng, int(remove_com), n_steps, stride
-            a.offset, a.advance, a.every = 1, 1, every
+            a.offset, a.advance, a.every = nbar, 1, every
             a.count[0], a.count[1] = counts
             a.mass, a.gas_constant = self.mass, cfg.gas_constant
             a.target_temperature = float(cfg.target_temperature)
             a.c = float(np.exp(-dt_o / cfg.tau))
             self.thermo_args = a
+        self.baro_mode = 0
         if barostat:
-            if barostat != "isotropic":
-                raise NotImplementedError("device barostat: isotropic SCR")
             b = _lib.ScrArgs()
+            if barostat == "semiisotropic":
+                p_l, p_n = target_pressure
+                b.mode, b.couple_l, b.couple_n = 1, int(bool(p_l)), int(bool(p_n))
+                b.target_pressure_n = float(p_n or 0.0)
+                target_pressure = float(p_l or 0.0)
+                self.baro_mode = 1
             b.n_types, b.n_steps, b.stride = self.T, n_steps, stride
             b.advance = 0 if thermostat else 1
             b.every = every
@@ -230,8 +244,9 @@ class RespaMD:
             self.baro_args = b
         if self.plan is not None:
             # CSVR: sums (with the fused second kick) + scale; the barostat runs
-            # in the rRESPA finish kernel and the paint
-            self.launches_per_step += 1 if thermostat else 0
+            # in the rRESPA finish kernel and the paint (semi-isotropic: a
+            # position kernel of its own)
+            self.launches_per_step += (1 if thermostat else 0) + self.baro_mode
         else:
             self.launches_per_step += (1 if thermostat else 0) + (2 if barostat else 0)
         # (the CSVR sums ride in the readout; its scaling is one more launch)
@@ -343,13 +358,19 @@ class RespaMD:
                       None, None, kick, st)
 
     def prime(self):
-        """Bonded and slow forces at the initial positions (main.py:494-588)."""
+        """Bonded and slow forces at the initial positions (main.py:494-588).
+        With the fused plan the bonded forces come from its deterministic
+        gather (hpf_respa_forces), so that runs are bit-reproducible."""
         st = _lib.stream_ptr()
         self._bonded(st, 0)
         if self.topo is not None:
-            self.f_b.copy_(self.f_bond)
-            self.f_b.add_(self.f_angle)
-            self.f_b.add_(self.f_dih)
+            if self.plan is not None:
+                _lib.call("hpf_respa_forces", self.plan, _lib.ptr(self.r), _lib.ptr(self.f_b),
+                          _lib.ptr(self.box), None, _lib.ptr(self.err), st)
+            else:
+                self.f_b.copy_(self.f_bond)
+                self.f_b.add_(self.f_angle)
+                self.f_b.add_(self.f_dih)
         self._field(st, self.field_sums)
         if self.baro_args is not None:
             # the barostat reads the bonded virials of the last inner step
@@ -403,7 +424,11 @@ class RespaMD:
         readout, then the thermostat's scaling."""
         scale = None
         if fused and self.baro_args is not None:
-            scale = self.state.data_ptr() + 12 * 8  # alpha, applied in the paint
+            if self.baro_mode == 0:
+                scale = self.state.data_ptr() + 12 * 8  # alpha, applied in the paint
+            else:
+                _lib.call("hpf_scr_scale_positions", _lib.ptr(self.r), self.n,
+                          _lib.ptr(self.state), 1, st)
         thermo = self.thermo_args is not None
         self._field(st, self.field_sums, pos_scale=scale, kick=self._kick_args(thermo))
         if thermo:

@@ -71,15 +71,23 @@ typedef struct {
     double c;           /* exp(-dt_outer / tau)                                  */
 } HpfCsvrArgs;
 
+/* SCR barostat (hymd/barostat_scr.py).  mode 0: isotropic (:34-132), one
+ * normal() per barostat step at row[0]; mode 1: semi-isotropic with z normal
+ * (:133-284), normal() for the lateral then the normal direction at row[0]
+ * and row[1]; a direction is coupled when its target pressure is nonzero
+ * (couple_l / couple_n, the reference's truth test of P_L / P_N). */
 typedef struct {
     int n_types, n_steps, stride, advance;
-    int every, pad[3];
+    int every;
+    int mode;               /* 0 isotropic, 1 semi-isotropic                     */
+    int couple_l, couple_n; /* semi-isotropic: lateral / normal directions coupled */
     double half_mQm;        /* 1/2 mc.Q.mc with mc_t = m_t N_t (paint mass x count),
                                so the k = 0 densities are mc_t / V               */
     double mass, gas_constant, target_temperature;
-    double target_pressure; /* bar                                              */
+    double target_pressure; /* bar (semi-isotropic: lateral P_L)                */
     double beta;            /* isothermal compressibility (1/bar)               */
     double tau_p, dt_outer, n_b;
+    double target_pressure_n; /* bar, semi-isotropic normal P_N                 */
 } HpfScrArgs;
 
 /* Optional outer half kick fused into the last readout of a field
@@ -325,16 +333,25 @@ int hpf_csvr(float* v, const int32_t* group, int64_t n, const float* const* kick
  * v alpha_g without COM removal) from state (hymd/thermostat.py:210-217). */
 int hpf_csvr_scale(float* v, const int32_t* group, int64_t n, const double* state,
                    int remove_com, void* stream);
-/* Stochastic cell rescaling, isotropic (hymd/barostat_scr.py:34-132): the
- * pressure from field_sums (device double[4] = A, B_xyz of the last field
- * evaluation, see hpf_kspace_force), bonded_out (device double[9] of
- * hpf_respa_step) and the kinetic energy of v; then box (the context's device
- * box state, kept in float32 values as the reference does) and positions are
- * scaled by alpha.  state[12] = alpha, state[13] = P (bar). */
+/* Stochastic cell rescaling (hymd/barostat_scr.py): args->mode 0 isotropic
+ * (:34-132), 1 semi-isotropic with z normal (:133-284).  The pressure from
+ * field_sums (device double[4] = A, B_xyz of the last field evaluation, see
+ * hpf_kspace_force), bonded_out (device double[9] of hpf_respa_step) and the
+ * kinetic energy of v; then the box (the context's device box state, kept in
+ * float32 values as the reference does) and the positions are rescaled as
+ * hpf_scr_scale_positions does.  state[12] = alpha (semi: alpha_L),
+ * state[13] = P (semi: P_L, bar), state[14] = alpha_N, state[15] = P_N,
+ * state[10] = surface tension (semi, bar nm). */
 int hpf_scr_isotropic(hpf_ctx* ctx, float* r, const float* v, int64_t n,
                       const double* field_sums, const double* bonded_out,
                       const HpfScrArgs* args, const double* randoms, int* counter,
                       double* state, double* ws, int* d_err, void* stream);
+/* Position update of an SCR step from `state` (above).  mode 0: every
+ * coordinate times alpha (barostat_scr.py:128).  mode 1: the reference's
+ * `positions[:][0:2] *= alpha_L; positions[:][2] *= alpha_N` (:249, :280),
+ * which index rows: all coordinates of particles 0 and 1 times alpha_L and
+ * of particle 2 times alpha_N, the others unchanged. */
+int hpf_scr_scale_positions(float* r, int64_t n, const double* state, int mode, void* stream);
 
 /* One launch of the fused rRESPA inner loop: the first outer half kick
  * v += 0.5 respa_inner dt F_s / mass for each slow force array (field, PIC,
@@ -357,6 +374,17 @@ int hpf_respa_step(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
                    double* out, hpf_ctx* baro_ctx, const HpfScrArgs* baro,
                    const double* field_sums, const double* randoms, int* counter, double* state,
                    int* d_err, void* stream);
+
+/* Bonded forces (bonds, angles, dihedrals with CBT) of the plan's topology at
+ * positions r, without any integration: f_bonded of every bead in a bonded
+ * term is overwritten with its force (other beads untouched), summed in the
+ * plan's fixed incidence order, so the result is bit-reproducible (the
+ * per-term kernels above accumulate with atomics).  out (device double[10]
+ * or NULL): energies and virials as hpf_respa_step's out[0..8]; out[9] = 0.
+ * The forces of compute_bond/angle/dihedral_forces (main.py:494-550) for the
+ * first step of an rRESPA run. */
+int hpf_respa_forces(hpf_respa_plan* plan, const float* r, float* f_bonded, const double* box,
+                     double* out, int* d_err, void* stream);
 
 /* Sum over particles of v^2 into out[0] (device workspace, HPF_OUT_DOUBLES);
  * KE = mass/2 * out[0]. */

@@ -1,5 +1,5 @@
 """Device CSVR thermostat and SCR barostat against host restatements of
-hymd/thermostat.py:111-219 and hymd/barostat_scr.py:34-132."""
+hymd/thermostat.py:111-219 and hymd/barostat_scr.py:34-284."""
 import numpy as np
 import pytest
 
@@ -92,6 +92,71 @@ def test_scr_barostat_matches_reference_formula():
                                                           rel=1e-6)
     assert box1 == pytest.approx((box0 * alpha).astype(np.float32).astype(np.float64), rel=1e-7)
     assert np.allclose(r_after, (r_before * alpha).astype(np.float32), rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("targets", [(1.0, 1.0), (1.0, 0.0), (0.0, 1.0)])
+def test_semiisotropic_barostat_matches_reference_formula(targets):
+    """Semi-isotropic SCR with z normal (hymd/barostat_scr.py:133-284): lateral
+    and normal pressures, surface tension, the two scale factors, the box,
+    and the reference's row-indexed position update (particles 0 and 1 by
+    alpha_L, particle 2 by alpha_N, the rest unchanged); a zero target leaves
+    its direction uncoupled."""
+    from hymd_gb300 import _lib
+    from hymd_gb300.md import RespaMD
+    s, cfg, ham = _system()
+    md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    md.couple(thermostat=False, barostat="semiisotropic", seed=6, n_steps=10,
+              target_pressure=targets)
+    md.prime()
+    r_field = md.r.cpu().numpy().copy()
+    box0 = md.box_now()
+    st = _lib.stream_ptr()
+    md._inner_fused(st)
+    r_before = md.r.cpu().numpy().copy()
+    v = md.v.cpu().numpy()
+    bonded = md.bonded_out.cpu().numpy()
+    box1 = md.box_now()
+    md._outer_rest(st)  # position update, then the field at the new box
+    r_after = md.r.cpu().numpy()
+    fun = _functional(cfg)
+    ref = of.update_field(r_field.astype(np.float64), s["types"], cfg.n_types, cfg.mesh(), box0,
+                          cfg.m, fun, cfg.sigma)
+    P18 = of.comp_pressure(ref["phi"], ref["phi_fourier"], fun, v, cfg.mass, cfg.mesh(), box0,
+                           cfg.sigma, bonded[1:4], bonded[5:8])
+    PL = (P18[-3] + P18[-2]) / 2 * 16.61
+    PN = P18[-1] * 16.61
+    gamma = box0[2] / 2 * (PN - PL)
+    Rxy, Rz = md.randoms.cpu().numpy().reshape(10, -1)[0, :2]
+    dt_o = cfg.respa_inner * cfg.time_step
+    beta, T_, R_ = 7.6e-4, cfg.target_temperature, cfg.gas_constant
+    box = box0.astype(np.float32).copy()
+    aL = aN = 1.0
+    if targets[0]:
+        V = np.prod(box.astype(np.float64))
+        noise = np.sqrt(4.0 * R_ * T_ * beta * dt_o / (3 * V * cfg.tau_p)) * Rxy
+        la = -2.0 * dt_o * beta / (3 * cfg.tau_p) * (targets[0] - PL - gamma / box[2]) + noise
+        aL = np.exp(la / 2.0)
+        box[0:2] *= aL
+    if targets[1]:
+        V = np.prod(box.astype(np.float64))
+        noise = np.sqrt(2.0 * R_ * T_ * beta * dt_o / (3 * V * cfg.tau_p)) * Rz
+        la = -dt_o * beta / (3 * cfg.tau_p) * (targets[1] - PN) + noise
+        aN = np.exp(la)
+        box[2] *= aN
+    state = md.state.cpu().numpy()
+    assert state[13] == pytest.approx(PL, rel=1e-5, abs=5e-2)
+    assert state[15] == pytest.approx(PN, rel=1e-5, abs=5e-2)
+    assert state[10] == pytest.approx(gamma, rel=1e-5, abs=5e-1)
+    assert state[12] == pytest.approx(aL, rel=1e-7)
+    assert state[14] == pytest.approx(aN, rel=1e-7)
+    assert box1 == pytest.approx(box.astype(np.float64), rel=1e-7)
+    want = r_before.copy()
+    want[0:2] = (r_before[0:2].astype(np.float64) * aL).astype(np.float32)
+    want[2] = (r_before[2].astype(np.float64) * aN).astype(np.float32)
+    # the field step's paint may wrap nothing here: positions are only rescaled
+    assert np.allclose(r_after[:3], want[:3], rtol=1e-6, atol=1e-6)
+    assert np.array_equal(r_after[3:], r_before[3:])
+    md.check_errors()
 
 
 def test_coupled_md_graph_runs_and_keeps_temperature():
