@@ -68,11 +68,15 @@ class RespaMD:
             self.transfer = torch.zeros((nd, 6, 3, 3), dtype=torch.float32, device=self.device)
         self.plan = None
         self.block_timings = None
+        self._packed = packed
+        self.block_beads = None
+        self.perm = None  # memory order -> input order, after sort_particles()
         if fused and self.topo is not None and packed is not None:
             if max_block_beads == "auto":
                 self.plan = self._tune_plan(packed)
             else:
                 self.plan = self._make_plan(packed, max_block_beads)
+                self.block_beads = int(max_block_beads)
         self.graph = None
         self.graph_inner = self.graph_field = None
         self.field_sums = torch.zeros(8, dtype=torch.float64, device=self.device)
@@ -160,12 +164,62 @@ class RespaMD:
             if best is None or t < best[0]:
                 if best is not None:
                     _lib.lib().hpf_respa_plan_destroy(best[1])
-                best = (t, plan)
+                best = (t, plan, c)
             else:
                 _lib.lib().hpf_respa_plan_destroy(plan)
         self.err.zero_()
         self.block_timings = timings
-        return None if best is None else best[1]
+        if best is None:
+            return None
+        self.block_beads = best[2]
+        return best[1]
+
+    # per-bead arrays that sort_particles() permutes together
+    _PER_BEAD = ("r", "v", "types", "charges", "f_field", "f_elec", "f_b", "f_bond", "f_angle",
+                 "f_dih", "group")
+
+    def sort_particles(self):
+        """Reorder the beads in memory by the mesh cell of their current
+        position (x-major cell index, stable), so that neighbouring threads of
+        the paint and readout touch neighbouring mesh points.  Every per-bead
+        array is permuted in place and the bonded topology and the fused plan
+        are rebuilt with the new indices; the physics is unchanged.  `perm`
+        maps memory order to the caller's order (`in_input_order`).  Call
+        before capture() (a captured graph holds the old plan)."""
+        if self.graph is not None or self.graph_inner is not None:
+            raise RuntimeError("sort_particles() must come before capture()")
+        n0, n1, n2 = self.pm.Nmesh
+        nn = torch.tensor([n0, n1, n2], dtype=torch.float64, device=self.device)
+        c = torch.floor(self.r.double() / self.box * nn).long()
+        c = torch.remainder(c, nn.long())
+        key = (c[:, 0] * n1 + c[:, 1]) * n2 + c[:, 2]
+        perm = torch.argsort(key, stable=True)
+        for name in self._PER_BEAD:
+            t = getattr(self, name, None)
+            if t is not None:
+                t.copy_(t[perm])
+        if self._packed is not None:
+            inv = torch.empty_like(perm)
+            inv[perm] = torch.arange(self.n, device=self.device)
+            inv = inv.cpu().numpy()
+            packed = list(self._packed)
+            for k in (0, 1, 4, 5, 6, 9, 10, 11, 12):  # bead index arrays
+                packed[k] = inv[np.asarray(packed[k], dtype=np.int64)].astype(np.int32)
+            self._packed = tuple(packed)
+            self.topo = BondedTopology(self._packed, device=self.device)
+            if self.plan is not None:
+                _lib.lib().hpf_respa_plan_destroy(self.plan)
+                self.plan = self._make_plan(self._packed, self.block_beads)
+        self.perm = perm if self.perm is None else self.perm[perm]
+        return self.perm
+
+    def in_input_order(self, t):
+        """A per-bead tensor (in memory order) returned in the caller's order."""
+        if self.perm is None:
+            return t
+        out = torch.empty_like(t)
+        out[self.perm] = t
+        return out
 
     def couple(self, thermostat=True, barostat=None, seed=0, n_steps=100000, groups=None,
                remove_com=True, target_pressure=1.0, beta=7.6e-4):
@@ -188,6 +242,8 @@ class RespaMD:
         counts = [float(self.n), 0.0]
         if groups is not None:
             g = np.asarray(groups, np.int32)
+            if self.perm is not None:  # groups come in the caller's order
+                g = g[self.perm.cpu().numpy()]
             ng = int(g.max()) + 1
             if ng > 2:
                 raise NotImplementedError("at most two thermostat coupling groups")

@@ -23,13 +23,16 @@ from .md import RespaMD
 
 
 class ReplicaBatch:
-    def __init__(self, systems, device="cuda", thermostat=True, seed=0, n_steps=100000):
+    def __init__(self, systems, device="cuda", thermostat=True, seed=0, n_steps=100000,
+                 sort=True):
         self.device = torch.device(device)
         self.replicas = []
         for i, s in enumerate(systems):
             cfg = s["config"]
             md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, get_hamiltonian(cfg),
                          topology=s.get("topology"), charges=s.get("charges"), device=self.device)
+            if sort:
+                md.sort_particles()
             md.couple(thermostat=thermostat, barostat=None, seed=seed + i, n_steps=n_steps)
             self.replicas.append(md)
         self.n_beads = [md.n for md in self.replicas]

@@ -157,3 +157,31 @@ def test_plan_forces_match_per_term_kernels_and_are_reproducible():
     for k, ws in ((0, md.ws_bond), (4, md.ws_angle), (8, md.ws_dih)):
         assert e[k] == pytest.approx(float(ws[0].item()), rel=1e-5)
     md.check_errors()
+
+
+@pytest.mark.parametrize("thermostat", [False, True])
+def test_sorted_bead_order_gives_the_same_trajectory(thermostat):
+    """sort_particles() only changes the memory order: a sorted run, read back
+    in the caller's order, follows the unsorted run (bit for bit without the
+    thermostat, whose sums then run in another order; to FP32 rounding with
+    it)."""
+    from hymd_gb300.md import RespaMD
+    s, cfg, ham, fun = _melt()
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    perm = b.sort_particles()
+    assert not torch.equal(perm, torch.arange(len(perm), device=perm.device))
+    for m in (a, b):
+        if thermostat:
+            m.couple(thermostat=True, seed=4, n_steps=20)
+        m.prime()
+        m.run(3)
+    torch.cuda.synchronize()
+    rb, vb = b.in_input_order(b.r), b.in_input_order(b.v)
+    if thermostat:
+        assert rel_rms(rb.cpu().numpy(), a.r.cpu().numpy()) < 1e-6
+        assert rel_rms(vb.cpu().numpy(), a.v.cpu().numpy()) < 1e-5
+    else:
+        assert torch.equal(rb, a.r) and torch.equal(vb, a.v)
+    a.check_errors()
+    b.check_errors()
