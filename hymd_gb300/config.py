@@ -46,6 +46,13 @@ class Config:
     cancel_com_momentum: Union[int, bool] = False
     coulombtype: Optional[str] = None
     dielectric_const: Optional[float] = None
+    # PIC_Spectral_GPE (hymd/input_parser.py:194-198): per-type relative
+    # dielectric values indexed by type id (as sort_dielectric_by_type_id
+    # leaves them), convergence measure, polarisation mixing, tolerance
+    dielectric_type: list = field(default_factory=list)
+    convergence_type: Optional[str] = None
+    pol_mixing: Optional[float] = None
+    conv_crit: Optional[float] = None
     self_energy: Optional[float] = None
     type_charges: Union[List[float], np.ndarray, None] = None
     rho0: Optional[float] = None

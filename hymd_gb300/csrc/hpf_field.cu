@@ -896,6 +896,10 @@ int hpf_ctx_destroy(hpf_ctx* c) {
     if (c->has_d2z) cufftDestroy(c->plan_d2z);
     cudaFree(c->d_grid64);
     cudaFree(c->d_spec64);
+    cudaFree(c->gpe_grid);
+    cudaFree(c->gpe_spec);
+    cudaFree(c->gpe_ws);
+    cudaFreeHost(c->gpe_host);
     free(c);
     return HPF_OK;
 }
@@ -1378,5 +1382,317 @@ extern "C" int hpf_field_adjoint(hpf_ctx* c, const float* pos, const int32_t* ty
 #undef HPF_KA
         HPF_LAUNCH_CHECK();
     }
+    return HPF_OK;
+}
+
+// ------------------------------------------------------ PIC_Spectral_GPE ---
+// Electrostatics with a density-weighted dielectric (hymd/field.py:764-1112):
+// eps(r) = sum_t eps_t phi~_t / sum_t phi~_t, the generalised Poisson
+// equation div(eps grad psi) = -rho~ solved by the reference's polarisation
+// iteration, then forces from V_t = q_t psi - (eps_t - eps) |E|^2 / (2 eps0^-1
+// sum phi~).  All transforms and products follow the reference's sequence;
+// its masked divisions (np.divide(..., where=...)) keep the previous values
+// where the mask is false, so phi_eps, the polarisation and |E|^2 / sum phi~
+// live in caller-owned grids across calls.
+namespace {
+
+enum { kGpeQ = 0, kGpeTot = 1, kGpeEta = 2, kGpeX = 5, kGpeE = 6, kGpePsi = 9, kGpeGrids = 10 };
+
+// spec *= H(k) / M (filter under the unnormalised r2c)
+__global__ void k_gpe_filter(float2* __restrict__ spec, int64_t Mc, KGeom g,
+                             const BoxState* __restrict__ bs, const Functional* __restrict__ fun) {
+    const float s2h = fun->sigma2_half;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        float kx, ky, kz, gx, gy, gz, wk;
+        mode_k(idx, g, bs, kx, ky, kz, gx, gy, gz, wk);
+        const float s = expf(-s2h * (kx * kx + ky * ky + kz * kz)) * g.invM;
+        const float2 v = spec[idx];
+        spec[idx] = make_float2(v.x * s, v.y * s);
+    }
+}
+
+// total density, dielectric (kept where the total is <= 1e-6), q = rho~/eps
+// (rho~ kept where eps <= 1e-6) and the first iteration's X = q + pol_prev
+__global__ void k_gpe_eps(const float* __restrict__ phi, int T, int64_t M, TypeScale eps_t,
+                          float* __restrict__ rho_q, float* __restrict__ tot,
+                          float* __restrict__ phi_eps, const float* __restrict__ pol_prev,
+                          float* __restrict__ X) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        float ts = 0.0f, num = 0.0f;
+        for (int t = 0; t < T; ++t) {
+            const float p = phi[(int64_t)t * M + e];
+            ts = ts + p;
+            num = num + eps_t.s[t] * p;
+        }
+        float pe = phi_eps[e];
+        if (ts > 1e-6f) {
+            pe = num / ts;
+            phi_eps[e] = pe;
+        }
+        tot[e] = ts;
+        const float r = rho_q[e];
+        const float q = pe > 1e-6f ? r / pe : r;
+        rho_q[e] = q;
+        X[e] = q + pol_prev[e];
+    }
+}
+
+// out[d] = sign * i k'_d in / M (k' the gradient wavevector)
+__global__ void k_gpe_grad_spec(const float2* __restrict__ in, float2* __restrict__ out,
+                                int64_t Mc, KGeom g, const BoxState* __restrict__ bs,
+                                float sign) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        float kx, ky, kz, gx, gy, gz, wk;
+        mode_k(idx, g, bs, kx, ky, kz, gx, gy, gz, wk);
+        const float2 v = in[idx];
+        const float gk[3] = {gx, gy, gz};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float k = sign * gk[d] * g.invM;
+            out[(int64_t)d * Mc + idx] = make_float2(-k * v.y, k * v.x);
+        }
+    }
+}
+
+// v = scale in / (M knorm); psi_k = v (when given); out[d] = -i k'_d v
+__global__ void k_gpe_field_spec(const float2* __restrict__ in, float2* __restrict__ out,
+                                 float2* __restrict__ psi_k, int64_t Mc, KGeom g,
+                                 const BoxState* __restrict__ bs, float scale) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        float kx, ky, kz, gx, gy, gz, wk;
+        mode_k(idx, g, bs, kx, ky, kz, gx, gy, gz, wk);
+        const float k2 = kx * kx + ky * ky + kz * kz;
+        const float s = scale * g.invM / (idx == 0 ? 1.0f : k2);
+        const float2 v = make_float2(in[idx].x * s, in[idx].y * s);
+        if (psi_k) psi_k[idx] = v;
+        const float gk[3] = {gx, gy, gz};
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            out[(int64_t)d * Mc + idx] = make_float2(gk[d] * v.y, -gk[d] * v.x);
+    }
+}
+
+__global__ void k_gpe_eta_div(float* __restrict__ eta, const float* __restrict__ phi_eps,
+                              int64_t M) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const float pe = phi_eps[e];
+        if (pe > 1e-6f)
+            for (int d = 0; d < 3; ++d) eta[(int64_t)d * M + e] /= pe;
+    }
+}
+
+// one polarisation update: pol = w (-eta.E) + (1 - w) pol_prev, the
+// convergence measure of |pol - pol_prev| (KIND 0 max, 1 sum, 2 sum of
+// squares), pol_prev = pol, X = q + pol
+template <int KIND>
+__global__ void k_gpe_pol(const float* __restrict__ eta, const float* __restrict__ E,
+                          const float* __restrict__ q, float* __restrict__ pol,
+                          float* __restrict__ X, int64_t M, float w,
+                          unsigned int* __restrict__ max_bits, double* ws) {
+    float loc = 0.0f;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const float p0 = -(eta[e] * E[e] + eta[M + e] * E[M + e] + eta[2 * M + e] * E[2 * M + e]);
+        const float pp = pol[e];
+        const float p = w * p0 + (1.0f - w) * pp;
+        const float d = fabsf(p - pp);
+        if (KIND == 0) loc = fmaxf(loc, d);
+        else if (KIND == 1) loc += d;
+        else loc = fmaf(d, d, loc);
+        pol[e] = p;
+        X[e] = q[e] + p;
+    }
+    if (KIND == 0) {
+        // max is order-independent: atomics on the bit pattern of non-negative floats
+        for (int o = 16; o > 0; o >>= 1) loc = fmaxf(loc, __shfl_down_sync(0xffffffffu, loc, o));
+        if ((threadIdx.x & 31) == 0) atomicMax(max_bits, __float_as_uint(loc));
+    } else {
+        float acc[1] = {loc};
+        grid_reduce_store_f<1>(acc, ws_partials(ws), ws_ticket(ws), ws);
+    }
+}
+
+// |E|^2, the kept |E|^2 / sum phi~, the external potentials V_t and the
+// energy sum of phi_eps |E|^2 (energy = scale * sum)
+__global__ void k_gpe_vbar(const float* __restrict__ E, const float* __restrict__ psi,
+                           const float* __restrict__ tot, const float* __restrict__ phi_eps,
+                           float* __restrict__ contrib, int T, int64_t M, TypeScale eps_t,
+                           TypeScale q_t, float half_e0, float* __restrict__ vbar,
+                           float* __restrict__ dot_out, double* ws, double* energy,
+                           const BoxState* __restrict__ bs, double half_e0_d) {
+    float acc[1] = {0.0f};
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const float d = E[e] * E[e] + E[M + e] * E[M + e] + E[2 * M + e] * E[2 * M + e];
+        if (tot[e] > 1e-6f) contrib[e] = d / tot[e];
+        const float c = contrib[e], pe = phi_eps[e], ps = psi[e];
+        for (int t = 0; t < T; ++t)
+            vbar[(int64_t)t * M + e] = q_t.s[t] * ps - half_e0 * (eps_t.s[t] - pe) * c;
+        if (dot_out) dot_out[e] = d;
+        acc[0] = fmaf(pe, d, acc[0]);
+    }
+    if (grid_reduce_store_f<1>(acc, ws_partials(ws), ws_ticket(ws), ws) && energy)
+        *energy = bs->dV * half_e0_d * ws[0];  // the current (device) box
+}
+
+// F_t,d(k) = -i k'_d H(k) V_t(k) / M
+__global__ void k_gpe_force_spec(const float2* __restrict__ vk, float2* __restrict__ out, int T,
+                                 int64_t Mc, KGeom g, const BoxState* __restrict__ bs,
+                                 const Functional* __restrict__ fun) {
+    const float s2h = fun->sigma2_half;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        float kx, ky, kz, gx, gy, gz, wk;
+        mode_k(idx, g, bs, kx, ky, kz, gx, gy, gz, wk);
+        const float s = expf(-s2h * (kx * kx + ky * ky + kz * kz)) * g.invM;
+        const float gk[3] = {gx, gy, gz};
+        for (int t = 0; t < T; ++t) {
+            const float2 v = vk[(int64_t)t * Mc + idx];
+            const float2 h = make_float2(v.x * s, v.y * s);
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                out[(int64_t)(3 * t + d) * Mc + idx] = make_float2(gk[d] * h.y, -gk[d] * h.x);
+        }
+    }
+}
+
+int gpe_scratch(hpf_ctx* c) {
+    if (c->gpe_grid) return HPF_OK;
+    HPF_CUDA_TRY(cudaMalloc(&c->gpe_grid, sizeof(float) * (size_t)kGpeGrids * c->M));
+    HPF_CUDA_TRY(cudaMalloc(&c->gpe_spec, sizeof(float2) * (size_t)4 * c->Mc));
+    HPF_CUDA_TRY(cudaMalloc(&c->gpe_ws, sizeof(double) * HPF_OUT_DOUBLES));
+    HPF_CUDA_TRY(cudaMemset(c->gpe_ws, 0, sizeof(double) * HPF_OUT_DOUBLES));
+    HPF_CUDA_TRY(cudaMallocHost(&c->gpe_host, sizeof(double) * 2));
+    return HPF_OK;
+}
+
+}  // namespace
+
+extern "C" int hpf_gpe_step(hpf_ctx* c, const float* pos, const int32_t* types,
+                            const float* charges, int64_t n, const float* phi_tilde,
+                            const double* eps_type, const double* type_charges,
+                            double coulomb_constant, double conv_crit, double mixing,
+                            int conv_kind, int max_iter, float* phi_eps, float* pol_prev,
+                            float* contrib, float* elec_forces, float* psi_out,
+                            float* elec_field_out, float* elec_dot_out, float* vbar_out,
+                            double* energy_out, int* iterations, void* stream) {
+    if (!c || n < 0 || (n > 0 && (!pos || !types || !charges || !elec_forces)) || !phi_tilde ||
+        !eps_type || !type_charges || !phi_eps || !pol_prev || !contrib || conv_kind < 0 ||
+        conv_kind > 2 || max_iter < 0 || !(coulomb_constant > 0))
+        return HPF_ERR_ARG;
+    int r = gpe_scratch(c);
+    if (r != HPF_OK) return r;
+    cudaStream_t st = as_stream(stream);
+    const int T = c->T;
+    const int64_t M = c->M, Mc = c->Mc;
+    float* G = c->gpe_grid;
+    float2* S = c->gpe_spec;  // [0] scalar spectrum, [1..3] vector spectra
+    const KGeom g = kgeom(c);
+    const int gm = grid_for(M, kThreads), gk = grid_for(Mc, kThreads);
+    TypeScale eps_t, q_t, one;
+    for (int t = 0; t < T; ++t) {
+        eps_t.s[t] = (float)eps_type[t];
+        q_t.s[t] = (float)type_charges[t];
+    }
+    one.s[0] = 1.0f;
+    // filtered charge density rho~ = c2r(H r2c(q / dV))
+    if ((r = do_paint(c, pos, nullptr, charges, n, 1, one, G + kGpeQ * M, st)) != HPF_OK) return r;
+    if ((r = exec_r2c(c, G + kGpeQ * M, S, 1, st)) != HPF_OK) return r;
+    k_gpe_filter<<<gk, kThreads, 0, st>>>(S, Mc, g, c->d_box, c->d_fun);
+    HPF_LAUNCH_CHECK();
+    if ((r = exec_c2r(c, S, G + kGpeQ * M, 1, st)) != HPF_OK) return r;
+    // dielectric, q = rho~/eps, X = q + pol_prev
+    k_gpe_eps<<<gm, kThreads, 0, st>>>(phi_tilde, T, M, eps_t, G + kGpeQ * M, G + kGpeTot * M,
+                                       phi_eps, pol_prev, G + kGpeX * M);
+    HPF_LAUNCH_CHECK();
+    // eta_d = (i k_d eps)(r) / eps
+    if ((r = exec_r2c(c, phi_eps, S, 1, st)) != HPF_OK) return r;
+    k_gpe_grad_spec<<<gk, kThreads, 0, st>>>(S, S + Mc, Mc, g, c->d_box, 1.0f);
+    HPF_LAUNCH_CHECK();
+    for (int d = 0; d < 3; ++d)
+        if ((r = exec_c2r(c, S + (1 + d) * Mc, G + (kGpeEta + d) * M, 1, st)) != HPF_OK) return r;
+    k_gpe_eta_div<<<gm, kThreads, 0, st>>>(G + kGpeEta * M, phi_eps, M);
+    HPF_LAUNCH_CHECK();
+    // polarisation iteration (host-driven: the reference tests convergence
+    // after every update, so each iteration ends with a 4-byte read-back)
+    unsigned int* max_bits = reinterpret_cast<unsigned int*>(c->gpe_ws + 8 + 8 * HPF_REDUCE_BLOCKS + 2);
+    int it = 0;
+    double delta = 1.0;
+    const int rg = reduce_grid(M, kThreads);
+    while (it < max_iter && delta > conv_crit) {
+        if ((r = exec_r2c(c, G + kGpeX * M, S, 1, st)) != HPF_OK) return r;
+        k_gpe_field_spec<<<gk, kThreads, 0, st>>>(S, S + Mc, nullptr, Mc, g, c->d_box, 1.0f);
+        HPF_LAUNCH_CHECK();
+        for (int d = 0; d < 3; ++d)
+            if ((r = exec_c2r(c, S + (1 + d) * Mc, G + (kGpeE + d) * M, 1, st)) != HPF_OK) return r;
+        if (conv_kind == 0) {
+            HPF_CUDA_TRY(cudaMemsetAsync(max_bits, 0, sizeof(unsigned int), st));
+            k_gpe_pol<0><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M, G + kGpeQ * M,
+                                                  pol_prev, G + kGpeX * M, M, (float)mixing,
+                                                  max_bits, c->gpe_ws);
+            HPF_LAUNCH_CHECK();
+            HPF_CUDA_TRY(cudaMemcpyAsync(c->gpe_host, max_bits, sizeof(unsigned int),
+                                         cudaMemcpyDeviceToHost, st));
+        } else {
+            if (conv_kind == 1)
+                k_gpe_pol<1><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M,
+                                                      G + kGpeQ * M, pol_prev, G + kGpeX * M, M,
+                                                      (float)mixing, max_bits, c->gpe_ws);
+            else
+                k_gpe_pol<2><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M,
+                                                      G + kGpeQ * M, pol_prev, G + kGpeX * M, M,
+                                                      (float)mixing, max_bits, c->gpe_ws);
+            HPF_LAUNCH_CHECK();
+            HPF_CUDA_TRY(cudaMemcpyAsync(c->gpe_host, c->gpe_ws, sizeof(double),
+                                         cudaMemcpyDeviceToHost, st));
+        }
+        HPF_CUDA_TRY(cudaStreamSynchronize(st));
+        if (conv_kind == 0) {
+            unsigned int b;
+            memcpy(&b, c->gpe_host, sizeof(b));
+            float f;
+            memcpy(&f, &b, sizeof(f));
+            delta = (double)f;
+        } else {
+            delta = c->gpe_host[0];
+        }
+        ++it;
+    }
+    if (iterations) *iterations = it;
+    // psi = c2r(eps0^-1 r2c(q + pol) / k^2), E = c2r(-i k psi_k)
+    const double e0inv = coulomb_constant * 4.0 * 3.14159265358979323846;
+    if ((r = exec_r2c(c, G + kGpeX * M, S, 1, st)) != HPF_OK) return r;
+    k_gpe_field_spec<<<gk, kThreads, 0, st>>>(S, S + Mc, S, Mc, g, c->d_box, (float)e0inv);
+    HPF_LAUNCH_CHECK();
+    for (int d = 0; d < 3; ++d)
+        if ((r = exec_c2r(c, S + (1 + d) * Mc, G + (kGpeE + d) * M, 1, st)) != HPF_OK) return r;
+    if ((r = exec_c2r(c, S, G + kGpePsi * M, 1, st)) != HPF_OK) return r;
+    // |E|^2, contributions, V_t (into the context's real scratch), energy
+    k_gpe_vbar<<<rg, kThreads, 0, st>>>(G + kGpeE * M, G + kGpePsi * M, G + kGpeTot * M, phi_eps,
+                                        contrib, T, M, eps_t, q_t, (float)(0.5 / e0inv), c->d_grid,
+                                        elec_dot_out, c->gpe_ws, energy_out, c->d_box,
+                                        0.5 / e0inv);
+    HPF_LAUNCH_CHECK();
+    if (psi_out)
+        HPF_CUDA_TRY(cudaMemcpyAsync(psi_out, G + kGpePsi * M, sizeof(float) * M,
+                                     cudaMemcpyDeviceToDevice, st));
+    if (elec_field_out)
+        HPF_CUDA_TRY(cudaMemcpyAsync(elec_field_out, G + kGpeE * M, sizeof(float) * 3 * M,
+                                     cudaMemcpyDeviceToDevice, st));
+    if (vbar_out)
+        HPF_CUDA_TRY(cudaMemcpyAsync(vbar_out, c->d_grid, sizeof(float) * T * M,
+                                     cudaMemcpyDeviceToDevice, st));
+    // forces: -grad (H * V_t) read out per type
+    if ((r = exec_r2c(c, c->d_grid, c->d_spec_phi, T, st)) != HPF_OK) return r;
+    k_gpe_force_spec<<<gk, kThreads, 0, st>>>(c->d_spec_phi, c->d_spec, T, Mc, g, c->d_box,
+                                              c->d_fun);
+    HPF_LAUNCH_CHECK();
+    if ((r = exec_c2r(c, c->d_spec, c->d_grid, 3 * T, st)) != HPF_OK) return r;
+    if (n > 0) return launch_readout(c, c->d_grid, pos, types, nullptr, n, T, elec_forces, nullptr, st);
     return HPF_OK;
 }

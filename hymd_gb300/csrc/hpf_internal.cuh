@@ -63,6 +63,13 @@ struct hpf_ctx {
     cufftHandle plan_c2r[3 * HPF_MAX_TYPES + 2];
     bool has_r2c[HPF_MAX_TYPES + 1];
     bool has_c2r[3 * HPF_MAX_TYPES + 2];
+    // PIC_Spectral_GPE scratch (created on first use): grids rho~ / q, total
+    // density, eta[3], X, E[3], psi (10 M floats); spectra (4 Mc); a
+    // reduction workspace and a pinned host word for the convergence test
+    float* gpe_grid;
+    float2* gpe_spec;
+    double* gpe_ws;
+    double* gpe_host;
 };
 
 #define HPF_REDUCE_GRID 304  // blocks of a reduction kernel (2 per SM on 152 SMs)

@@ -189,7 +189,21 @@ def initialize_pm(pmesh, config, comm=None):
         eff_all = pm.complex_field(3)
         coulomb_list = [[eff_all[d] for d in range(3)], pm.complex_field()]
     elif config.coulombtype == "PIC_Spectral_GPE":
-        raise NotImplementedError("PIC_Spectral_GPE has no GPU implementation")
+        # the 12 grids of the reference's GPE list (hymd/field.py:81-131), in
+        # its order; phi_eps / phi_pol_prev / elec_field_contrib persist
+        eta_all = pm.real_field(3)
+        etaf_all = pm.complex_field(3)
+        vbar_all = pm.real_field(T)
+        vbarf_all = pm.complex_field(T)
+        fme_all = pm.real_field(T, 3)
+        fmef_all = pm.complex_field(T, 3)
+        coulomb_list = [pm.real_field(), pm.complex_field(), [eta_all[d] for d in range(3)],
+                        [etaf_all[d] for d in range(3)], pm.real_field(), pm.real_field(),
+                        pm.real_field(), pm.real_field(), [vbar_all[t] for t in range(T)],
+                        [vbarf_all[t] for t in range(T)],
+                        [[fme_all[t, d] for d in range(3)] for t in range(T)],
+                        [[fmef_all[t, d] for d in range(3)] for t in range(T)]]
+        pm.gpe = dict(vbar=vbar_all, elec_field=ef_all)
     field_list = [phi, phi_fourier, force_on_grid, v_ext_fourier, v_ext, phi_transfer,
                   phi_laplacian]
     _REGISTRY[phi_all.data_ptr()] = pm
@@ -362,6 +376,66 @@ def update_field_force_q(charges, phi_q, phi_q_fourier, psi, psi_fourier, elec_f
               _lib.ptr(psi_fourier), _lib.ptr(pm.pic_sums), None, _lib.stream_ptr())
     # the charges of this evaluation, for the FP64 energy / pressure
     pm.pic_charges = q
+
+
+_CONV_KINDS = {None: 0, "max_diff": 0, "csum": 1, "euclidean_norm": 2}
+
+
+def update_field_force_q_GPE(conv_fun, phi, types, charges, phi_q, phi_q_fourier, phi_eps,
+                             phi_eps_fourier, phi_eta, phi_eta_fourier, phi_pol_prev, phi_pol,
+                             elec_field, elec_forces, elec_field_contrib, psi, Vbar_elec,
+                             Vbar_elec_fourier, force_mesh_elec, force_mesh_elec_fourier,
+                             hamiltonian, layout_q, layouts, pm, positions, config, comm=None):
+    """hymd/field.py:764-1112 (PIC_Spectral_GPE) -> (Vbar_elec, phi_eps, elec_dot).
+
+    `conv_fun` is the reference's convergence closure; the measure it stands
+    for is taken from config.convergence_type (max_diff when unset, as
+    hymd/main.py:141-165 does).  phi_eps, phi_pol_prev and elec_field_contrib
+    keep their contents between calls, as in the reference; elec_forces is
+    written in place.  psi, elec_field and Vbar_elec are filled; the Fourier
+    grids of the argument list are scratch in the reference and not written.
+    Synchronises once per iteration (the convergence test)."""
+    T = pm.n_types
+    pos = _lib.require_cuda(positions, "positions", torch.float32)
+    n = pos.shape[0]
+    typ = _types32(types, n)
+    q = _lib.require_cuda(charges, "charges", torch.float32, (n,))
+    phi_all = _stack_base(phi, (T,), torch.float32, "phi")
+    pm.set_functional(hamiltonian)
+    kind = _CONV_KINDS.get(getattr(config, "convergence_type", None))
+    if kind is None:
+        raise ValueError(f"unknown convergence_type {config.convergence_type!r}")
+    eps = [float(x) for x in config.dielectric_type]
+    qt = [float(x) for x in (config.type_charges or [0.0] * T)]
+    ef = pm.gpe["elec_field"] if hasattr(pm, "gpe") else pm.real_field(3)
+    vb = pm.gpe["vbar"] if hasattr(pm, "gpe") else pm.real_field(T)
+    dot = pm.real_field()
+    it = _lib.ctypes.c_int(0)
+    _lib.call("hpf_gpe_step", pm._h, _lib.ptr(pos), _lib.ptr(typ), _lib.ptr(q), n,
+              _lib.ptr(phi_all), _lib.dvec(eps), _lib.dvec(qt), float(config.coulomb_constant),
+              float(config.conv_crit if config.conv_crit is not None else 1e-6),
+              float(config.pol_mixing if config.pol_mixing is not None else 0.6), kind, 100,
+              _lib.ptr(phi_eps), _lib.ptr(phi_pol_prev), _lib.ptr(elec_field_contrib),
+              _lib.ptr(elec_forces), _lib.ptr(psi), _lib.ptr(ef), _lib.ptr(dot), _lib.ptr(vb),
+              None, _lib.ctypes.byref(it), _lib.stream_ptr())
+    for d in range(3):
+        if elec_field[d].data_ptr() != ef[d].data_ptr():
+            elec_field[d].copy_(ef[d])
+    for t in range(T):
+        if Vbar_elec[t].data_ptr() != vb[t].data_ptr():
+            Vbar_elec[t].copy_(vb[t])
+    phi_pol.copy_(phi_pol_prev)
+    pm.gpe_iterations = it.value
+    return Vbar_elec, phi_eps, dot
+
+
+def compute_field_energy_q_GPE(config, phi_eps, field_q_energy, dot_elec, comm=None):
+    """hymd/field.py:706-761: dV eps0/2 sum(phi_eps |E|^2), in FP64."""
+    V = float(np.prod(np.asarray(config.box_size, dtype=np.float64)))
+    n = np.asarray(config.mesh_size).reshape(-1)
+    cells = float(np.prod(np.full(3, n[0]) if n.size == 1 else n))
+    eps_0 = 1.0 / (config.coulomb_constant * 4 * np.pi)
+    return V / cells * (0.5 * eps_0) * float((phi_eps.double() * dot_elec.double()).sum())
 
 
 def comp_laplacian(phi_fourier, phi_transfer, phi_laplacian, hamiltonian, config):

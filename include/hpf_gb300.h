@@ -186,6 +186,31 @@ int hpf_energy_fp64(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_
                     const double* type_mass, const float* charges, const double* type_charges,
                     double elec_factor, double* out, void* stream);
 
+/* ---- PIC_Spectral_GPE electrostatics ------------------------------------
+ * update_field_force_q_GPE (hymd/field.py:764-1112) and the energy of
+ * compute_field_energy_q_GPE (:706-761): dielectric
+ * eps = sum_t eps_t phi~_t / sum_t phi~_t from the filtered densities
+ * phi_tilde (device float[T][M], what update_field leaves in phi), the
+ * generalised Poisson equation solved by the reference's polarisation
+ * iteration (mixing, conv_crit, max_iter; conv_kind 0 max_diff, 1 csum,
+ * 2 euclidean_norm as the mesh library's cnorm, a sum of squares),
+ * psi = eps0^-1 (q + pol) / k^2 with q = rho~/eps, E = -grad psi,
+ * V_t = q_t psi - (eps_t - eps) |E|^2 / (2 eps0^-1 sum phi~) and the forces
+ * -grad(H * V_t) read out per type into elec_forces (device float[n][3]).
+ * phi_eps, pol_prev and contrib (device float[M]) carry the reference's
+ * persistent grids between calls (its masked divisions keep old values;
+ * zero them before the first call).  Optional outputs (NULL to skip): psi,
+ * elec_field (float[3][M]), elec_dot (|E|^2, float[M]), vbar (float[T][M]),
+ * energy (device double: dV eps0/2 sum eps |E|^2).  The convergence test
+ * after each update reads 4-8 bytes back, so this call synchronises the
+ * stream once per iteration; *iterations receives their number. */
+int hpf_gpe_step(hpf_ctx* ctx, const float* pos, const int32_t* types, const float* charges,
+                 int64_t n, const float* phi_tilde, const double* eps_type,
+                 const double* type_charges, double coulomb_constant, double conv_crit,
+                 double mixing, int conv_kind, int max_iter, float* phi_eps, float* pol_prev,
+                 float* contrib, float* elec_forces, float* psi, float* elec_field,
+                 float* elec_dot, float* vbar, double* energy, int* iterations, void* stream);
+
 /* ---- adjoint of the field energy ------------------------------------------
  * Gradients of W = sum_g w(phi~(g)) dV (hymd/field.py:688-703 with the
  * functional set by hpf_ctx_set_functional), for fitting the functional's

@@ -7,6 +7,8 @@ space:
   compute_field_and_kinetic_energy  hymd/field.py:619-703
   compute_self_energy_q       hymd/field.py:203-238
   update_field_force_q        hymd/field.py:241-403 (PIC_Spectral)
+  update_field_force_q_GPE    hymd/field.py:764-1112 (PIC_Spectral_GPE, with the
+                              energy of compute_field_energy_q_GPE :706-761)
   comp_laplacian              hymd/field.py:406-425
   comp_pressure               hymd/pressure.py:9-179
 
@@ -282,3 +284,84 @@ def gaussian_core_energy(r, kappa, sigma, rho0, names=None, chi=None, a_shift=Tr
                     E += 2 * kappa * chi[tuple(sorted((names[i], names[j])))] / c * np.exp(
                         -np.dot(d, d) / (4.0 * sigma ** 2))
     return E
+
+
+def _conv(diff, kind):
+    """Convergence measures of hymd/main.py:141-165 over the mesh: max_diff
+    (the default), csum (sum), euclidean_norm (pmesh cnorm: sum of squares)."""
+    if kind == "csum":
+        return float(np.sum(diff))
+    if kind == "euclidean_norm":
+        return float(np.sum(diff * diff))
+    return float(np.max(diff))
+
+
+def gpe_step(phi_tilde, charges, positions, types, n_types, mesh, box, sigma, eps_type,
+             type_charges, state, conv_crit=1e-6, mixing=0.6, conv_kind="max_diff",
+             max_iter=100, coulomb_constant=COULOMB_CONSTANT):
+    """PIC_Spectral_GPE electrostatics (hymd/field.py:764-1112) and its energy
+    (:706-761) in FP64.
+
+    phi_tilde: list of the filtered type densities (what update_field leaves
+    in phi).  state: dict of the grids the reference keeps between calls --
+    phi_eps, pol_prev, contrib (its masked divisions leave old values where
+    the mask is false) -- updated in place.  Returns dict(forces, psi,
+    elec_field, phi_eps, elec_dot, Vbar, energy, iterations)."""
+    n = _mesh(mesh)
+    box = np.asarray(box, dtype=np.float64)
+    M = n[0] * n[1] * n[2]
+    dV = float(np.prod(box)) / M
+    K2 = k2(n, box)
+    H = filter_H(K2, sigma)
+    kg = kvectors_gradient(n, box)
+    knorm = K2.copy()
+    knorm[0, 0, 0] = 1.0
+    pos = np.asarray(positions, dtype=np.float64)
+    rho = cic_paint(pos, np.asarray(charges, np.float64), n, box) / dV
+    rho_t = c2r(r2c(rho) * H, n)
+    tot = np.zeros(n)
+    num = np.zeros(n)
+    for t in range(n_types):
+        tot += phi_tilde[t]
+        num += eps_type[t] * phi_tilde[t]
+    m_tot = tot > 1e-6
+    phi_eps = state["phi_eps"]
+    phi_eps[m_tot] = num[m_tot] / tot[m_tot]
+    eps_k = r2c(phi_eps)
+    m_eps = phi_eps > 1e-6
+    q = rho_t.copy()
+    q[m_eps] = rho_t[m_eps] / phi_eps[m_eps]
+    eta = []
+    for d in range(3):
+        g = c2r(1j * kg[d] * eps_k, n)
+        g[m_eps] = g[m_eps] / phi_eps[m_eps]
+        eta.append(g)
+    pol_prev = state["pol_prev"].copy()
+    it, delta = 0, 1.0
+    while it < max_iter and delta > conv_crit:
+        X = r2c(q + pol_prev)
+        E = [c2r(X * (-1j * kg[d]) / knorm, n) for d in range(3)]
+        pol = -(eta[0] * E[0] + eta[1] * E[1] + eta[2] * E[2])
+        pol = mixing * pol + (1.0 - mixing) * pol_prev
+        delta = _conv(np.abs(pol - pol_prev), conv_kind)
+        pol_prev = pol.copy()
+        it += 1
+    state["pol_prev"][...] = pol_prev
+    eps0_inv = coulomb_constant * 4.0 * np.pi
+    psik = r2c(eps0_inv * (q + pol_prev)) / knorm
+    psi = c2r(psik, n)
+    E = [c2r(-1j * kg[d] * psik, n) for d in range(3)]
+    dot = E[0] * E[0] + E[1] * E[1] + E[2] * E[2]
+    contrib = state["contrib"]
+    contrib[m_tot] = dot[m_tot] / tot[m_tot]
+    Vbar = [type_charges[t] * psi - (0.5 / eps0_inv) * (eps_type[t] - phi_eps) * contrib
+            for t in range(n_types)]
+    F = np.zeros((len(pos), 3))
+    for t in range(n_types):
+        sel = types == t
+        Vk = r2c(Vbar[t]) * H
+        for d in range(3):
+            F[sel, d] = cic_readout(c2r(-1j * kg[d] * Vk, n), pos[sel], n, box)
+    energy = dV * 0.5 / eps0_inv * float(np.sum(phi_eps * dot))
+    return dict(forces=F, psi=psi, elec_field=E, phi_eps=phi_eps.copy(), elec_dot=dot,
+                Vbar=Vbar, energy=energy, iterations=it)
