@@ -12,6 +12,7 @@
 // shared with the fused rRESPA kernel).  Energies and virials are summed in
 // FP64 by a deterministic grid reduction; forces are accumulated with FP32
 // atomics into the zeroed force array.
+#include "hpf_dual.cuh"
 #include "hpf_internal.cuh"
 #include "hpf_terms.cuh"
 
@@ -160,6 +161,54 @@ int grid_for(int64_t work) {
     return (int)g;
 }
 
+
+// Directional derivative of the bond and angle forces along lambda (the
+// Hessian-vector product of the bonded energy, with a minus sign), summed
+// into out with FP32 atomics.
+__global__ void k_bonds_hvp(float* __restrict__ out, const float* __restrict__ r,
+                            const float* __restrict__ lam, int64_t n,
+                            const double* __restrict__ box, const int32_t* __restrict__ a,
+                            const int32_t* __restrict__ b, const float* __restrict__ r0,
+                            const float* __restrict__ k, int64_t nb, int* err) {
+    const Box bx = load_box(box);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nb;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int ia = a[t], ib = b[t];
+        if (!in_range(ia, n) || !in_range(ib, n)) {
+            hpf_flag(err, HPF_ERR_INDEX);
+            continue;
+        }
+        const V3 dfb = bond_force_tangent(load3(r, ia), load3(r, ib), load3(lam, ia),
+                                          load3(lam, ib), r0[t], k[t], bx);
+        add3(out, ia, -dfb);
+        add3(out, ib, dfb);
+    }
+}
+
+__global__ void k_angles_hvp(float* __restrict__ out, const float* __restrict__ r,
+                             const float* __restrict__ lam, int64_t n,
+                             const double* __restrict__ box, const int32_t* __restrict__ a,
+                             const int32_t* __restrict__ b, const int32_t* __restrict__ c,
+                             const float* __restrict__ t0, const float* __restrict__ k,
+                             int64_t na, int* err) {
+    const Box bx = load_box(box);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < na;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int ia = a[t], ib = b[t], ic = c[t];
+        if (!in_range(ia, n) || !in_range(ib, n) || !in_range(ic, n)) {
+            hpf_flag(err, HPF_ERR_INDEX);
+            continue;
+        }
+        V3 dga, dgc;
+        if (!angle_grad_tangent(load3(r, ia), load3(r, ib), load3(r, ic), load3(lam, ia),
+                                load3(lam, ib), load3(lam, ic), t0[t], k[t], bx, dga, dgc))
+            continue;
+        add3(out, ia, -dga);
+        add3(out, ic, -dgc);
+        add3(out, ib, dga + dgc);
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -219,6 +268,28 @@ int hpf_dipole_redistribute(float* f_on_bead, int64_t n, const float* f_dipoles,
         k_dipole_redistribute<<<grid_for(nd), kThreads, 0, st>>>(f_on_bead, n, f_dipoles,
                                                                  transfer, a, b, c, d, dtype,
                                                                  last, nd);
+        HPF_LAUNCH_CHECK();
+    }
+    return HPF_OK;
+}
+
+int hpf_bonded_hvp(float* out, const float* r, const float* lam, int64_t n, const double* box,
+                   const int32_t* ba, const int32_t* bb, const float* br0, const float* bk,
+                   int64_t nb, const int32_t* aa, const int32_t* ab, const int32_t* ac,
+                   const float* at0, const float* ak, int64_t na, int* d_err, void* stream) {
+    if (!out || !r || !lam || !box || n < 0 || nb < 0 || na < 0 ||
+        (nb > 0 && (!ba || !bb || !br0 || !bk)) || (na > 0 && (!aa || !ab || !ac || !at0 || !ak)))
+        return HPF_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    HPF_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * 3 * (size_t)n, st));
+    if (nb > 0) {
+        k_bonds_hvp<<<grid_for(nb), kThreads, 0, st>>>(out, r, lam, n, box, ba, bb, br0, bk, nb,
+                                                       d_err);
+        HPF_LAUNCH_CHECK();
+    }
+    if (na > 0) {
+        k_angles_hvp<<<grid_for(na), kThreads, 0, st>>>(out, r, lam, n, box, aa, ab, ac, at0, ak,
+                                                        na, d_err);
         HPF_LAUNCH_CHECK();
     }
     return HPF_OK;

@@ -559,7 +559,8 @@ __global__ void k_kspace_pot(const float2* __restrict__ phi_raw, float2* __restr
 __global__ void k_readout_grad(const float* __restrict__ vg, const float* __restrict__ pos,
                                const int32_t* __restrict__ types, int64_t n, int T, int64_t M,
                                const BoxState* __restrict__ bs, TypeScale sc,
-                               float* __restrict__ grad, int* err) {
+                               float* __restrict__ grad, int* err, int accumulate = 0,
+                               int per_volume = 0) {
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
@@ -596,14 +597,20 @@ __global__ void k_readout_grad(const float* __restrict__ vg, const float* __rest
                         gr[2] = fmaf(wx[a] * wy[b] * dz[c], v, gr[2]);
                     }
                 }
-            const float m = sc.s[t];
+            const float m = per_volume ? sc.s[t] * bs->inv_dV : sc.s[t];
             gr[0] *= m;
             gr[1] *= m;
             gr[2] *= m;
         }
-        grad[3 * i] = gr[0];
-        grad[3 * i + 1] = gr[1];
-        grad[3 * i + 2] = gr[2];
+        if (accumulate) {
+            grad[3 * i] += gr[0];
+            grad[3 * i + 1] += gr[1];
+            grad[3 * i + 2] += gr[2];
+        } else {
+            grad[3 * i] = gr[0];
+            grad[3 * i + 1] = gr[1];
+            grad[3 * i + 2] = gr[2];
+        }
     }
 }
 
@@ -1694,5 +1701,222 @@ extern "C" int hpf_gpe_step(hpf_ctx* c, const float* pos, const int32_t* types,
     HPF_LAUNCH_CHECK();
     if ((r = exec_c2r(c, c->d_spec, c->d_grid, 3 * T, st)) != HPF_OK) return r;
     if (n > 0) return launch_readout(c, c->d_grid, pos, types, nullptr, n, T, elec_forces, nullptr, st);
+    return HPF_OK;
+}
+
+// ------------------------------------------------- force vector-Jacobian ---
+// Reverse-mode product of the field force with a cotangent lambda (N x 3):
+// F_i = sum_g W(g - x_i) E_{t_i}(g), E_{t,d} = A_d H^2 (Q phi)_t with A_d the
+// spectral derivative -i k'_d (antisymmetric), phi_j = m_j/dV sum W.  Then
+//   d(lambda.F)/dx_j = sum_g grad W(g - x_j) (lambda_j . E_{t_j}(g))     (local)
+//                    + m_{t_j}/dV sum_g U_{t_j}(g) grad W(g - x_j)      (global)
+// with U_j = sum_{t,d} Q_jt H^2 (+i k'_d) rho_{t,d} and the lambda-weighted
+// paint rho_{t,d}(g) = sum_{i in t} lambda_{i,d} W(g - x_i);
+//   d(lambda.F)/dQ_tj = sum_d <rho_{t,d}, A_d H^2 phi_j>  (Parseval).
+namespace {
+
+__global__ void k_vjp_local(const float* __restrict__ E, const float* __restrict__ pos,
+                            const int32_t* __restrict__ types, const float* __restrict__ lam,
+                            int64_t n, int T, int64_t M, const BoxState* __restrict__ bs,
+                            float* __restrict__ grad, int* err) {
+    const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
+    const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
+    const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
+    const float i0 = h0 + l0, i1 = h1 + l1, i2 = h2 + l2;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        const int t = types[i];
+        float gr[3] = {0.0f, 0.0f, 0.0f};
+        const bool ok = isfinite(x) && isfinite(y) && isfinite(z) && t >= 0 && t < T;
+        if (!ok) hpf_flag(err, (t >= 0 && t < T) ? HPF_ERR_NONFINITE : HPF_ERR_INDEX);
+        if (ok) {
+            int ix, iy, iz;
+            float fx, fy, fz;
+            grid_coord(x, h0, l0, n0, ix, fx);
+            grid_coord(y, h1, l1, n1, iy, fy);
+            grid_coord(z, h2, l2, n2, iz, fz);
+            const int xs[2] = {ix, ix + 1 == n0 ? 0 : ix + 1};
+            const int ys[2] = {iy, iy + 1 == n1 ? 0 : iy + 1};
+            const int zs[2] = {iz, iz + 1 == n2 ? 0 : iz + 1};
+            const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy}, wz[2] = {1.0f - fz, fz};
+            const float dx[2] = {-i0, i0}, dy[2] = {-i1, i1}, dz[2] = {-i2, i2};
+            const float lx = lam[3 * i], ly = lam[3 * i + 1], lz = lam[3 * i + 2];
+            const float* base = E + (int64_t)t * 3 * M;
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    const int64_t row = ((int64_t)xs[a] * n1 + ys[b]) * n2;
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const int64_t o = row + zs[c];
+                        const float v = fmaf(lx, __ldg(base + o),
+                                             fmaf(ly, __ldg(base + M + o), lz * __ldg(base + 2 * M + o)));
+                        gr[0] = fmaf(dx[a] * wy[b] * wz[c], v, gr[0]);
+                        gr[1] = fmaf(wx[a] * dy[b] * wz[c], v, gr[1]);
+                        gr[2] = fmaf(wx[a] * wy[b] * dz[c], v, gr[2]);
+                    }
+                }
+        }
+        grad[3 * i] = gr[0];
+        grad[3 * i + 1] = gr[1];
+        grad[3 * i + 2] = gr[2];
+    }
+}
+
+// rho[d][t][g] += lambda_{i,d} W(g - x_i) (float atomics)
+__global__ void k_paint_lambda(const float* __restrict__ pos, const int32_t* __restrict__ types,
+                               const float* __restrict__ lam, int64_t n, int T, int64_t M,
+                               const BoxState* __restrict__ bs, float* __restrict__ rho) {
+    const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
+    const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
+    const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        const int t = types[i];
+        if (!(isfinite(x) && isfinite(y) && isfinite(z)) || t < 0 || t >= T) continue;
+        int ix, iy, iz;
+        float fx, fy, fz;
+        grid_coord(x, h0, l0, n0, ix, fx);
+        grid_coord(y, h1, l1, n1, iy, fy);
+        grid_coord(z, h2, l2, n2, iz, fz);
+        const int xs[2] = {ix, ix + 1 == n0 ? 0 : ix + 1};
+        const int ys[2] = {iy, iy + 1 == n1 ? 0 : iy + 1};
+        const int zs[2] = {iz, iz + 1 == n2 ? 0 : iz + 1};
+        const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy}, wz[2] = {1.0f - fz, fz};
+        const float l[3] = {lam[3 * i], lam[3 * i + 1], lam[3 * i + 2]};
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                const int64_t row = ((int64_t)xs[a] * n1 + ys[b]) * n2;
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const float w = wx[a] * wy[b] * wz[c];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                        atomicAdd(rho + ((int64_t)d * T + t) * M + row + zs[c], w * l[d]);
+                }
+            }
+    }
+}
+
+// U_j(k) = H^2/M sum_t Q_jt S_t, S_t = sum_d i k'_d rho_{d,t}(k), written over
+// phi_k (read first); dQ_tj += w_k H^2/M Re(conj(S_t) phi_j(k))
+template <int TT>
+__global__ void k_vjp_kspace(const float2* __restrict__ rho_k, float2* phi_k, int64_t Mc,
+                             KGeom g, const BoxState* __restrict__ bs,
+                             const Functional* __restrict__ fun, double* dQ, double* partials,
+                             unsigned int* ticket) {
+    constexpr int K = TT * TT;
+    float acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0f;
+    const float s2h = fun->sigma2_half;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        float kx, ky, kz, gx, gy, gz, wk;
+        mode_k(idx, g, bs, kx, ky, kz, gx, gy, gz, wk);
+        const float H = expf(-s2h * (kx * kx + ky * ky + kz * kz));
+        const float h2m = H * H * g.invM;
+        const float gk[3] = {gx, gy, gz};
+        float2 S[TT], ph[TT];
+#pragma unroll
+        for (int t = 0; t < TT; ++t) {
+            float sx = 0.0f, sy = 0.0f;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float2 r = rho_k[((int64_t)d * TT + t) * Mc + idx];
+                sx = fmaf(-gk[d], r.y, sx);
+                sy = fmaf(gk[d], r.x, sy);
+            }
+            S[t] = make_float2(sx, sy);
+            ph[t] = phi_k[(int64_t)t * Mc + idx];
+        }
+        if (dQ) {
+#pragma unroll
+            for (int t = 0; t < TT; ++t)
+#pragma unroll
+                for (int j = 0; j < TT; ++j)
+                    acc[t * TT + j] =
+                        fmaf(wk * h2m, fmaf(S[t].x, ph[j].x, S[t].y * ph[j].y), acc[t * TT + j]);
+        }
+#pragma unroll
+        for (int j = 0; j < TT; ++j) {
+            float ux = 0.0f, uy = 0.0f;
+#pragma unroll
+            for (int t = 0; t < TT; ++t) {
+                const float q = fun->Q[j * TT + t];
+                ux = fmaf(q, S[t].x, ux);
+                uy = fmaf(q, S[t].y, uy);
+            }
+            phi_k[(int64_t)j * Mc + idx] = make_float2(ux * h2m, uy * h2m);
+        }
+    }
+    if (dQ) grid_reduce_store_f<K>(acc, partials, ticket, dQ);
+}
+
+}  // namespace
+
+extern "C" int hpf_field_force_vjp(hpf_ctx* c, const float* pos, const int32_t* types, int64_t n,
+                                   const double* type_mass, const float* lam, float* grad_pos,
+                                   double* dQ, void* stream) {
+    if (!c || !type_mass || n < 0 || (n > 0 && (!pos || !types || !lam || !grad_pos)))
+        return HPF_ERR_ARG;
+    const int T = c->T;
+    if (T > 8) return HPF_ERR_NOT_IMPLEMENTED;
+    if (n == 0) return HPF_OK;
+    cudaStream_t st = as_stream(stream);
+    const int64_t M = c->M, Mc = c->Mc;
+    TypeScale sc;
+    for (int t = 0; t < T; ++t) sc.s[t] = (float)type_mass[t];
+    int r;
+    // forward force mesh E (kept raw spectra phi_k in d_spec_phi)
+    if ((r = do_paint(c, pos, types, nullptr, n, T, sc, c->d_grid, st)) != HPF_OK) return r;
+    if ((r = exec_r2c(c, c->d_grid, c->d_spec_phi, T, st)) != HPF_OK) return r;
+    if ((r = launch_kspace_force(c, c->d_spec_phi, c->d_spec, nullptr, nullptr, nullptr, st)) !=
+        HPF_OK)
+        return r;
+    if ((r = exec_c2r(c, c->d_spec, c->d_grid, 3 * T, st)) != HPF_OK) return r;
+    k_vjp_local<<<grid_for(n, kThreads), kThreads, 0, st>>>(c->d_grid, pos, types, lam, n, T, M,
+                                                            c->d_box, grad_pos, c->d_err);
+    HPF_LAUNCH_CHECK();
+    // lambda-weighted paint [d][t][M], its spectra, U, and the readout
+    HPF_CUDA_TRY(cudaMemsetAsync(c->d_grid, 0, sizeof(float) * 3 * T * M, st));
+    k_paint_lambda<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, types, lam, n, T, M,
+                                                               c->d_box, c->d_grid);
+    HPF_LAUNCH_CHECK();
+    for (int d = 0; d < 3; ++d)
+        if ((r = exec_r2c(c, c->d_grid + (int64_t)d * T * M, c->d_spec + (int64_t)d * T * Mc, T,
+                          st)) != HPF_OK)
+            return r;
+    const KGeom g = kgeom(c);
+    const int K = T * T;
+    int grid = dQ ? reduce_grid(Mc, kThreads) : grid_for(Mc, kThreads);
+    if (dQ && grid > 8 * HPF_REDUCE_BLOCKS / K) grid = 8 * HPF_REDUCE_BLOCKS / K;
+    double* part = ws_partials(c->d_ws);
+    unsigned int* tick = ws_ticket(c->d_ws);
+#define HPF_VK(TT)                                                                         \
+    k_vjp_kspace<TT><<<grid, kThreads, 0, st>>>(c->d_spec, c->d_spec_phi, Mc, g, c->d_box, \
+                                                c->d_fun, dQ, part, tick)
+    switch (T) {
+        case 1: HPF_VK(1); break;
+        case 2: HPF_VK(2); break;
+        case 3: HPF_VK(3); break;
+        case 4: HPF_VK(4); break;
+        case 5: HPF_VK(5); break;
+        case 6: HPF_VK(6); break;
+        case 7: HPF_VK(7); break;
+        default: HPF_VK(8); break;
+    }
+#undef HPF_VK
+    HPF_LAUNCH_CHECK();
+    if ((r = exec_c2r(c, c->d_spec_phi, c->d_grid, T, st)) != HPF_OK) return r;
+    k_readout_grad<<<grid_for(n, kThreads), kThreads, 0, st>>>(c->d_grid, pos, types, n, T, M,
+                                                               c->d_box, sc, grad_pos, c->d_err,
+                                                               1, 1);
+    HPF_LAUNCH_CHECK();
     return HPF_OK;
 }

@@ -186,6 +186,30 @@ int hpf_energy_fp64(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_
                     const double* type_mass, const float* charges, const double* type_charges,
                     double elec_factor, double* out, void* stream);
 
+/* ---- reverse mode through the force ----------------------------------------
+ * No counterpart in the reference (it has no gradients); used to
+ * differentiate MD trajectories.  With the cotangent lam (device float[n][3])
+ * of the field force F = compute_field_force after update_field
+ * (hymd/field.py:152-200, 428-616) at positions pos:
+ *   grad_pos (device float[n][3]) = d(lam . F)/dpos -- a local CIC-gradient
+ *     readout of lam . E plus a global term through the lambda-weighted
+ *     paint, the adjoint k-space operator and a CIC-gradient readout;
+ *   dQ (device double[T][T], or NULL) = d(lam . F)/dQ_tj for the quadratic
+ *     functional's matrix Q (hpf_ctx_set_functional).
+ * The lambda paint uses FP32 atomics (not bit-reproducible).  T <= 8. */
+int hpf_field_force_vjp(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_t n,
+                        const double* type_mass, const float* lam, float* grad_pos, double* dQ,
+                        void* stream);
+/* out (device float[n][3]) = d/de F_b(r + e lam) at e = 0 for the bond and
+ * angle forces of cbf / caf (the terms of hpf_bonds / hpf_angles): minus the
+ * Hessian of the bonded energy times lam, which is also the vector-Jacobian
+ * product of the forces (the Hessian is symmetric).  Forward-mode dual
+ * arithmetic through the same FP32 formulas; out is zeroed first. */
+int hpf_bonded_hvp(float* out, const float* r, const float* lam, int64_t n, const double* box,
+                   const int32_t* ba, const int32_t* bb, const float* br0, const float* bk,
+                   int64_t nb, const int32_t* aa, const int32_t* ab, const int32_t* ac,
+                   const float* at0, const float* ak, int64_t na, int* d_err, void* stream);
+
 /* ---- PIC_Spectral_GPE electrostatics ------------------------------------
  * update_field_force_q_GPE (hymd/field.py:764-1112) and the energy of
  * compute_field_energy_q_GPE (:706-761): dielectric

@@ -1,0 +1,116 @@
+"""Plain-torch FP64 restatement of the field and bonded forces, written so that
+torch autograd can differentiate it (test infrastructure only: the reference
+gradients for the hand-written reverse-mode kernels).
+
+Same conventions as oracle/field.py (pmesh's CIC nodes at x = i h, r2c
+normalised by 1/M, gradient wavevector with the Nyquist index at zero, filter
+on the full |k|^2):
+  field force   hymd/field.py:152-200, 428-616 (update_field, compute_field_force)
+  bond force    hymd/compute_bond_forces.f90:45-61
+  angle force   hymd/compute_angle_forces.f90:58-92
+The forces are minus the autograd gradient of the energies for the bonded
+terms, and the explicit spectral-gradient readout for the field.
+"""
+import math
+
+import numpy as np
+import torch
+
+
+def _kgrids(n, box, device):
+    kx = 2 * math.pi / box[0] * torch.fft.fftfreq(n[0], 1.0 / n[0], dtype=torch.float64,
+                                                   device=device)
+    ky = 2 * math.pi / box[1] * torch.fft.fftfreq(n[1], 1.0 / n[1], dtype=torch.float64,
+                                                   device=device)
+    kz = 2 * math.pi / box[2] * torch.arange(n[2] // 2 + 1, dtype=torch.float64, device=device)
+    kx, ky, kz = kx[:, None, None], ky[None, :, None], kz[None, None, :]
+    k2 = kx * kx + ky * ky + kz * kz
+    gx, gy, gz = kx.clone(), ky.clone(), kz.clone()
+    if n[0] % 2 == 0:
+        gx[n[0] // 2] = 0.0
+    if n[1] % 2 == 0:
+        gy[:, n[1] // 2] = 0.0
+    if n[2] % 2 == 0:
+        gz[:, :, n[2] // 2] = 0.0
+    return k2, (gx, gy, gz)
+
+
+def _cic(x, n, box):
+    """Corner indices (8, N) into the flat mesh and weights (8, N), the
+    weights differentiable in x."""
+    nn = torch.tensor(n, dtype=torch.float64, device=x.device)
+    L = torch.tensor(box, dtype=torch.float64, device=x.device)
+    s = x * (nn / L)
+    i0 = torch.floor(s).detach()
+    f = s - i0
+    i0 = i0.long()
+    idx, w = [], []
+    for a in (0, 1):
+        for b in (0, 1):
+            for c in (0, 1):
+                ix = (i0[:, 0] + a) % n[0]
+                iy = (i0[:, 1] + b) % n[1]
+                iz = (i0[:, 2] + c) % n[2]
+                idx.append((ix * n[1] + iy) * n[2] + iz)
+                wa = f[:, 0] if a else 1.0 - f[:, 0]
+                wb = f[:, 1] if b else 1.0 - f[:, 1]
+                wc = f[:, 2] if c else 1.0 - f[:, 2]
+                w.append(wa * wb * wc)
+    return torch.stack(idx), torch.stack(w)
+
+
+def field_force(x, types, n_types, masses, mesh, box, Q, sigma):
+    """F (N,3) FP64 of the quadratic functional with matrix Q (T,T); x, Q may
+    require grad."""
+    n = tuple(int(v) for v in mesh)
+    M = n[0] * n[1] * n[2]
+    dV = float(np.prod(box)) / M
+    idx, w = _cic(x, n, box)
+    t = types.long()
+    m = torch.as_tensor(masses, dtype=torch.float64, device=x.device)[t]
+    flat = torch.zeros(n_types * M, dtype=torch.float64, device=x.device)
+    flat = flat.index_add(0, (t[None, :] * M + idx).reshape(-1), (w * (m / dV)[None, :]).reshape(-1))
+    phi = flat.reshape(n_types, *n)
+    Phi = torch.fft.rfftn(phi, dim=(1, 2, 3))
+    k2, g = _kgrids(n, box, x.device)
+    H2 = torch.exp(-sigma * sigma * k2)
+    QPhi = torch.einsum("tj,jxyz->txyz", Q.to(torch.complex128), Phi) * H2
+    E = [torch.fft.irfftn(-1j * g[d] * QPhi, s=n, dim=(1, 2, 3)).reshape(n_types, M)
+         for d in range(3)]
+    F = []
+    for d in range(3):
+        Ed = E[d][t[None, :].expand(8, -1), idx]
+        F.append((w * Ed).sum(0))
+    return torch.stack(F, 1)
+
+
+def _min_image(r, box):
+    L = torch.tensor(box, dtype=r.dtype, device=r.device)
+    return r - L * torch.round(r / L)
+
+
+def bonded_energy(x, box, bonds=None, angles=None):
+    """E of harmonic bonds (a, b, r0, k) and angles (a, b, c, t0, k)."""
+    E = x.new_zeros(())
+    if bonds is not None and len(bonds[0]):
+        a, b, r0, k = bonds
+        r = _min_image(x[b] - x[a], box)
+        d = torch.linalg.norm(r, dim=1)
+        E = E + 0.5 * (k * (d - r0) ** 2).sum()
+    if angles is not None and len(angles[0]):
+        a, b, c, t0, k = angles
+        ra = _min_image(x[a] - x[b], box)
+        rc = _min_image(x[c] - x[b], box)
+        ea = ra / torch.linalg.norm(ra, dim=1, keepdim=True)
+        ec = rc / torch.linalg.norm(rc, dim=1, keepdim=True)
+        th = torch.atan2(torch.linalg.norm(torch.cross(ea, ec, dim=1), dim=1), (ea * ec).sum(1))
+        E = E + 0.5 * (k * (th - t0) ** 2).sum()
+    return E
+
+
+def bonded_force(x, box, bonds=None, angles=None, create_graph=True):
+    if not x.requires_grad:
+        x = x.detach().requires_grad_(True)
+    E = bonded_energy(x, box, bonds, angles)
+    (g,) = torch.autograd.grad(E, x, create_graph=create_graph)
+    return -g

@@ -1,0 +1,172 @@
+"""Reverse mode through the forces and the rRESPA trajectory
+(hymd_gb300.reverse) against a plain-torch FP64 reference differentiated by
+torch autograd (oracle/torch_field.py), and that reference against FP64
+central finite differences.
+
+Tolerances: force vector-Jacobian products within 1e-4 relative RMS of the
+FP64 autograd values (FP32 kernels); the K-step gradient of the profile loss
+with respect to chi within 2e-3 relative (FP32 trajectory against FP64); the
+FP64 reference gradient within 1e-5 of its central finite difference.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import torch_field as tf  # noqa: E402
+
+
+def rel_rms(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
+
+
+def _membrane(respa_inner=3):
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.lipid_membrane(seed=8, n_lipids=60, n_water=900, box=5.6, mesh=20)
+    cfg = s["config"]
+    cfg.respa_inner = respa_inner
+    md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, get_hamiltonian(cfg),
+                 topology=s["topology"], max_block_beads=36)
+    names = cfg.unique_names
+    T = cfg.n_types
+    chi = np.zeros((T, T))
+    for c in cfg.chi:
+        i, j = names.index(c.atom_1), names.index(c.atom_2)
+        chi[i, j] = chi[j, i] = c.interaction_energy
+    return s, cfg, md, chi
+
+
+def _Q_torch(chi, kappa, rho0):
+    T = chi.shape[0]
+    off = 1.0 - torch.eye(T, dtype=torch.float64, device=chi.device)
+    return 1.0 / (kappa * rho0) + 0.5 * (chi + chi.T) * off / rho0
+
+
+def test_field_force_vjp_matches_torch_autograd():
+    from hymd_gb300 import _lib
+    from hymd_gb300.reverse import ForceModel
+    s, cfg, md, chi = _membrane()
+    model = ForceModel(md)
+    chi_t = torch.tensor(chi, dtype=torch.float64)
+    model.set_chi(chi_t)
+    rng = np.random.default_rng(1)
+    lam = torch.tensor(rng.normal(size=(md.n, 3)), dtype=torch.float32, device="cuda")
+    g = torch.empty_like(md.r)
+    dQ = torch.zeros(md.T * md.T, dtype=torch.float64, device="cuda")
+    _lib.call("hpf_field_force_vjp", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n,
+              md.masses, _lib.ptr(lam), _lib.ptr(g), _lib.ptr(dQ), _lib.stream_ptr())
+    x = md.r.double().clone().requires_grad_(True)
+    Q = _Q_torch(chi_t.cuda(), model.kappa, model.rho0).detach().requires_grad_(True)
+    F = tf.field_force(x, md.types, md.T, list(cfg.m), cfg.mesh(), list(cfg.box()), Q,
+                       model.sigma)
+    # the forward agrees first
+    F32 = torch.empty_like(md.r)
+    _lib.call("hpf_field_step", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.types), md.n, md.masses,
+              _lib.ptr(F32), None, None, None, _lib.stream_ptr())
+    assert rel_rms(F32.cpu().numpy(), F.detach().cpu().numpy()) < 1e-5
+    (lam.double() * F).sum().backward()
+    assert rel_rms(g.cpu().numpy(), x.grad.cpu().numpy()) < 1e-4
+    assert rel_rms(dQ.cpu().numpy(), Q.grad.reshape(-1).cpu().numpy()) < 1e-4
+    md.check_errors()
+
+
+def test_bonded_hvp_matches_torch_double_backward():
+    from hymd_gb300 import _lib
+    s, cfg, md, chi = _membrane()
+    t = md.topo
+    rng = np.random.default_rng(2)
+    lam = torch.tensor(rng.normal(size=(md.n, 3)), dtype=torch.float32, device="cuda")
+    out = torch.empty_like(md.r)
+    _lib.call("hpf_bonded_hvp", _lib.ptr(out), _lib.ptr(md.r), _lib.ptr(lam), md.n,
+              _lib.ptr(md.box), _lib.ptr(t.bond_a), _lib.ptr(t.bond_b), _lib.ptr(t.bond_r0),
+              _lib.ptr(t.bond_k), t.n_bonds, _lib.ptr(t.ang_a), _lib.ptr(t.ang_b),
+              _lib.ptr(t.ang_c), _lib.ptr(t.ang_t0), _lib.ptr(t.ang_k), t.n_angles,
+              _lib.ptr(md.err), _lib.stream_ptr())
+    bonds = (t.bond_a.long(), t.bond_b.long(), t.bond_r0.double(), t.bond_k.double())
+    angles = (t.ang_a.long(), t.ang_b.long(), t.ang_c.long(), t.ang_t0.double(),
+              t.ang_k.double())
+    x = md.r.double().clone().requires_grad_(True)
+    Fb = tf.bonded_force(x, list(cfg.box()), bonds, angles, create_graph=True)
+    (hv,) = torch.autograd.grad((Fb * lam.double()).sum(), x)
+    assert rel_rms(out.cpu().numpy(), hv.cpu().numpy()) < 1e-4
+    md.check_errors()
+
+
+def _torch_loss(x0, v0, chi, md, cfg, model, K, target, n_bins, bonds, angles):
+    """The same NVE rRESPA trajectory and profile loss with the FP64 torch
+    forces."""
+    from hymd_gb300.reverse import z_profile
+    box = list(cfg.box())
+    L = torch.tensor(box, dtype=torch.float64, device=x0.device)
+    Q = _Q_torch(chi, model.kappa, model.rho0)
+    m, dt, n_in = md.mass, md.dt, md.respa
+    dto = n_in * dt
+
+    def ff(x):
+        return tf.field_force(x, md.types, md.T, list(cfg.m), cfg.mesh(), box, Q, model.sigma)
+
+    def fb(x):
+        return tf.bonded_force(x, box, bonds, angles, create_graph=True)
+
+    x, v = x0, v0
+    f_field, f_bond = ff(x), fb(x)
+    acc = 0.0
+    for _ in range(K):
+        v = v + (0.5 * dto / m) * f_field
+        for _ in range(n_in):
+            v = v + (0.5 * dt / m) * f_bond
+            x = torch.remainder(x + dt * v, L)
+            f_bond = fb(x)
+            v = v + (0.5 * dt / m) * f_bond
+        f_field = ff(x)
+        v = v + (0.5 * dto / m) * f_field
+        acc = acc + z_profile(x, md.types, md.T, n_bins, box)
+    prof = acc / K
+    return torch.mean((prof - target) ** 2)
+
+
+def test_profile_loss_gradient_matches_fp64_autograd_and_finite_differences():
+    from hymd_gb300.reverse import ForceModel, profile_loss
+    s, cfg, md, chi = _membrane()
+    model = ForceModel(md)
+    K, n_bins = 4, 20
+    rng = np.random.default_rng(3)
+    target = torch.tensor(rng.uniform(0.0, 3.0, size=(md.T, n_bins)), dtype=torch.float32,
+                          device="cuda")
+    chi_t = torch.tensor(chi, dtype=torch.float32, device="cuda", requires_grad=True)
+    loss, _ = profile_loss(md.r.clone(), md.v.clone(), chi_t, model, K, target, n_bins=n_bins,
+                           segment=2)
+    loss.backward()
+    g = chi_t.grad.double().cpu().numpy()
+    t = md.topo
+    bonds = (t.bond_a.long(), t.bond_b.long(), t.bond_r0.double(), t.bond_k.double())
+    angles = (t.ang_a.long(), t.ang_b.long(), t.ang_c.long(), t.ang_t0.double(),
+              t.ang_k.double())
+    chi64 = torch.tensor(chi, dtype=torch.float64, device="cuda", requires_grad=True)
+    args = (md, cfg, model, K, target.double(), n_bins, bonds, angles)
+    x0, v0 = md.r.double(), md.v.double()
+    L64 = _torch_loss(x0, v0, chi64, *args)
+    L64.backward()
+    g64 = chi64.grad.cpu().numpy()
+    assert float(loss.detach()) == pytest.approx(float(L64.detach()), rel=1e-4)
+    pairs = [(i, j) for i in range(md.T) for j in range(i + 1, md.T) if chi[i, j] != 0]
+    got = np.array([g[i, j] + g[j, i] for i, j in pairs])
+    want = np.array([g64[i, j] + g64[j, i] for i, j in pairs])
+    assert rel_rms(got, want) < 2e-3
+    # the FP64 reference itself against a central finite difference (one pair)
+    i, j = pairs[0]
+    h = 1e-3
+    with torch.no_grad():
+        cp, cm = chi64.detach().clone(), chi64.detach().clone()
+        cp[i, j] += h
+        cp[j, i] += h
+        cm[i, j] -= h
+        cm[j, i] -= h
+    fd = (float(_torch_loss(x0, v0, cp, *args)) - float(_torch_loss(x0, v0, cm, *args))) / (2 * h)
+    assert want[0] == pytest.approx(fd, rel=1e-5)
+    md.check_errors()
