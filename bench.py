@@ -544,6 +544,83 @@ def run_replicas(args):
     return 0
 
 
+def run_reverse(args):
+    """Reverse mode on the membrane recipe scaled to 1.3M beads (54 nm box,
+    mesh 128^3): the gradient with respect to chi of the MSE between the
+    z-density profile (100 bins per type) averaged over K outer steps and a
+    target made by the same K-step run with chi perturbed by seeded N(0, 1)
+    kJ/mol; sqrt(K) checkpoints.  Also the adjoint's cost on this system."""
+    import torch
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    from hymd_gb300.reverse import ForceModel, profile_loss
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    n_total, box = 1_300_000, 54.0
+    n_lipids = int(round(0.444 * n_total / 12))
+    s = systems.lipid_membrane(seed=7, n_lipids=n_lipids, n_water=n_total - 12 * n_lipids,
+                               box=box, mesh=128)
+    cfg = s["config"]
+    md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, get_hamiltonian(cfg),
+                 topology=s["topology"], device=dev)
+    model = ForceModel(md)
+    T = cfg.n_types
+    names = cfg.unique_names
+    chi0 = np.zeros((T, T))
+    for c in cfg.chi:
+        i, j = names.index(c.atom_1), names.index(c.atom_2)
+        chi0[i, j] = chi0[j, i] = c.interaction_energy
+    rng = np.random.default_rng(17)
+    pert = np.triu(rng.normal(0.0, 1.0, (T, T)), 1)
+    chi_target = chi0 + pert + pert.T
+    K, n_bins = args.reverse_steps, 100
+    x0, v0 = md.r.clone(), md.v.clone()
+    zero = torch.zeros((T, n_bins), dtype=torch.float32, device=dev)
+    with torch.no_grad():
+        _, target = profile_loss(x0, v0, torch.tensor(chi_target, dtype=torch.float32,
+                                                      device=dev), model, K, zero, n_bins)
+    chi = torch.tensor(chi0, dtype=torch.float32, device=dev, requires_grad=True)
+    torch.cuda.synchronize()
+    a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    with torch.no_grad():
+        a.record()
+        profile_loss(x0, v0, chi.detach(), model, K, target, n_bins)
+        b.record()
+    b.synchronize()
+    fwd_ms = a.elapsed_time(b)
+    torch.cuda.reset_peak_memory_stats(dev)
+    a.record()
+    loss, _ = profile_loss(x0, v0, chi, model, K, target, n_bins)
+    loss.backward()
+    c.record()
+    c.synchronize()
+    fb_ms = a.elapsed_time(c)
+    peak_gb = torch.cuda.max_memory_allocated(dev) / 1e9
+    g = chi.grad.detach().cpu().numpy()
+    flush = L2Flush(torch, dev)
+    adj = adjoint_cost(md, flush, torch)
+    line = {"metric": "reverse-mode K-step gradient of a z-profile loss w.r.t. chi (s)",
+            "value": fb_ms / 1000.0, "unit": "s", "n_gpus": 1, "steps": K, "warmup": 0,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 energies)", "data": "synthetic",
+            "forward_only_s": fwd_ms / 1000.0, "backward_over_forward": fb_ms / fwd_ms - 1.0,
+            "peak_device_memory_gb": peak_gb, "loss": float(loss.detach()),
+            "grad_chi_pairs": {f"{names[i]}-{names[j]}": float(g[i, j] + g[j, i])
+                               for i in range(T) for j in range(i + 1, T)},
+            "adjoint": adj,
+            "config": {"workload": f"lipid membrane {md.n} beads ({n_lipids} lipids + W), "
+                                   f"box {box} nm, mesh 128^3, 5 types",
+                       "K": K, "checkpoint_every": int(np.ceil(np.sqrt(K))),
+                       "respa_inner": int(cfg.respa_inner), "ensemble": "NVE",
+                       "target": "same K-step run with chi + seeded N(0,1) kJ/mol"}}
+    print(json.dumps(line))
+    return 0
+
+
 def profile_stage(args):
     """Run one stage of the step eagerly (no graph, no timing) `--reps` times
     on the workload and exit: a small program for kernel profilers.
@@ -596,11 +673,16 @@ def main():
     ap.add_argument("--reps", type=int, default=4)
     ap.add_argument("--replicas", action="store_true",
                     help="batched 64-replica workload instead of a single system")
+    ap.add_argument("--reverse", action="store_true",
+                    help="reverse-mode chi gradient on the 1.3M-bead membrane")
+    ap.add_argument("--reverse-steps", type=int, default=200)
     args = ap.parse_args()
     if args.profile_stage:
         return profile_stage(args)
     if args.replicas:
         return run_replicas(args)
+    if args.reverse:
+        return run_reverse(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
