@@ -239,7 +239,11 @@ def step_breakdown(md, flush, torch, reps=10):
                                       md.n, _lib.ptr(md.state),
                                       int(md.thermo_args.remove_com) if thermo else 1,
                                       _lib.stream_ptr()))
-    names = ["respa", "paint", "r2c", "kspace", "c2r", "readout_kick", "thermostat_scale"]
+    fused = md.pm.spectral == "fused"
+    # with the fused spectral passes, the profile's second stage holds all
+    # three passes (accumulators -> force mesh) and the next two are empty
+    names = ["respa", "paint", "spectral_fused" if fused else "r2c", "kspace", "c2r",
+             "readout_kick", "thermostat_scale"]
     tot = {k: 0.0 for k in names}
     # the fused kernel with its data left in L2 (back-to-back replays), for
     # comparison with the flushed figure
@@ -271,6 +275,8 @@ def step_breakdown(md, flush, torch, reps=10):
                   md._kick_args(thermo), _lib.stream_ptr(), us)
         for k, x in zip(names[1:6], us):
             tot[k] += x / reps
+    if fused:
+        del tot["kspace"], tot["c2r"]
         flush.zero_()
         a.record(st)
         g_scale.replay()
@@ -436,10 +442,18 @@ def run_gpu(args):
     if args.breakdown and rank == 0:
         print(json.dumps({"breakdown_us": bd}), file=sys.stderr)
     adj = adjoint_cost(md, flush, torch)
-    stage_bytes = {"paint": 16 * n + 4 * T * M, "kspace": 32 * T * Mc,
+    # paint: positions and types read; the float densities written (library
+    # path) or the int64 accumulators (fused path, no finalize pass)
+    paint_b = 16 * n + (8 if "spectral_fused" in bd else 4) * T * M
+    stage_bytes = {"paint": paint_b, "kspace": 32 * T * Mc,
+                   # fused passes: accumulators read and cleared, force mesh
+                   # written (the two intermediate spectra are extra traffic)
+                   "spectral_fused": 28 * T * M,
                    "readout_kick": 28 * n + 12 * T * M + 36 * n}
     kernels = {}
     for k, b_ in stage_bytes.items():
+        if k not in bd:
+            continue
         gbs = b_ / (bd[k] * 1e-6) / 1e9
         kernels[k] = {"algorithmic_bytes": b_, "us": bd[k], "achieved": gbs, "frac": gbs / peak,
                       "traffic": traffic.get(k)}

@@ -41,6 +41,8 @@ _SIGNATURES = {
     "hpf_ctx_destroy": [P],
     "hpf_ctx_set_box": [P, ctypes.POINTER(D), P],
     "hpf_ctx_box_state": [P, ctypes.POINTER(P)],
+    "hpf_ctx_set_spectral": [P, I],
+    "hpf_ctx_get_spectral": [P, ctypes.POINTER(I), ctypes.POINTER(I)],
     "hpf_ctx_set_functional": [P, ctypes.POINTER(D), ctypes.POINTER(D), D, D],
     "hpf_get_error": [P, P, ctypes.POINTER(I)],
     "hpf_paint": [P, P, P, I64, ctypes.POINTER(D), P, P],

@@ -28,20 +28,6 @@ struct TypeScale {
     float s[HPF_MAX_TYPES + 1];
 };
 
-// Paint deposits are integers in units of 2^-24 of a particle's weight (a
-// charge of up to 2^7 e keeps a deposit inside int32).
-constexpr float kFixScale = 16777216.0f;          // 2^24
-constexpr float kFixInv = 5.9604644775390625e-8f;  // 2^-24
-
-// int64 -> float without the 64-bit conversion instruction (FP64 pipe on
-// GB300): magnitude split into 32-bit halves, one FMA.  Deterministic.
-__device__ __forceinline__ float fix_to_float(long long x) {
-    const bool neg = x < 0;
-    const unsigned long long a = neg ? (unsigned long long)(-x) : (unsigned long long)x;
-    const float f = fmaf((float)(unsigned)(a >> 32), 4294967296.0f, (float)(unsigned)a);
-    return neg ? -f : f;
-}
-
 struct TypeScaleD {
     double s[HPF_MAX_TYPES + 1];
 };
@@ -775,7 +761,7 @@ int launch_kspace_force(hpf_ctx* c, const float2* phi_raw, float2* force_k, floa
 
 int do_paint(hpf_ctx* c, const float* pos, const int32_t* types, const float* charges,
              int64_t n, int G, const TypeScale& sc, float* out, cudaStream_t st,
-             const double* scale = nullptr) {
+             const double* scale = nullptr, bool finalize = true) {
     // G = number of grids (T for densities; 1 for charges, painted into the
     // accumulator slot after the T density slots)
     unsigned long long* acc = c->d_acc + (charges ? (int64_t)c->T * c->M : 0);
@@ -785,6 +771,7 @@ int do_paint(hpf_ctx* c, const float* pos, const int32_t* types, const float* ch
                                                            c->M, c->d_err, scale);
         HPF_LAUNCH_CHECK();
     }
+    if (!finalize) return HPF_OK;  // the fused spectral pass reads the accumulators
     if (c->M % 4 == 0) {
         dim3 grid(grid_for(c->M / 4, kThreads), G);
         k_paint_finalize<<<grid, kThreads, 0, st>>>(acc, out, c->M, G, sc, c->d_box);
@@ -907,6 +894,8 @@ int hpf_ctx_destroy(hpf_ctx* c) {
     cudaFree(c->gpe_spec);
     cudaFree(c->gpe_ws);
     cudaFreeHost(c->gpe_host);
+    cudaFree(c->d_tw);
+    cudaFree(c->d_spec_ws);
     free(c);
     return HPF_OK;
 }
@@ -984,6 +973,7 @@ int hpf_ctx_create(hpf_ctx** out, int n0, int n1, int n2, int T, const double bo
         CK(cudaMemcpy(c->d_fun, &c->h_fun, sizeof(Functional), cudaMemcpyHostToDevice));
     }
 #undef CK
+    if ((st = spectral_setup(c)) != HPF_OK) goto fail;
     *out = c;
     return HPF_OK;
 fail:
@@ -999,6 +989,20 @@ int hpf_ctx_set_box(hpf_ctx* c, const double box[3], void* stream) {
     HPF_CUDA_TRY(cudaMemcpyAsync(c->d_box, &c->h_box, sizeof(BoxState), cudaMemcpyHostToDevice,
                                  as_stream(stream)));
     HPF_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    return HPF_OK;
+}
+
+int hpf_ctx_set_spectral(hpf_ctx* c, int fused) {
+    if (!c || fused < 0 || fused > 1) return HPF_ERR_ARG;
+    if (fused && !c->spec_ok) return HPF_ERR_ARG;
+    c->spec_fused = fused;
+    return HPF_OK;
+}
+
+int hpf_ctx_get_spectral(const hpf_ctx* c, int* fused, int* available) {
+    if (!c) return HPF_ERR_ARG;
+    if (fused) *fused = c->spec_fused;
+    if (available) *available = c->spec_ok;
     return HPF_OK;
 }
 
@@ -1165,6 +1169,15 @@ int hpf_field_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
     TypeScale sc;
     for (int t = 0; t < c->T; ++t) sc.s[t] = (float)type_mass[t];
     int r;
+    if (c->spec_fused) {
+        if ((r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale,
+                          false)) != HPF_OK)
+            return r;
+        if ((r = spectral_field_force(c, sc.s, sums, st)) != HPF_OK) return r;
+        if (n > 0)
+            return launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, kick, st);
+        return HPF_OK;
+    }
     if ((r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale)) != HPF_OK)
         return r;
     if ((r = exec_r2c(c, c->d_grid, c->d_spec_phi, c->T, st)) != HPF_OK) return r;
@@ -1188,14 +1201,26 @@ int hpf_field_step_profile(hpf_ctx* c, float* pos, const int32_t* types, int64_t
     for (int t = 0; t < c->T; ++t) sc.s[t] = (float)type_mass[t];
     int r = HPF_OK;
     cudaEventRecord(ev[0], st);
-    if (!r) r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale);
-    cudaEventRecord(ev[1], st);
-    if (!r) r = exec_r2c(c, c->d_grid, c->d_spec_phi, c->T, st);
-    cudaEventRecord(ev[2], st);
-    if (!r) r = launch_kspace_force(c, c->d_spec_phi, c->d_spec, nullptr, nullptr, sums, st);
-    cudaEventRecord(ev[3], st);
-    if (!r) r = exec_c2r(c, c->d_spec, c->d_grid, 3 * c->T, st);
-    cudaEventRecord(ev[4], st);
+    if (c->spec_fused) {
+        // paint (deposits only) | fused passes A+B+C, split evenly | readout:
+        // the stage boundaries of the library path are not separate launches
+        // here, so "r2c" holds the passes, the next two stages are empty
+        if (!r) r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale, false);
+        cudaEventRecord(ev[1], st);
+        if (!r) r = spectral_field_force(c, sc.s, sums, st);
+        cudaEventRecord(ev[2], st);
+        cudaEventRecord(ev[3], st);
+        cudaEventRecord(ev[4], st);
+    } else {
+        if (!r) r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale);
+        cudaEventRecord(ev[1], st);
+        if (!r) r = exec_r2c(c, c->d_grid, c->d_spec_phi, c->T, st);
+        cudaEventRecord(ev[2], st);
+        if (!r) r = launch_kspace_force(c, c->d_spec_phi, c->d_spec, nullptr, nullptr, sums, st);
+        cudaEventRecord(ev[3], st);
+        if (!r) r = exec_c2r(c, c->d_spec, c->d_grid, 3 * c->T, st);
+        cudaEventRecord(ev[4], st);
+    }
     if (!r) r = launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, kick, st);
     cudaEventRecord(ev[5], st);
     cudaEventSynchronize(ev[5]);
@@ -1216,22 +1241,30 @@ int hpf_pic_step(hpf_ctx* c, const float* pos, const float* charges, int64_t n,
     cudaStream_t st = as_stream(stream);
     TypeScale sc;
     sc.s[0] = 1.0f;
-    float* rho = phi_q ? phi_q : c->d_grid;
+    const float four_pi_fac = (float)(4.0 * 3.14159265358979323846 * elec_factor);
     int r;
-    if ((r = do_paint(c, pos, nullptr, charges, n, 1, sc, rho, st)) != HPF_OK) return r;
-    if ((r = exec_r2c(c, rho, c->d_spec_phi, 1, st)) != HPF_OK) return r;
-    KGeom g = kgeom(c);
-    const int grid = sums ? reduce_grid(c->Mc, kThreads) : grid_for(c->Mc, kThreads);
-    k_kspace_pic<<<grid, kThreads, 0, st>>>(c->d_spec_phi, c->d_spec, c->Mc, g, c->d_box,
-                                            c->d_fun,
-                                            (float)(4.0 * 3.14159265358979323846 * elec_factor),
-                                            sums, ws_partials(c->d_ws), ws_ticket(c->d_ws));
-    HPF_LAUNCH_CHECK();
-    if (psi_k)
-        HPF_CUDA_TRY(cudaMemcpyAsync(psi_k, c->d_spec, sizeof(float2) * c->Mc,
-                                     cudaMemcpyDeviceToDevice, st));
-    // c2r of psi and the three field components
-    if ((r = exec_c2r(c, c->d_spec, c->d_grid, 4, st)) != HPF_OK) return r;
+    if (c->spec_fused && !phi_q && !psi_k) {
+        // fused passes (no real charge grid or psi spectrum is produced)
+        if ((r = do_paint(c, pos, nullptr, charges, n, 1, sc, c->d_grid, st, nullptr, false)) !=
+            HPF_OK)
+            return r;
+        if ((r = spectral_pic(c, four_pi_fac, psi != nullptr, sums, st)) != HPF_OK) return r;
+    } else {
+        float* rho = phi_q ? phi_q : c->d_grid;
+        if ((r = do_paint(c, pos, nullptr, charges, n, 1, sc, rho, st)) != HPF_OK) return r;
+        if ((r = exec_r2c(c, rho, c->d_spec_phi, 1, st)) != HPF_OK) return r;
+        KGeom g = kgeom(c);
+        const int grid = sums ? reduce_grid(c->Mc, kThreads) : grid_for(c->Mc, kThreads);
+        k_kspace_pic<<<grid, kThreads, 0, st>>>(c->d_spec_phi, c->d_spec, c->Mc, g, c->d_box,
+                                                c->d_fun, four_pi_fac, sums,
+                                                ws_partials(c->d_ws), ws_ticket(c->d_ws));
+        HPF_LAUNCH_CHECK();
+        if (psi_k)
+            HPF_CUDA_TRY(cudaMemcpyAsync(psi_k, c->d_spec, sizeof(float2) * c->Mc,
+                                         cudaMemcpyDeviceToDevice, st));
+        // c2r of psi and the three field components
+        if ((r = exec_c2r(c, c->d_spec, c->d_grid, 4, st)) != HPF_OK) return r;
+    }
     if (psi)
         HPF_CUDA_TRY(cudaMemcpyAsync(psi, c->d_grid, sizeof(float) * c->M,
                                      cudaMemcpyDeviceToDevice, st));

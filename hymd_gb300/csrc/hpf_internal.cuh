@@ -70,7 +70,35 @@ struct hpf_ctx {
     float2* gpe_spec;
     double* gpe_ws;
     double* gpe_host;
+    // fused spectral passes (power-of-two meshes): twiddle table
+    // exp(-2 pi i m / 512), k-space tile width, partial sums + ticket
+    float2* d_tw;
+    double* d_spec_ws;
+    int spec_W, spec_tiles;
+    int spec_ok;     // the mesh qualifies and the scratch exists
+    int spec_fused;  // use them (default when spec_ok)
 };
+
+// Paint deposits are integers in units of 2^-24 of a particle's weight (a
+// charge of up to 2^7 e keeps a deposit inside int32).
+constexpr float kFixScale = 16777216.0f;          // 2^24
+constexpr float kFixInv = 5.9604644775390625e-8f;  // 2^-24
+
+// int64 -> float without the 64-bit conversion instruction (FP64 pipe on
+// GB300): magnitude split into 32-bit halves, one FMA.  Deterministic.
+__device__ __forceinline__ float fix_to_float(long long x) {
+    const bool neg = x < 0;
+    const unsigned long long a = neg ? (unsigned long long)(-x) : (unsigned long long)x;
+    const float f = fmaf((float)(unsigned)(a >> 32), 4294967296.0f, (float)(unsigned)a);
+    return neg ? -f : f;
+}
+
+// Fused spectral passes (hpf_spectral.cu): eligibility, setup at context
+// creation, and accumulators -> force mesh (c->d_grid, [3T][M]).
+bool spectral_eligible(const hpf_ctx* c);
+int spectral_setup(hpf_ctx* c);
+int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cudaStream_t st);
+int spectral_pic(hpf_ctx* c, float four_pi_fac, bool want_psi, double* sums, cudaStream_t st);
 
 #define HPF_REDUCE_GRID 304  // blocks of a reduction kernel (2 per SM on 152 SMs)
 

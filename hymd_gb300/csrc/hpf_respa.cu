@@ -109,10 +109,12 @@ struct CtaSync {
 };
 
 // Shared-memory layout of one group (offsets in bytes, 16-byte aligned).
+// Bead positions, velocities, forces and the term force slots are float4
+// (x, y, z, unused): one 128-bit shared-memory access per vector.
 struct GroupSmem {
     float2 *bond_p, *ang_p;
     int2* ang_ijk;
-    float *rs, *vs, *fs, *slot;
+    float4 *rs, *vs, *fs, *slot;
     int *bond_ij, *inc_start, *inc;
 };
 
@@ -123,8 +125,8 @@ __host__ __device__ inline size_t group_smem_bytes(int nb, int ns, int ni, int n
     o += align16(sizeof(float2) * nbd);  // bond_p
     o += align16(sizeof(float2) * na);   // ang_p
     o += align16(sizeof(int2) * na);     // ang_ijk
-    o += align16(sizeof(float) * 9 * nb);
-    o += align16(sizeof(float) * 3 * ns);
+    o += align16(sizeof(float4) * 3 * nb);
+    o += align16(sizeof(float4) * ns);
     o += align16(sizeof(int) * nbd);
     o += align16(sizeof(int) * (nb + 1));
     o += align16(sizeof(int) * ni);
@@ -140,12 +142,12 @@ __device__ __forceinline__ GroupSmem carve(char* base, const hpf_respa_plan& p) 
     o += align16(sizeof(float2) * p.mx_angles);
     g.ang_ijk = reinterpret_cast<int2*>(base + o);
     o += align16(sizeof(int2) * p.mx_angles);
-    g.rs = reinterpret_cast<float*>(base + o);
-    g.vs = g.rs + 3 * p.mx_beads;
-    g.fs = g.rs + 6 * p.mx_beads;
-    o += align16(sizeof(float) * 9 * p.mx_beads);
-    g.slot = reinterpret_cast<float*>(base + o);
-    o += align16(sizeof(float) * 3 * p.mx_slots);
+    g.rs = reinterpret_cast<float4*>(base + o);
+    g.vs = g.rs + p.mx_beads;
+    g.fs = g.rs + 2 * p.mx_beads;
+    o += align16(sizeof(float4) * 3 * p.mx_beads);
+    g.slot = reinterpret_cast<float4*>(base + o);
+    o += align16(sizeof(float4) * p.mx_slots);
     g.bond_ij = reinterpret_cast<int*>(base + o);
     o += align16(sizeof(int) * p.mx_bonds);
     g.inc_start = reinterpret_cast<int*>(base + o);
@@ -154,10 +156,17 @@ __device__ __forceinline__ GroupSmem carve(char* base, const hpf_respa_plan& p) 
     return g;
 }
 
-__device__ __forceinline__ void put3(float* s, int slot, V3 v) {
-    s[3 * slot] = v.x;
-    s[3 * slot + 1] = v.y;
-    s[3 * slot + 2] = v.z;
+__device__ __forceinline__ void put3(float4* s, int slot, V3 v) {
+    s[slot] = make_float4(v.x, v.y, v.z, 0.0f);
+}
+
+__device__ __forceinline__ V3 get3(const float4* s, int i) {
+    const float4 q = s[i];
+    return v3(q.x, q.y, q.z);
+}
+
+__device__ __forceinline__ float comp(const float4& q, int d) {
+    return d == 0 ? q.x : (d == 1 ? q.y : q.z);
 }
 
 // Group-local work shared by the warp and CTA variants.  `lane`/`width`
@@ -188,9 +197,9 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
         const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
         float x = forces_only ? 0.0f : v[g];
         for (int q = 0; q < slow.n; ++q) x = x + h_out * div_m(slow.f[q][g], mass, inv_m);
-        s.vs[e] = x;
-        s.rs[e] = r[g];
-        s.fs[e] = fb[g];
+        reinterpret_cast<float*>(s.vs + i)[d] = x;
+        reinterpret_cast<float*>(s.rs + i)[d] = r[g];
+        reinterpret_cast<float*>(s.fs + i)[d] = fb[g];
     }
     for (int t = lane; t < nbd; t += width) {
         s.bond_ij[t] = p.bond_ij[b0 + t];
@@ -210,42 +219,39 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
         // the fixed incidence order), closing half kick of that step; then,
         // unless all steps are done, the opening half kick, drift and wrap
         for (int i = lane; i < nb; i += width) {
-            float F[3];
+            float4 F;
             if (it == 0) {
-                F[0] = s.fs[3 * i];
-                F[1] = s.fs[3 * i + 1];
-                F[2] = s.fs[3 * i + 2];
+                F = s.fs[i];
             } else {
-                F[0] = F[1] = F[2] = 0.0f;
+                // signed sum in the fixed incidence order; fmaf(-1, x, F) is
+                // the exactly rounded F - x, so no branch on the sign
+                F = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 for (int q = s.inc_start[i]; q < s.inc_start[i + 1]; ++q) {
                     const int en = s.inc[q];
-                    const float* sl = s.slot + 3 * (en >> 1);
-                    if (en & 1) {
-                        F[0] -= sl[0];
-                        F[1] -= sl[1];
-                        F[2] -= sl[2];
-                    } else {
-                        F[0] += sl[0];
-                        F[1] += sl[1];
-                        F[2] += sl[2];
-                    }
+                    const float4 sl = s.slot[en >> 1];
+                    const float sg = (en & 1) ? -1.0f : 1.0f;
+                    F.x = fmaf(sg, sl.x, F.x);
+                    F.y = fmaf(sg, sl.y, F.y);
+                    F.z = fmaf(sg, sl.z, F.z);
                 }
-                s.fs[3 * i] = F[0];
-                s.fs[3 * i + 1] = F[1];
-                s.fs[3 * i + 2] = F[2];
+                s.fs[i] = F;
             }
             if (forces_only) continue;
+            float4 rv = s.rs[i], vv = s.vs[i];
+            float xr[3] = {rv.x, rv.y, rv.z}, xv[3] = {vv.x, vv.y, vv.z};
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                const float a = div_m(F[d], mass, inv_m);
-                float x = s.vs[3 * i + d];
+                const float a = div_m(comp(F, d), mass, inv_m);
+                float x = xv[d];
                 if (it > 0) x = x + hdt * a;
                 if (it < respa) {
                     x = x + hdt * a;
-                    s.rs[3 * i + d] = wrapf(s.rs[3 * i + d] + dt * x, bx.L[d]);
+                    xr[d] = wrapf(xr[d] + dt * x, bx.L[d]);
                 }
-                s.vs[3 * i + d] = x;
+                xv[d] = x;
             }
+            s.vs[i] = make_float4(xv[0], xv[1], xv[2], 0.0f);
+            s.rs[i] = make_float4(xr[0], xr[1], xr[2], 0.0f);
         }
         if (it == respa) break;
         sync();
@@ -255,8 +261,8 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
             const float2 pr = s.bond_p[t];
             float e;
             V3 vir;
-            const V3 pa = v3(s.rs[3 * bi], s.rs[3 * bi + 1], s.rs[3 * bi + 2]);
-            const V3 pb = v3(s.rs[3 * bj], s.rs[3 * bj + 1], s.rs[3 * bj + 2]);
+            const V3 pa = get3(s.rs, bi);
+            const V3 pb = get3(s.rs, bj);
             put3(s.slot, t, bond_term(pa, pb, pr.x, pr.y, bx, e, vir));
             if (last_it) {
                 acc[0] += e;
@@ -269,9 +275,9 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
             const int2 q = s.ang_ijk[t];
             const int ai = q.x & 0xffff, aj = q.x >> 16, ak = q.y;
             const float2 pr = s.ang_p[t];
-            const V3 pa = v3(s.rs[3 * ai], s.rs[3 * ai + 1], s.rs[3 * ai + 2]);
-            const V3 pb = v3(s.rs[3 * aj], s.rs[3 * aj + 1], s.rs[3 * aj + 2]);
-            const V3 pc = v3(s.rs[3 * ak], s.rs[3 * ak + 1], s.rs[3 * ak + 2]);
+            const V3 pa = get3(s.rs, ai);
+            const V3 pb = get3(s.rs, aj);
+            const V3 pc = get3(s.rs, ak);
             V3 ga, gc, vir;
             float e;
             if (!angle_term(pa, pb, pc, pr.x, pr.y, bx, ga, gc, e, vir)) {
@@ -294,8 +300,7 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                 const int2 tl = p.dih_tl[d0 + t];
                 const int li[4] = {q.x, q.y, q.z, q.w};
                 V3 pos[4];
-                for (int j = 0; j < 4; ++j)
-                    pos[j] = v3(s.rs[3 * li[j]], s.rs[3 * li[j] + 1], s.rs[3 * li[j] + 2]);
+                for (int j = 0; j < 4; ++j) pos[j] = get3(s.rs, li[j]);
                 float* dip = nullptr;
                 float* tmx = nullptr;
                 if (last_it && dipoles) {
@@ -319,15 +324,17 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
     // write back (each bead by the lane that owns it)
     for (int i = lane; i < nb; i += width) {
         const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i];
+        const float4 fq = s.fs[i];
         if (forces_only) {
-            for (int d = 0; d < 3; ++d) fb[g + d] = s.fs[3 * i + d];
+            for (int d = 0; d < 3; ++d) fb[g + d] = comp(fq, d);
             continue;
         }
+        const float4 vq = s.vs[i], rq = s.rs[i];
         for (int d = 0; d < 3; ++d) {
-            const float x = s.vs[3 * i + d];
+            const float x = comp(vq, d);
             v[g + d] = x;
-            r[g + d] = s.rs[3 * i + d];
-            fb[g + d] = s.fs[3 * i + d];
+            r[g + d] = comp(rq, d);
+            fb[g + d] = comp(fq, d);
             acc[9] = fmaf(x, x, acc[9]);
         }
     }

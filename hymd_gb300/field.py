@@ -92,6 +92,26 @@ class ParticleMesh:
             self._functional_Q = Q
         return Q, b, c, sigma
 
+    @property
+    def spectral(self):
+        """Transform path of the fused field step: "fused" (this library's
+        shared-memory FFTs; default on power-of-two meshes) or "cufft"."""
+        f, a = _lib.ctypes.c_int(0), _lib.ctypes.c_int(0)
+        _lib.call("hpf_ctx_get_spectral", self._h, _lib.ctypes.byref(f), _lib.ctypes.byref(a))
+        return "fused" if f.value else "cufft"
+
+    @spectral.setter
+    def spectral(self, path):
+        if path not in ("fused", "cufft"):
+            raise ValueError(f"spectral path {path!r}: 'fused' or 'cufft'")
+        _lib.call("hpf_ctx_set_spectral", self._h, 1 if path == "fused" else 0)
+
+    @property
+    def spectral_available(self):
+        f, a = _lib.ctypes.c_int(0), _lib.ctypes.c_int(0)
+        _lib.call("hpf_ctx_get_spectral", self._h, _lib.ctypes.byref(f), _lib.ctypes.byref(a))
+        return bool(a.value)
+
     def check_errors(self):
         code = _lib.ctypes.c_int(0)
         _lib.call("hpf_get_error", self._h, _lib.stream_ptr(), _lib.ctypes.byref(code))

@@ -122,6 +122,16 @@ int hpf_ctx_destroy(hpf_ctx* ctx);
 int hpf_ctx_set_box(hpf_ctx* ctx, const double box[3], void* stream);
 /* Device pointer to the box state (double L[3], V, dV at offsets 0..4). */
 int hpf_ctx_box_state(hpf_ctx* ctx, void** d_state);
+/* Transform path of hpf_field_step and hpf_pic_step (same arithmetic, FP32
+ * either way): on a mesh whose axes are powers of two (n0 8..256, n1 and n2
+ * 16..128; n_types <= 8) the default is this library's fused passes
+ * (shared-memory FFTs, the k-space map inside the x transform, the paint's
+ * accumulators read directly);
+ * fused = 0 selects the cuFFT path.  fused = 1 on a mesh that does not
+ * qualify returns HPF_ERR_ARG.  The getter reports the current choice and
+ * whether the fused path is available (either pointer may be NULL). */
+int hpf_ctx_set_spectral(hpf_ctx* ctx, int fused);
+int hpf_ctx_get_spectral(const hpf_ctx* ctx, int* fused, int* available);
 /* Quadratic interaction functional w = 1/2 phi.Q.phi + b.phi + c and filter
  * width sigma (hymd/hamiltonian.py:74-486, H at :57-71).  Q is T*T row-major. */
 int hpf_ctx_set_functional(hpf_ctx* ctx, const double* Q, const double* b, double c,

@@ -255,3 +255,54 @@ def test_gaussian_core_energy_known_answer():
                                                   None, cfg, None)
     E = of.gaussian_core_energy(r, cfg.kappa, cfg.sigma, cfg.rho0, a_shift=True)
     assert W == pytest.approx(E, rel=1e-6)
+
+
+@pytest.mark.parametrize("mesh,T", [
+    ((32, 32, 32), 3), ((8, 16, 32), 2), ((16, 16, 16), 1), ((64, 32, 16), 5),
+    ((32, 64, 128), 3), ((128, 16, 16), 2), ((16, 128, 64), 4), ((256, 16, 32), 1),
+    ((16, 32, 16), 8)])
+def test_fused_spectral_path_matches_oracle_and_library_path(mesh, T):
+    """hpf_field_step through this library's shared-memory transforms (the
+    default on power-of-two meshes) and through cuFFT, against the FP64
+    oracle: forces within FORCE_RTOL; the k-space energy and pressure sums of
+    the two paths within 1e-6 of each other; the paint accumulators left
+    cleared (a second step gives the same forces)."""
+    from hymd_gb300 import _lib
+    cfg, ham, fun, r, types = make_system(sum(mesh) + T, n=3000, T=T, mesh=mesh)
+    gf, pm, fl, _, _, R, Ty = _setup(cfg, ham, r, types)
+    pm.set_functional(ham)
+    assert pm.spectral_available and pm.spectral == "fused"
+    ref = of.update_field(r.astype(np.float64), types, cfg.n_types, cfg.mesh(), cfg.box(), cfg.m,
+                          fun, cfg.sigma)
+    Fref = of.compute_field_force(ref["force_mesh"], r.astype(np.float64), types, cfg.n_types,
+                                  cfg.mesh(), cfg.box())
+    out = {}
+    for path in ("fused", "cufft", "fused"):
+        pm.spectral = path
+        F = torch.zeros_like(R)
+        sums = _lib.new_workspace(R.device)
+        _lib.call("hpf_field_step", pm._h, _lib.ptr(R), _lib.ptr(Ty), R.shape[0],
+                  _lib.dvec(cfg.m), _lib.ptr(F), _lib.ptr(sums), None, None, _lib.stream_ptr())
+        torch.cuda.synchronize()
+        f = F.cpu().numpy()
+        assert rel_rms(f, Fref) < FORCE_RTOL, path
+        s = sums[:4].cpu().numpy()
+        if path in out:
+            assert np.array_equal(f, out[path][0])  # accumulators were cleared
+            assert np.array_equal(s, out[path][1])
+        out[path] = (f, s)
+    assert rel_rms(out["fused"][0], out["cufft"][0]) < 1e-6
+    np.testing.assert_allclose(out["fused"][1], out["cufft"][1], rtol=1e-6)
+    pm.check_errors()
+
+
+def test_fused_spectral_path_availability():
+    from hymd_gb300 import _lib
+    from hymd_gb300.field import ParticleMesh
+    assert ParticleMesh((64, 64, 64), (10.0, 10.0, 10.0), 5).spectral == "fused"
+    for mesh, T in [((24, 24, 26), 3), ((32, 32, 32), 9), ((512, 32, 32), 1),
+                    ((16, 256, 16), 2), ((16, 16, 512), 1)]:
+        pm = ParticleMesh(mesh, (10.0, 10.0, 10.0), T)
+        assert not pm.spectral_available and pm.spectral == "cufft"
+        with pytest.raises(_lib.HPFError):
+            pm.spectral = "fused"
