@@ -169,9 +169,17 @@ struct IntC {
     static constexpr int value = V;
 };
 
-template <int N, bool INV, bool CFAST, class LD, class ST, class FIN>
+struct NoPre {
+    template <int R>
+    __device__ __forceinline__ void operator()(int, int, float2 (&)[R]) const {}
+};
+
+// pre(c, n2, a): applied to an item's N1 loaded values (natural elements
+// N2*i + n2) before its transform; the loads come first, all of them, so
+// that they are in flight together.
+template <int N, bool INV, bool CFAST, class LD, class ST, class FIN, class PRE = NoPre>
 __device__ __forceinline__ void fft_step1(int count, float inv_count, LD ld, ST st, FIN fin,
-                                          const float2* __restrict__ tw) {
+                                          const float2* __restrict__ tw, PRE pre = PRE()) {
     constexpr int N1 = split1(N), N2 = N / N1;
     constexpr int TW = kTableN / N;
     const int items = count * N2;
@@ -187,6 +195,7 @@ __device__ __forceinline__ void fft_step1(int count, float inv_count, LD ld, ST 
         float2 a[N1];
 #pragma unroll
         for (int i = 0; i < N1; ++i) a[i] = ld(c, N2 * i + n2);
+        pre(c, n2, a);
         reg_fft<N1, INV>(a);
         if (N2 == 1) {
 #pragma unroll

@@ -100,6 +100,11 @@ int spectral_setup(hpf_ctx* c);
 int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cudaStream_t st);
 int spectral_pic(hpf_ctx* c, float four_pi_fac, bool want_psi, double* sums, cudaStream_t st);
 
+// CSVR per-group velocity sums and scale factors (no kick), hpf_md.cu.
+int launch_csvr_sums(float* v, const int32_t* group, int64_t n, const HpfCsvrArgs& a,
+                     const double* randoms, int* counter, double* state, double* ws, int* err,
+                     cudaStream_t st);
+
 #define HPF_REDUCE_GRID 304  // blocks of a reduction kernel (2 per SM on 152 SMs)
 
 // Layout of a reduction workspace (see HPF_OUT_DOUBLES in the C ABI header).

@@ -15,14 +15,16 @@
 //      accumulators (and clear them), scale to density, r2c along z (a
 //      length-n2/2 complex transform and the usual split of even and odd
 //      samples), c2c along y; write the plane of the half spectrum.
+//   B  k_spec_kspace one block per tile of W (y, kz) columns: c2c along x of
+//      the T density columns, the k-space map above and the Parseval sums of
+//      the energy and pressure, inverse c2c along x of two columns per type,
+//      -i k'_x v and v (the y and z forces -i k'_y v, -i k'_z v differ from
+//      v by factors constant along x, applied in pass C).
+//   C  k_spec_inv    one block per (force grid, x) plane: inverse c2c along
+//      y, c2r along z; write the real plane.
 // Each transform's first step reads its inputs from global memory (or
 // computes them) and its second step writes global memory; shared memory
 // holds only the data between steps.
-//   B  k_spec_kspace one block per tile of W (y, kz) columns: c2c along x of
-//      the T density columns, the k-space map above and the Parseval sums of
-//      the energy and pressure, inverse c2c along x of the 3T force columns.
-//   C  k_spec_inv    one block per (force grid, x) plane: inverse c2c along
-//      y, c2r along z; write the real plane.
 // Each element is read and written once per pass; the intermediates of a
 // 64^3 mesh stay in L2.  The FFTs are unnormalised as cuFFT's, so the
 // k-space map is the same expression.
@@ -188,9 +190,9 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
 // ------------------------------------------------------------ pass B ---
 // One block per tile of W (y, kz) columns: x transform of the T density
 // columns (step 1 reads the spectrum planes), then the inverse x transforms
-// of the 3T force columns, whose first step computes its inputs from the
-// transformed densities (the k-space map) and whose second step writes the
-// force spectra.  Tile layout [grid][x][w], grids g.ts apart.
+// of two columns per type (-i g_x v_t and v_t, v_t from the k-space map
+// applied in place to the transformed densities), whose second step writes
+// the output spectra.  Tile layout [grid][x][w], grids g.ts apart.
 template <int N>
 __global__ void __launch_bounds__(kSpecThreads, 2)
     k_spec_kspace(const float2* __restrict__ phi, float2* __restrict__ force, SpecGeom g, int T,
@@ -204,7 +206,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     const int64_t plane = (int64_t)g.n1 * g.nzc;  // stride of x in a half spectrum
     const int j0 = blockIdx.x * W;
     float2* in = sm;            // [T][Nx][W]
-    float2* out = sm + T * TS;  // [3T][Nx][W]
+    float2* out = sm + T * TS;  // [2T][Nx][W]
     for (int e = threadIdx.x; e < T * T; e += blockDim.x)
         sQ[(e / T) * kSpecMaxT + e % T] = fun->Q[e];
     for (int e = threadIdx.x; e < T; e += blockDim.x) sb[e] = fun->b[e];
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     const float invM = (float)bs->inv_M;
     const float s2h = fun->sigma2_half;
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    const int cin = T * W, cout = 3 * T * W;
+    const int cin = T * W, cout = 2 * T * W;
     const float inv_cin = 1.0f / (float)cin, inv_cout = 1.0f / (float)cout;
     {
         constexpr int N1 = split1(N), N2 = N / N1;
@@ -278,24 +280,24 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             }
         }
         __syncthreads();
-        // inverse x transforms, step 1; item (grid 3 to + d, w, n2):
-        // F_{to,d} = -i g_d v_to
+        // inverse x transforms, step 1; item (grid 2 to + e, w, n2): e = 0
+        // -i g_x v_to (the x force), e = 1 v_to itself (the y and z forces,
+        // -i g_y v and -i g_z v, are formed from it in pass C: g_y and g_z
+        // do not vary along x)
         const int items = cout * N2;
         for (int it = threadIdx.x; it < items; it += blockDim.x) {
             const int n2 = N2 == 1 ? 0 : div_inv(it, cout, inv_cout);
             const int c = it - n2 * cout;
             const int gq = c >> ws, w = c & (W - 1);
-            const int to = gq / 3, d = gq - 3 * to;
-            const ColInfo ci = col[w];
-            const float gyz = d == 1 ? ci.gy : ci.gz;
+            const int to = gq >> 1, e = gq & 1;
             const float2* vt = in + to * TS + w;
             float2 a[N1];
 #pragma unroll
             for (int i = 0; i < N1; ++i) {
                 const int ix = N2 * i + n2;
                 const float2 v = vt[fx.pos(ix) * W];
-                const float gd = d == 0 ? (ix == N / 2 ? 0.0f : (ix <= N / 2 ? ix : ix - N) * kf0) : gyz;
-                a[i] = make_float2(gd * v.y, -gd * v.x);
+                const float gx = ix == N / 2 ? 0.0f : (ix <= N / 2 ? ix : ix - N) * kf0;
+                a[i] = e ? v : make_float2(gx * v.y, -gx * v.x);
             }
             reg_fft<N1, true>(a);
             if (N2 > 1) {
@@ -328,14 +330,14 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
 
 // PIC_Spectral variant of pass B (hymd/field.py:241-403, the library path's
 // k_kspace_pic): one charge-density column set in, psi = 4 pi f H rho / k^2
-// (k^2 = 1 at k = 0) and the field components -i k'_d psi out, at grids
-// 1..3 of the output (psi at grid 0 only when want_psi); sum of
+// (k^2 = 1 at k = 0) out as -i k'_x psi (grid 0) and psi (grid 1), pass C
+// forming psi and the field components -i k'_d psi from them; sum of
 // w_k rho(k).psi(k) over the half spectrum into sums[0].
 template <int N>
 __global__ void __launch_bounds__(kSpecThreads, 2)
     k_spec_kspace_pic(const float2* __restrict__ rho, float2* __restrict__ out_spec, SpecGeom g,
                       const BoxState* __restrict__ bs, const Functional* __restrict__ fun,
-                      float four_pi_fac, int want_psi, const float2* __restrict__ tw,
+                      float four_pi_fac, const float2* __restrict__ tw,
                       double* sums, double* partials, unsigned int* ticket) {
     extern __shared__ __align__(16) float2 sm[];
     __shared__ ColInfo col[16];
@@ -343,15 +345,14 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     const int64_t plane = (int64_t)g.n1 * g.nzc;
     const int j0 = blockIdx.x * W;
     float2* in = sm;        // [Nx][W]
-    float2* out = sm + TS;  // [4][Nx][W]: psi, E_x, E_y, E_z
+    float2* out = sm + TS;  // [2][Nx][W]: -i g_x psi, psi
     tile_columns(col, g, j0, bs);
     const FftIdx fx = fft_idx(N);
     const float kf0 = bs->kf[0];
     const float invM = (float)bs->inv_M;
     const float s2h = fun->sigma2_half;
-    const int first = want_psi ? 0 : 1;
     float acc[1] = {0.0f};
-    const int cout = (4 - first) * W;
+    const int cout = 2 * W;
     const float inv_w = 1.0f / (float)W, inv_cout = 1.0f / (float)cout;
     {
         constexpr int N1 = split1(N), N2 = N / N1;
@@ -365,16 +366,14 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
         auto ld2 = [&](int c, int p) { return in[p * W + c]; };
         fft_step2<N, false, true>(W, inv_w, ld2, fin);
         __syncthreads();
-        // item (grid d, w, n2), d from `first`: psi = 4 pi f H rho / k^2,
-        // E_d = -i g_d psi
+        // item (grid e, w, n2): psi = 4 pi f H rho / k^2; e = 0 -i g_x psi
+        // (E_x), e = 1 psi (psi, and E_y, E_z formed in pass C)
         const int items = cout * N2;
         for (int it = threadIdx.x; it < items; it += blockDim.x) {
             const int n2 = N2 == 1 ? 0 : div_inv(it, cout, inv_cout);
             const int c = it - n2 * cout;
-            const int gq = c >> ws, w = c & (W - 1);
-            const int d = gq + first;
+            const int e = c >> ws, w = c & (W - 1);
             const ColInfo ci = col[w];
-            const float gyz = d == 2 ? ci.gy : ci.gz;
             float2 a[N1];
 #pragma unroll
             for (int i = 0; i < N1; ++i) {
@@ -387,14 +386,10 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                 const float2 rq = make_float2(r.x * invM, r.y * invM);
                 const float sc = four_pi_fac * Hk / k2;
                 const float2 v = make_float2(rq.x * sc, rq.y * sc);
-                if (sums && d == first)
+                if (sums && e == 0)
                     acc[0] = fmaf(ci.wk, fmaf(rq.x, v.x, rq.y * v.y), acc[0]);
-                if (d == 0) {
-                    a[i] = v;
-                } else {
-                    const float gd = d == 1 ? (ix == N / 2 ? 0.0f : kx) : gyz;
-                    a[i] = make_float2(gd * v.y, -gd * v.x);
-                }
+                const float gx = ix == N / 2 ? 0.0f : kx;
+                a[i] = e ? v : make_float2(gx * v.y, -gx * v.x);
             }
             reg_fft<N1, true>(a);
             if (N2 > 1) {
@@ -405,19 +400,19 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                 }
             }
 #pragma unroll
-            for (int k1 = 0; k1 < N1; ++k1) out[gq * TS + (N2 * k1 + n2) * W + w] = a[k1];
+            for (int k1 = 0; k1 < N1; ++k1) out[e * TS + (N2 * k1 + n2) * W + w] = a[k1];
         }
         __syncthreads();
-        auto at_out = [&](int c, int e) -> float2& { return out[(c >> ws) * TS + e * W + (c & (W - 1))]; };
+        auto at_out = [&](int c, int q) -> float2& { return out[(c >> ws) * TS + q * W + (c & (W - 1))]; };
         auto ldo = [&](int c, int p) { return at_out(c, p); };
         auto fino = [&](int c, int xx, int p, float2 v2) {
-            out_spec[(int64_t)((c >> ws) + first) * g.Mc + xx * plane + j0 + (c & (W - 1))] = v2;
+            out_spec[(int64_t)(c >> ws) * g.Mc + xx * plane + j0 + (c & (W - 1))] = v2;
         };
         if (N2 > 1) {
             fft_step2<N, true, true>(cout, inv_cout, ldo, fino);
         } else {
-            for (int e = threadIdx.x; e < cout * N; e += blockDim.x) {
-                const int xx = div_inv(e, cout, inv_cout), c = e - xx * cout;
+            for (int q = threadIdx.x; q < cout * N; q += blockDim.x) {
+                const int xx = div_inv(q, cout, inv_cout), c = q - xx * cout;
                 fino(c, xx, xx, at_out(c, xx));
             }
         }
@@ -435,10 +430,15 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
 // the packing is computed in the z transform's first step (rows handled by
 // one warp each, since X[m] and X[h-m] are overwritten in place) and its
 // second step writes the real plane.
+// Output grid gi (density: 3 t + d; PIC: psi, E_x, E_y, E_z) comes from
+// pass B's grid src: -i g_x v (x force) as is, v times -i g_y (a function
+// of the row ky) or -i g_z (of the column kz) for the y and z forces, v as
+// is for psi.
 template <int NY, int HZ>
 __global__ void __launch_bounds__(kSpecThreads, 2)
     k_spec_inv(const float2* __restrict__ spec, float* __restrict__ grid, SpecGeom g,
-               const float2* __restrict__ tw, int first) {
+               const BoxState* __restrict__ bs, const float2* __restrict__ tw, int first,
+               int pic) {
     extern __shared__ __align__(16) float2 sm[];
     constexpr int Ny = NY, H = HZ, Nzc = H + 1, Ls = plane_ls(H), PZ = plane_pz(H);
     constexpr int step = kTableN / (2 * H);
@@ -446,15 +446,37 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const FftIdx fy = fft_idx(Ny);
     auto zs = [](int e) { return e + (e >> PZ); };
-    const float2* in = spec + (int64_t)gi * g.Mc + (int64_t)x * Ny * Nzc;
+    int src, mul;  // mul: 0 none, 1 -i g_y, 2 -i g_z
+    if (pic) {
+        src = gi == 1 ? 0 : 1;
+        mul = gi == 2 ? 1 : (gi == 3 ? 2 : 0);
+    } else {
+        const int t = gi / 3, d = gi - 3 * t;
+        src = 2 * t + (d > 0);
+        mul = d;
+    }
+    const float kf1 = bs->kf[1], kf2 = bs->kf[2];
+    const float2* in = spec + (int64_t)src * g.Mc + (int64_t)x * Ny * Nzc;
     float2* out = reinterpret_cast<float2*>(grid + ((int64_t)gi * g.n0 + x) * Ny * (2 * H));
     constexpr float inv_rows = 1.0f / (float)Ny, inv_cols = 1.0f / (float)Nzc;
     {
         // y: rows left at FftIdx positions of y
         auto ld = [&](int c, int n) { return __ldg(in + n * Nzc + c); };
+        auto pre = [&](int c, int n2, auto& a) {
+            constexpr int N1 = split1(Ny), N2 = Ny / N1;
+            if (mul == 0) return;
+#pragma unroll
+            for (int i = 0; i < N1; ++i) {
+                const int n = N2 * i + n2;
+                const float gd = mul == 1
+                                     ? (n == Ny / 2 ? 0.0f : (n <= Ny / 2 ? n : n - Ny) * kf1)
+                                     : (c == H ? 0.0f : c * kf2);
+                a[i] = make_float2(gd * a[i].y, -gd * a[i].x);
+            }
+        };
         auto st = [&](int c, int p, float2 v) { sm[p * Ls + c] = v; };
         auto fin = [&](int c, int k, int p, float2 v) { sm[p * Ls + c] = v; };
-        fft_step1<Ny, true, true>(Nzc, inv_cols, ld, st, fin, tw);
+        fft_step1<Ny, true, true>(Nzc, inv_cols, ld, st, fin, tw, pre);
         __syncthreads();
         auto ld2 = [&](int c, int p) { return sm[p * Ls + c]; };
         fft_step2<Ny, true, true>(Nzc, inv_cols, ld2, fin);
@@ -564,10 +586,10 @@ int with_planes(int n1, int h, F f) {
 #undef HPF_PLANE
     return HPF_ERR_ARG;
 }
-// a k-space tile: T density blocks in + 3T force blocks out, or 1 charge
-// block in + 4 out (PIC)
+// a k-space tile: T density blocks in + 2T out, or 1 charge block in + 2
+// out (PIC)
 size_t tile_smem(const hpf_ctx* c, int W) {
-    const int blocks = 4 * c->T > 5 ? 4 * c->T : 5;
+    const int blocks = 3 * c->T;
     return sizeof(float2) * (size_t)blocks * (c->n0 * W + tile_pad(W));
 }
 
@@ -655,7 +677,8 @@ int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cuda
     if (r != HPF_OK) return r;
     HPF_LAUNCH_CHECK();
     with_planes(c->n1, c->n2 / 2, [&](auto, auto ki) {
-        ki<<<dim3(c->n0, 3 * c->T), kSpecThreads, ps, st>>>(c->d_spec, c->d_grid, g, c->d_tw, 0);
+        ki<<<dim3(c->n0, 3 * c->T), kSpecThreads, ps, st>>>(c->d_spec, c->d_grid, g, c->d_box,
+                                                             c->d_tw, 0, 0);
         return HPF_OK;
     });
     HPF_LAUNCH_CHECK();
@@ -679,16 +702,16 @@ int spectral_pic(hpf_ctx* c, float four_pi_fac, bool want_psi, double* sums, cud
     unsigned int* tick = reinterpret_cast<unsigned int*>(c->d_spec_ws + 4 * (size_t)c->spec_tiles);
     int r = with_kspace(c->n0, [&](auto, auto kp) {
         kp<<<c->spec_tiles, kSpecThreads, ts, st>>>(c->d_spec_phi, c->d_spec, g, c->d_box,
-                                                    c->d_fun, four_pi_fac, want_psi ? 1 : 0,
-                                                    c->d_tw, sums, part, tick);
+                                                    c->d_fun, four_pi_fac, c->d_tw, sums, part,
+                                                    tick);
         return HPF_OK;
     });
     if (r != HPF_OK) return r;
     HPF_LAUNCH_CHECK();
     const int first = want_psi ? 0 : 1;
     with_planes(c->n1, c->n2 / 2, [&](auto, auto ki) {
-        ki<<<dim3(c->n0, 4 - first), kSpecThreads, ps, st>>>(c->d_spec, c->d_grid, g, c->d_tw,
-                                                             first);
+        ki<<<dim3(c->n0, 4 - first), kSpecThreads, ps, st>>>(c->d_spec, c->d_grid, g, c->d_box,
+                                                             c->d_tw, first, 1);
         return HPF_OK;
     });
     HPF_LAUNCH_CHECK();
