@@ -277,13 +277,18 @@ __global__ void k_kspace_sums(const float2* __restrict__ phi_f, const float2* __
 }
 
 // ---------------------------------------------------------------- readout ---
-// Kick fused into the readout (MODE 1); with a thermostat the CSVR velocity
-// sums follow in a separate streaming pass (launch_csvr_sums).
+// Kick fused into the readout (MODE 1), plus CSVR velocity sums (MODE 2).
 struct KickDev {
     float* v;
     const float* prev[4];
     int n_prev;
     float mass, h;
+    HpfCsvrArgs a;
+    const int32_t* group;
+    const double* randoms;
+    int* counter;
+    double* state;
+    double* ws;
 };
 
 template <int MODE>
@@ -291,6 +296,7 @@ __global__ void k_readout(const float* __restrict__ fm, const float* __restrict_
                           const int32_t* __restrict__ types, const float* __restrict__ charges,
                           int64_t n, int T, int64_t M, const BoxState* __restrict__ bs,
                           float* __restrict__ force, int* err, KickDev kd) {
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
@@ -336,16 +342,31 @@ __global__ void k_readout(const float* __restrict__ fm, const float* __restrict_
         force[3 * i] = out[0];
         force[3 * i + 1] = out[1];
         force[3 * i + 2] = out[2];
-        if (MODE == 1) {
+        if (MODE >= 1) {
             // v += 0.5 dt_o F_q / m for the earlier slow forces, then this one
+            float w[3];
             for (int d = 0; d < 3; ++d) {
                 float x = kd.v[3 * i + d];
                 for (int q2 = 0; q2 < kd.n_prev; ++q2)
                     x = x + kd.h * (kd.prev[q2][3 * i + d] / kd.mass);
                 x = x + kd.h * (out[d] / kd.mass);
                 kd.v[3 * i + d] = x;
+                w[d] = x;
+            }
+            if (MODE == 2) {
+                const int g = kd.group ? kd.group[i] : 0;
+                if (g == 0 || g == 1) {
+                    acc[4 * g + 0] += w[0];
+                    acc[4 * g + 1] += w[1];
+                    acc[4 * g + 2] += w[2];
+                    acc[4 * g + 3] += fmaf(w[0], w[0], fmaf(w[1], w[1], w[2] * w[2]));
+                }
             }
         }
+    }
+    if (MODE == 2) {
+        if (grid_reduce_store_f<8>(acc, ws_partials(kd.ws), ws_ticket(kd.ws), kd.ws))
+            csvr_update(kd.a, kd.ws, kd.randoms, kd.counter, kd.state, err);
     }
 }
 
@@ -785,6 +806,12 @@ int launch_readout(hpf_ctx* c, const float* fm, const float* pos, const int32_t*
             if (!kick->randoms || !kick->counter || !kick->state || !kick->ws ||
                 a.n_groups < 1 || a.n_groups > 2 || (a.n_groups > 1 && !kick->group))
                 return HPF_ERR_ARG;
+            kd.a = a;
+            kd.group = kick->group;
+            kd.randoms = kick->randoms;
+            kd.counter = kick->counter;
+            kd.state = kick->state;
+            kd.ws = kick->ws;
             mode = 2;
         }
     }
@@ -796,19 +823,10 @@ int launch_readout(hpf_ctx* c, const float* fm, const float* pos, const int32_t*
         k_readout<1><<<grid_for(n, kThreads), kThreads, 0, st>>>(fm, pos, types, charges, n, T,
                                                                  c->M, c->d_box, force, c->d_err,
                                                                  kd);
-    else {
-        // kick in the gather (one bead per thread), then the CSVR velocity
-        // sums and scale factors in a streaming pass over v: the sums inside
-        // the gather would cap its grid at the partials' capacity and leave
-        // it latency-bound
-        k_readout<1><<<grid_for(n, kThreads), kThreads, 0, st>>>(fm, pos, types, charges, n, T,
-                                                                 c->M, c->d_box, force, c->d_err,
-                                                                 kd);
-        HPF_LAUNCH_CHECK();
-        return launch_csvr_sums(kick->v, kick->group, n, *kick->thermo, kick->randoms,
-                                kick->counter, kick->state, kick->ws,
-                                kick->d_err ? kick->d_err : c->d_err, st);
-    }
+    else
+        k_readout<2><<<reduce_grid(n, kThreads), kThreads, 0, st>>>(
+            fm, pos, types, charges, n, T, c->M, c->d_box, force,
+            kick->d_err ? kick->d_err : c->d_err, kd);
     HPF_LAUNCH_CHECK();
     return HPF_OK;
 }

@@ -100,11 +100,6 @@ int spectral_setup(hpf_ctx* c);
 int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cudaStream_t st);
 int spectral_pic(hpf_ctx* c, float four_pi_fac, bool want_psi, double* sums, cudaStream_t st);
 
-// CSVR per-group velocity sums and scale factors (no kick), hpf_md.cu.
-int launch_csvr_sums(float* v, const int32_t* group, int64_t n, const HpfCsvrArgs& a,
-                     const double* randoms, int* counter, double* state, double* ws, int* err,
-                     cudaStream_t st);
-
 #define HPF_REDUCE_GRID 304  // blocks of a reduction kernel (2 per SM on 152 SMs)
 
 // Layout of a reduction workspace (see HPF_OUT_DOUBLES in the C ABI header).
@@ -340,10 +335,14 @@ __device__ __forceinline__ void grid_coord(float x, float ih_hi, float ih_lo, in
 // Warp + block reduction of K doubles; thread 0 returns the block totals.
 template <int K>
 __device__ __forceinline__ void block_reduce(double (&v)[K], double* smem /* K*32 */) {
+    // the K shuffle trees advance level by level together (latencies overlap)
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
+    for (int o = 16; o > 0; o >>= 1) {
+        double t[K];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        for (int k = 0; k < K; ++k) t[k] = __shfl_down_sync(0xffffffffu, v[k], o);
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] += t[k];
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (blockDim.x + 31) >> 5;
@@ -354,11 +353,14 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double* smem /* K*3
     __syncthreads();
     if (warp == 0) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            double x = lane < nw ? smem[k * 32 + lane] : 0.0;
+        for (int k = 0; k < K; ++k) v[k] = lane < nw ? smem[k * 32 + lane] : 0.0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-            v[k] = x;
+        for (int o = 16; o > 0; o >>= 1) {
+            double t[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) t[k] = __shfl_down_sync(0xffffffffu, v[k], o);
+#pragma unroll
+            for (int k = 0; k < K; ++k) v[k] += t[k];
         }
     }
 }
@@ -383,6 +385,21 @@ __device__ __forceinline__ DF df_shfl_down(DF v, int o) {
     return DF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
 }
 
+// Warp sum of K double-float values (shuffle tree, lane 0 holds the sums).
+// The K trees advance level by level together, so their latencies overlap;
+// each value's summation order is the fixed tree order.
+template <int K>
+__device__ __forceinline__ void warp_df_reduce(DF (&v)[K]) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        DF t[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) t[k] = df_shfl_down(v[k], o);
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = df_add(v[k], t[k]);
+    }
+}
+
 // Block sum of K float values in double-float (TwoSum) arithmetic, written
 // value-major as partials[k * G + blockIdx.x] (float2 hi/lo); G = number of
 // partial slots per value (the grid size).  All threads must call it.
@@ -391,24 +408,28 @@ __device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partial
     __shared__ float2 red_p[K * 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (blockDim.x + 31) >> 5;
+    DF v[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        DF v{vf[k], 0.0f};
+    for (int k = 0; k < K; ++k) v[k] = DF{vf[k], 0.0f};
+    warp_df_reduce<K>(v);
+    if (lane == 0) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = df_add(v, df_shfl_down(v, o));
-        if (lane == 0) red_p[k * 32 + warp] = make_float2(v.hi, v.lo);
+        for (int k = 0; k < K; ++k) red_p[k * 32 + warp] = make_float2(v[k].hi, v[k].lo);
     }
     __syncthreads();
     float2* part = reinterpret_cast<float2*>(partials);
     if (warp == 0) {
+        DF t[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const float2 x = lane < nw ? red_p[k * 32 + lane] : make_float2(0.0f, 0.0f);
-            DF t{x.x, x.y};
+            t[k] = DF{x.x, x.y};
+        }
+        warp_df_reduce<K>(t);
+        // value-major: the final pass's loads of one value are coalesced
+        if (lane == 0) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t = df_add(t, df_shfl_down(t, o));
-            // value-major: the final pass's loads of one value are coalesced
-            if (lane == 0) part[(size_t)k * G + blockIdx.x] = make_float2(t.hi, t.lo);
+            for (int k = 0; k < K; ++k) part[(size_t)k * G + blockIdx.x] = make_float2(t[k].hi, t[k].lo);
         }
     }
 }
@@ -442,21 +463,23 @@ __device__ __forceinline__ void final_partials_f(const double* partials, unsigne
             acc[k] = df_add(acc[k], DF{x1[k].x, x1[k].y});
         }
     }
+    warp_df_reduce<K>(acc);
+    if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[k] = df_add(acc[k], df_shfl_down(acc[k], o));
-        if (lane == 0) red_f[k * 32 + warp] = make_float2(acc[k].hi, acc[k].lo);
+        for (int k = 0; k < K; ++k) red_f[k * 32 + warp] = make_float2(acc[k].hi, acc[k].lo);
     }
     __syncthreads();
     if (warp == 0) {
+        DF t[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const float2 x = lane < nw ? red_f[k * 32 + lane] : make_float2(0.0f, 0.0f);
-            DF t{x.x, x.y};
+            t[k] = DF{x.x, x.y};
+        }
+        warp_df_reduce<K>(t);
+        if (lane == 0) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t = df_add(t, df_shfl_down(t, o));
-            if (lane == 0) out[k] = (double)t.hi + (double)t.lo;
+            for (int k = 0; k < K; ++k) out[k] = (double)t[k].hi + (double)t[k].lo;
         }
     }
 }

@@ -244,21 +244,6 @@ int hpf_csvr(float* v, const int32_t* group, int64_t n, const float* const* kick
     return HPF_OK;
 }
 
-}  // extern "C"
-
-int launch_csvr_sums(float* v, const int32_t* group, int64_t n, const HpfCsvrArgs& a,
-                     const double* randoms, int* counter, double* state, double* ws, int* err,
-                     cudaStream_t st) {
-    ForceList fl;
-    fl.n = 0;
-    k_csvr_sums_alpha<<<reduce_grid_md(n), kThreads, 0, st>>>(v, group, n, fl, 0.0f, ws, a,
-                                                              randoms, counter, state, err);
-    HPF_LAUNCH_CHECK();
-    return HPF_OK;
-}
-
-extern "C" {
-
 int hpf_csvr_scale(float* v, const int32_t* group, int64_t n, const double* state,
                    int remove_com, void* stream) {
     if (!v || !state || n < 0) return HPF_ERR_ARG;
