@@ -360,10 +360,6 @@ __device__ __forceinline__ void free_beads(const hpf_respa_plan& p, int fblock, 
     }
 }
 
-__device__ __forceinline__ void scr_epilogue(const BaroFuse& f, const double* out, int* err) {
-    scr_update(f.a, out[9], f.field, out, f.randoms, f.counter, f.bs, f.fun, f.state, err);
-}
-
 template <bool DIH>
 __global__ void __launch_bounds__(kThreads)
 k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
@@ -413,11 +409,74 @@ k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
 // barostat when coupled.  A separate one-block launch: a last-block reduction
 // inside the main kernel (fence + ticket on every block, then a serial pass
 // at the end) cost more than this launch.
-__global__ void __launch_bounds__(256)
+//
+// The pass is one latency chain, so it is kept short: every thread loads all
+// its partials before adding (up to kFinishRounds x 256 blocks in one round
+// trip), the sums stay in shared memory for the barostat, and one warp
+// fetches the barostat's inputs into L1 while the partials are summed.
+constexpr int kFinishThreads = 256;
+constexpr int kFinishRounds = 6;
+
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+__global__ void __launch_bounds__(kFinishThreads)
 k_respa_finish(const double* __restrict__ partials, unsigned int G, double* out, BaroFuse baro,
                int* err) {
-    final_partials_f<kOut>(partials, G, out);
-    if (threadIdx.x == 0 && baro.on) scr_epilogue(baro, out, err);
+    __shared__ double res[kOut];
+    __shared__ float2 red[kOut * 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (baro.on && threadIdx.x == 32) {
+        const int s = *baro.counter;
+        prefetch_l1(baro.field);
+        prefetch_l1(baro.bs);
+        prefetch_l1(reinterpret_cast<const char*>(baro.bs) + 128);
+        prefetch_l1(&baro.fun->c);
+        if (s >= 0 && s < baro.a.n_steps) prefetch_l1(baro.randoms + (int64_t)s * baro.a.stride);
+    }
+    const float2* part = reinterpret_cast<const float2*>(partials);
+    DF acc[kOut];
+#pragma unroll
+    for (int k = 0; k < kOut; ++k) acc[k] = DF{0.0f, 0.0f};
+    for (unsigned int b0 = threadIdx.x; b0 < G; b0 += kFinishRounds * kFinishThreads) {
+        float2 x[kFinishRounds][kOut];
+#pragma unroll
+        for (int u = 0; u < kFinishRounds; ++u) {
+            const unsigned int b = b0 + u * kFinishThreads;
+#pragma unroll
+            for (int k = 0; k < kOut; ++k)
+                x[u][k] = b < G ? __ldcg(part + (size_t)k * G + b) : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < kFinishRounds; ++u)
+#pragma unroll
+            for (int k = 0; k < kOut; ++k) acc[k] = df_add(acc[k], DF{x[u][k].x, x[u][k].y});
+    }
+    warp_df_reduce<kOut>(acc);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < kOut; ++k) red[k * 32 + warp] = make_float2(acc[k].hi, acc[k].lo);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        DF t[kOut];
+#pragma unroll
+        for (int k = 0; k < kOut; ++k) {
+            const float2 x = lane < kFinishThreads / 32 ? red[k * 32 + lane] : make_float2(0.0f, 0.0f);
+            t[k] = DF{x.x, x.y};
+        }
+        warp_df_reduce<kOut>(t);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < kOut; ++k) res[k] = (double)t[k].hi + (double)t[k].lo;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < kOut) out[threadIdx.x] = res[threadIdx.x];
+    if (threadIdx.x == 0 && baro.on)
+        scr_update(baro.a, res[9], baro.field, res, baro.randoms, baro.counter, baro.bs, baro.fun,
+                   baro.state, err);
 }
 
 // ------------------------------------------------------------- planner ---
@@ -734,7 +793,7 @@ int hpf_respa_step(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
 #undef HPF_RESPA
     HPF_LAUNCH_CHECK();
     if (out) {
-        k_respa_finish<<<1, 256, 0, st>>>(p->partials, (unsigned int)grid, out, bf, d_err);
+        k_respa_finish<<<1, kFinishThreads, 0, st>>>(p->partials, (unsigned int)grid, out, bf, d_err);
         HPF_LAUNCH_CHECK();
     }
     return HPF_OK;
@@ -765,7 +824,7 @@ int hpf_respa_forces(hpf_respa_plan* p, const float* r, float* f_bonded, const d
     if (out) {
         BaroFuse none;
         memset(&none, 0, sizeof(none));
-        k_respa_finish<<<1, 256, 0, st>>>(p->partials, (unsigned int)grid, out, none, d_err);
+        k_respa_finish<<<1, kFinishThreads, 0, st>>>(p->partials, (unsigned int)grid, out, none, d_err);
         HPF_LAUNCH_CHECK();
     }
     return HPF_OK;
