@@ -1,19 +1,20 @@
-// Shared-memory FFTs for power-of-two lengths 2..256, used by the fused
-// spectral passes (hpf_spectral.cu).
+// Shared-memory FFTs for lengths 2^a and 3 * 2^a up to 256, used by the
+// fused spectral passes (hpf_spectral.cu).
 //
-// A batch of 1-D transforms over float2 data in shared memory is done in two
-// steps (the four-step method, N = N1 * N2): N2 transforms of length N1 over
-// the elements n = N2*n1 + n2 in registers, a twiddle w_N^(n2 k1), then N1
-// transforms of length N2 over contiguous runs, again in registers.  The
-// result is left in place in digit-transposed order: frequency k = k1 + N1*k2
-// sits at element N2*k1 + k2 (FftIdx::pos below), so no reordering pass or
-// extra buffer is needed; the callers read through the index maps.
+// A batch of 1-D transforms is done in two steps (the four-step method,
+// N = N1 * N2): N2 transforms of length N1 over the elements n = N2*n1 + n2
+// in registers, a twiddle w_N^(n2 k1), then N1 transforms of length N2 over
+// contiguous runs, again in registers.  The result is left in
+// digit-transposed order: frequency k = k1 + N1*k2 sits at element N2*k1 + k2
+// (Idx<N>::pos below), so no reordering pass or extra buffer is needed; the
+// callers read through the index maps.
 //
 // Sign convention as cuFFT / FFTW: forward exp(-2 pi i k n / N), inverse
-// exp(+2 pi i k n / N), both unnormalised.  The in-register radix-2 stages use
-// the exact values of cos and sin at multiples of 2 pi / 16; the twiddles of
-// the middle step come from a table exp(-2 pi i m / 512) computed on the host
-// in double precision.
+// exp(+2 pi i k n / N), both unnormalised.  The in-register transforms are
+// radix 2 with the exact cos and sin of multiples of 2 pi / 16, and for
+// lengths 3, 6, 12 one radix-3 stage (cos and sin of multiples of 2 pi / 12).
+// The twiddles of the middle step come from tables exp(-2 pi i m / 512) and
+// exp(-2 pi i m / 768) computed on the host in double precision.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -21,7 +22,24 @@
 
 namespace hpf_fft {
 
-constexpr int kTableN = 512;  // twiddle table length: exp(-2 pi i m / 512)
+// twiddle tables, back to back: exp(-2 pi i m / 512), m < 512, then
+// exp(-2 pi i m / 768), m < 768
+constexpr int kTable2 = 512;
+constexpr int kTable3 = 768;
+constexpr int kTableTotal = kTable2 + kTable3;
+
+__host__ __device__ constexpr bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+// 2^a or 3 * 2^a
+__host__ __device__ constexpr bool fft_len_ok(int n) {
+    return is_pow2(n) || (n % 3 == 0 && is_pow2(n / 3));
+}
+
+// Twiddle m of length N: tw[Tw<N>::off + m * Tw<N>::stride].
+template <int N>
+struct Tw {
+    static constexpr int off = is_pow2(N) ? 0 : kTable2;
+    static constexpr int stride = (is_pow2(N) ? kTable2 : kTable3) / N;
+};
 
 // (loops, not recursion, so that they fold to constants once the callers'
 // loops are unrolled)
@@ -35,10 +53,12 @@ __host__ __device__ __forceinline__ constexpr int bitrev(int i, int bits) {
     for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
     return r;
 }
-// first-step length N1 of the split N = N1 * N2 (N1 <= 16, N2 <= 16; N1 = 8
-// from 32 to 128 keeps the per-thread arrays of the first step short)
+// first-step length N1 of the split N = N1 * N2.  Powers of two: N1 = 8
+// from 32 to 128, which keeps the per-thread arrays of the first step short.
+// 3 * 2^a above 16: N1 the power of two (8 or 16), N2 = 3, 6 or 12.
 __host__ __device__ constexpr int split1(int n) {
-    return n <= 16 ? n : (n <= 128 ? 8 : 16);
+    return n <= 16 ? n
+                   : (is_pow2(n) ? (n <= 128 ? 8 : 16) : (n % 16 == 0 ? 16 : 8));
 }
 
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) {
@@ -73,10 +93,49 @@ __device__ __forceinline__ float2 rot16(float2 v, int m) {
     return c_mul(v, make_float2(cr, INV ? si : -si));
 }
 
-// In-register radix-2 transform of length R <= 16, natural order in and out.
+// v * exp(-+2 pi i m / 12) for m = 0..11 (compile-time after unrolling).
+template <bool INV>
+__device__ __forceinline__ float2 rot12(float2 v, int m) {
+    constexpr float s3 = 0.86602540378443864676f;  // sqrt(3)/2
+    switch (m) {
+        case 0: return v;
+        case 3: return INV ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
+        case 6: return make_float2(-v.x, -v.y);
+        case 9: return INV ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
+        default: break;
+    }
+    float cr, si;  // cos(2 pi m/12), sin(2 pi m/12)
+    switch (m) {
+        case 1: cr = s3; si = 0.5f; break;
+        case 2: cr = 0.5f; si = s3; break;
+        case 4: cr = -0.5f; si = s3; break;
+        case 5: cr = -s3; si = 0.5f; break;
+        case 7: cr = -s3; si = -0.5f; break;
+        case 8: cr = -0.5f; si = -s3; break;
+        case 10: cr = 0.5f; si = -s3; break;
+        default: cr = s3; si = -0.5f; break;  // m == 11
+    }
+    return c_mul(v, make_float2(cr, INV ? si : -si));
+}
+
+// Length-3 transform in place.
+template <bool INV>
+__device__ __forceinline__ void dft3(float2& b0, float2& b1, float2& b2) {
+    constexpr float s3 = 0.86602540378443864676f;
+    const float2 s = c_add(b1, b2), d = c_sub(b1, b2);
+    const float2 t = make_float2(fmaf(-0.5f, s.x, b0.x), fmaf(-0.5f, s.y, b0.y));
+    // -+i (sqrt(3)/2) d
+    const float2 m = INV ? make_float2(-s3 * d.y, s3 * d.x) : make_float2(s3 * d.y, -s3 * d.x);
+    b0 = c_add(b0, s);
+    b1 = c_add(t, m);
+    b2 = c_sub(t, m);
+}
+
+// In-register radix-2 transform of length R = 2^a <= 16, natural order in
+// and out.
 template <int R, bool INV>
-__device__ __forceinline__ void reg_fft(float2 (&a)[R]) {
-    static_assert(R >= 1 && R <= 16 && (R & (R - 1)) == 0, "register FFT length");
+__device__ __forceinline__ void reg_fft2(float2 (&a)[R]) {
+    static_assert(R >= 1 && R <= 16 && is_pow2(R), "register FFT length");
     constexpr int bits = ilog2(R);
     float2 b[R];
 #pragma unroll
@@ -98,24 +157,42 @@ __device__ __forceinline__ void reg_fft(float2 (&a)[R]) {
     for (int i = 0; i < R; ++i) a[i] = b[i];
 }
 
-// Index maps of a length-n transform's digit-transposed order, as shifts
-// and masks (n a power of two <= 256): pos(k) is the element holding
-// frequency k, freq(p) the frequency held by element p.
-struct FftIdx {
-    int n1s, n1m, n2s, n2m;
-    __device__ __forceinline__ int pos(int k) const { return ((k & n1m) << n2s) + (k >> n1s); }
-    __device__ __forceinline__ int freq(int p) const { return (p >> n2s) + ((p & n2m) << n1s); }
-};
-__device__ __forceinline__ FftIdx fft_idx(int n) {
-    const int s = 31 - __clz(n);
-    const int s1 = n <= 16 ? s : (n <= 128 ? 3 : 4);
-    FftIdx f;
-    f.n1s = s1;
-    f.n1m = (1 << s1) - 1;
-    f.n2s = s - s1;
-    f.n2m = (1 << (s - s1)) - 1;
-    return f;
+// In-register transform of length R in {1, 2, 4, 8, 16, 3, 6, 12}: for
+// R = 3P, a length-3 transform over n1 of x[P n1 + n2] for each n2, the
+// twiddle w_R^(n2 k1), then length-P transforms over n2: X[k1 + 3 k2].
+template <int R, bool INV>
+__device__ __forceinline__ void reg_fft(float2 (&a)[R]) {
+    if constexpr (R % 3 != 0) {
+        reg_fft2<R, INV>(a);
+    } else {
+        constexpr int P = R / 3;
+        static_assert(P == 1 || P == 2 || P == 4, "register FFT length");
+        float2 y[3][P];
+#pragma unroll
+        for (int n2 = 0; n2 < P; ++n2) {
+            float2 b0 = a[n2], b1 = a[P + n2], b2 = a[2 * P + n2];
+            dft3<INV>(b0, b1, b2);
+            y[0][n2] = b0;
+            y[1][n2] = rot12<INV>(b1, (n2 * (12 / R)) % 12);
+            y[2][n2] = rot12<INV>(b2, (2 * n2 * (12 / R)) % 12);
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < 3; ++k1) {
+            reg_fft2<P, INV>(y[k1]);
+#pragma unroll
+            for (int k2 = 0; k2 < P; ++k2) a[k1 + 3 * k2] = y[k1][k2];
+        }
+    }
 }
+
+// Index maps of a length-N transform's digit-transposed order: pos(k) is
+// the element holding frequency k, freq(p) the frequency held by element p.
+template <int N>
+struct Idx {
+    static constexpr int N1 = split1(N), N2 = N / N1;
+    __device__ __forceinline__ static int pos(int k) { return N2 * (k % N1) + k / N1; }
+    __device__ __forceinline__ static int freq(int p) { return p / N2 + N1 * (p % N2); }
+};
 
 // n / d for 0 <= n < 2^22 and a block-invariant d >= 1 (inv = 1.0f / d):
 // the float quotient is within one of the truth, one correction step.
@@ -125,28 +202,6 @@ __device__ __forceinline__ int div_inv(int n, int d, float inv) {
     if (r >= d) ++q;
     else if (r < 0) --q;
     return q;
-}
-
-// Layout of a batch of transforms in shared memory: transform c (of count)
-// starts at (c >> inner_shift) * s_outer + (c & inner_mask) * s_inner and
-// its elements are es apart.
-struct Batch {
-    int count, inner_shift, s_outer, s_inner, es;
-    float inv_count;
-    __device__ __forceinline__ int base(int c) const {
-        return (c >> inner_shift) * s_outer + (c & ((1 << inner_shift) - 1)) * s_inner;
-    }
-};
-__device__ __forceinline__ Batch make_batch(int count, int inner_shift, int s_outer, int s_inner,
-                                            int es) {
-    Batch b;
-    b.count = count;
-    b.inner_shift = inner_shift;
-    b.s_outer = s_outer;
-    b.s_inner = s_inner;
-    b.es = es;
-    b.inv_count = 1.0f / (float)count;
-    return b;
 }
 
 // Two-step transforms with caller-supplied element access, so that the
@@ -164,11 +219,6 @@ __device__ __forceinline__ Batch make_batch(int count, int inner_shift, int s_ou
 // position it came from.
 // CFAST: neighbouring threads take neighbouring transforms c (for layouts
 // where c is the unit stride); else neighbouring elements of one transform.
-template <int V>
-struct IntC {
-    static constexpr int value = V;
-};
-
 struct NoPre {
     template <int R>
     __device__ __forceinline__ void operator()(int, int, float2 (&)[R]) const {}
@@ -181,7 +231,6 @@ template <int N, bool INV, bool CFAST, class LD, class ST, class FIN, class PRE 
 __device__ __forceinline__ void fft_step1(int count, float inv_count, LD ld, ST st, FIN fin,
                                           const float2* __restrict__ tw, PRE pre = PRE()) {
     constexpr int N1 = split1(N), N2 = N / N1;
-    constexpr int TW = kTableN / N;
     const int items = count * N2;
     for (int it = threadIdx.x; it < items; it += blockDim.x) {
         int c, n2;
@@ -203,7 +252,7 @@ __device__ __forceinline__ void fft_step1(int count, float inv_count, LD ld, ST 
         } else {
 #pragma unroll
             for (int k1 = 1; k1 < N1; ++k1) {
-                float2 w = __ldg(tw + n2 * k1 * TW);
+                float2 w = __ldg(tw + Tw<N>::off + n2 * k1 * Tw<N>::stride);
                 if (INV) w.y = -w.y;
                 a[k1] = c_mul(a[k1], w);
             }
@@ -234,86 +283,6 @@ __device__ __forceinline__ void fft_step2(int count, float inv_count, LD ld, FIN
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) fin(c, k1 + N1 * k2, N2 * k1 + k2, a[k2]);
     }
-}
-
-// Calls f(IntC<n>()) for a runtime power of two n in [4, 256].
-template <class F>
-__device__ __forceinline__ void with_len(int n, F f) {
-    switch (n) {
-        case 4: f(IntC<4>()); break;
-        case 8: f(IntC<8>()); break;
-        case 16: f(IntC<16>()); break;
-        case 32: f(IntC<32>()); break;
-        case 64: f(IntC<64>()); break;
-        case 128: f(IntC<128>()); break;
-        default: f(IntC<256>()); break;
-    }
-}
-
-// One batch of length-N transforms in shared memory, in place.  Transform c
-// starts at L.base(c), its elements L.es apart; the result is left at the
-// step-1 positions (FftIdx order).  All threads call it; the caller
-// synchronises before and after.
-template <int N, bool INV>
-__device__ __forceinline__ void smem_fft(float2* buf, const Batch& L, const float2* __restrict__ tw) {
-    auto at = [&](int c, int e) -> float2& { return buf[L.base(c) + e * L.es]; };
-    auto ld = [&](int c, int e) { return at(c, e); };
-    auto st = [&](int c, int p, float2 v) { at(c, p) = v; };
-    auto fin = [&](int c, int k, int p, float2 v) { at(c, p) = v; };
-    if (L.es == 1) {
-        fft_step1<N, INV, false>(L.count, L.inv_count, ld, st, fin, tw);
-        __syncthreads();
-        fft_step2<N, INV, true>(L.count, L.inv_count, ld, fin);
-    } else {
-        fft_step1<N, INV, true>(L.count, L.inv_count, ld, st, fin, tw);
-        __syncthreads();
-        fft_step2<N, INV, true>(L.count, L.inv_count, ld, fin);
-    }
-}
-
-template <bool INV>
-__device__ __forceinline__ void smem_fft_n(int n, float2* buf, const Batch& L,
-                                           const float2* __restrict__ tw) {
-    with_len(n, [&](auto nc) { smem_fft<decltype(nc)::value, INV>(buf, L, tw); });
-}
-
-// ---- bulk copies global -> shared (TMA, completion on an mbarrier) -------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-                 : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-// dst, src 16-byte aligned; bytes a multiple of 16
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
-                                         uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-        "[%3];" ::"r"(smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
-    return ok != 0;
-}
-// Bounded wait for phase `parity` (a bulk copy that never lands would
-// otherwise hang the block): false after ~2^22 polls (each try_wait itself
-// suspends for a while), with the caller then recording an error.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (int i = 0; i < (1 << 22); ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
 }
 
 }  // namespace hpf_fft

@@ -70,8 +70,8 @@ struct hpf_ctx {
     float2* gpe_spec;
     double* gpe_ws;
     double* gpe_host;
-    // fused spectral passes (power-of-two meshes): twiddle table
-    // exp(-2 pi i m / 512), k-space tile width, partial sums + ticket
+    // fused spectral passes: twiddle tables exp(-2 pi i m / 512) and
+    // exp(-2 pi i m / 768), k-space tile width, partial sums + ticket
     float2* d_tw;
     double* d_spec_ws;
     int spec_W, spec_tiles;

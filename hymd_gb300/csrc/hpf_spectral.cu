@@ -9,8 +9,9 @@
 // evaluated as in the library-FFT path (hpf_field.cu, k_kspace_force).
 //
 // Layouts are the library path's: real grids [g][x][y][z], half spectra
-// [g][x][y][kz] with kz in [0, n2/2].  For power-of-two meshes (n0 8..256,
-// n1 and n2 16..128; the plane kernels are instantiated per (n1, n2)):
+// [g][x][y][kz] with kz in [0, n2/2].  For meshes with n0 in {8..256 powers
+// of two, 24, 48, 96, 192} and (n1, n2) both powers of two in 16..128 or
+// both 24, 48 or 96 (the kernels are instantiated per size):
 //   A  k_spec_fwd    one block per (type, x) plane: read the int64
 //      accumulators (and clear them), scale to density, r2c along z (a
 //      length-n2/2 complex transform and the usual split of even and odd
@@ -83,17 +84,14 @@ __device__ __forceinline__ void tile_columns(ColInfo* col, const SpecGeom& g, in
 
 // ------------------------------------------------------------ pass A ---
 // Plane layout (passes A and C): row r of the (y, z) plane at r * plane_ls;
-// within a row the z transform's positions p sit at p + (p >> plane_pz)
-// (one pad after every N2 elements, N2 the transform's second-step length),
-// so that its strided accesses fall in distinct banks; plane_ls = 8 mod 16
-// (in float2) puts the two rows a 16-lane access touches in complementary
-// banks.  Without a second step (h <= 16) each lane owns a row: odd stride.
-__host__ __device__ constexpr int plane_pz(int h) {
-    return h / split1(h) > 1 ? ilog2(h / split1(h)) : 30;
-}
+// within a row the z transform's positions p sit at p + p / N2 (one pad
+// after every N2 elements, N2 the transform's second-step length), so that
+// its strided accesses fall in distinct banks; plane_ls = 8 mod 16 (in
+// float2) puts the two rows a 16-lane access touches in complementary banks.
+// Without a second step (h <= 16) each lane owns a row: odd stride.
+__host__ __device__ constexpr int plane_n2(int h) { return h / split1(h); }
 __host__ __device__ constexpr int plane_ls(int h) {
-    return h / split1(h) > 1 ? ((h + h / (h / split1(h)) + 1 + 7) / 16) * 16 + 8
-                             : ((h + 1) | 1);
+    return plane_n2(h) > 1 ? ((h + h / plane_n2(h) + 1 + 7) / 16) * 16 + 8 : ((h + 1) | 1);
 }
 
 // One block per (grid, x) plane.  z: int64 accumulators (read and cleared)
@@ -106,12 +104,13 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     k_spec_fwd(unsigned long long* __restrict__ acc, float2* __restrict__ spec, SpecGeom g,
                SpecScale sc, const BoxState* __restrict__ bs, const float2* __restrict__ tw) {
     extern __shared__ __align__(16) float2 sm[];
-    constexpr int Ny = NY, H = HZ, Nzc = H + 1, Ls = plane_ls(H), PZ = plane_pz(H);
-    constexpr int step = kTableN / (2 * H);
+    constexpr int Ny = NY, H = HZ, Nzc = H + 1, Ls = plane_ls(H), PN = plane_n2(H);
+    // twiddles exp(-2 pi i k / n2) of the even/odd split
+    constexpr int zoff = Tw<2 * H>::off, step = Tw<2 * H>::stride;
     const int x = blockIdx.x, t = blockIdx.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const FftIdx fz = fft_idx(H);
-    auto zs = [](int e) { return e + (e >> PZ); };
+    using fz = Idx<H>;
+    auto zs = [](int e) { return PN > 1 ? e + e / PN : e; };
     const float s = sc.s[t] * bs->inv_dV * kFixInv;
     ulonglong2* a =
         reinterpret_cast<ulonglong2*>(acc + (int64_t)t * g.M + (int64_t)x * Ny * (2 * H));
@@ -138,9 +137,9 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     // lanes 0-15 take 16 columns q, lanes 16-31 their partners h - q (h for
     // q = 0), one row offset n2 per warp task, a warp barrier between the
     // loads and the stores.  X[k] goes where Z[k] was, X[h] to slot h.
-    auto colslot = [&](int c) { return zs(c == H ? H : fz.pos(c)); };
+    auto colslot = [&](int c) { return zs(c == H ? H : fz::pos(c)); };
     {
-        constexpr int N1 = split1(Ny), N2 = Ny / N1, TW = kTableN / Ny;
+        constexpr int N1 = split1(Ny), N2 = Ny / N1;
         constexpr int pairs = H / 2 + 1, groups = (pairs + 15) / 16;
         for (int task = warp; task < groups * N2; task += kSpecWarps) {
             const int gq = task / N2, n2 = task - gq * N2;
@@ -148,8 +147,8 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             const bool active = q < pairs && !(side && q == H / 2);
             const int c = !active ? 0 : (side ? (q == 0 ? H : H - q) : q);
             const int kk = c == H ? 0 : c;
-            const int pk = zs(fz.pos(kk)), pp = kk == 0 ? pk : zs(fz.pos(H - kk));
-            const float2 w = __ldg(tw + kk * step);
+            const int pk = zs(fz::pos(kk)), pp = kk == 0 ? pk : zs(fz::pos(H - kk));
+            const float2 w = __ldg(tw + zoff + kk * step);
             float2 v[N1];
 #pragma unroll
             for (int i = 0; i < N1; ++i) {
@@ -163,7 +162,8 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             reg_fft<N1, false>(v);
             if (N2 > 1) {
 #pragma unroll
-                for (int k1 = 1; k1 < N1; ++k1) v[k1] = c_mul(v[k1], __ldg(tw + n2 * k1 * TW));
+                for (int k1 = 1; k1 < N1; ++k1)
+                    v[k1] = c_mul(v[k1], __ldg(tw + Tw<Ny>::off + n2 * k1 * Tw<Ny>::stride));
             }
             __syncwarp();
             if (active) {
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
         sQ[(e / T) * kSpecMaxT + e % T] = fun->Q[e];
     for (int e = threadIdx.x; e < T; e += blockDim.x) sb[e] = fun->b[e];
     tile_columns(col, g, j0, bs);
-    const FftIdx fx = fft_idx(N);
+    using fx = Idx<N>;
     const float kf0 = bs->kf[0];
     const float invM = (float)bs->inv_M;
     const float s2h = fun->sigma2_half;
@@ -220,7 +220,6 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     const float inv_cin = 1.0f / (float)cin, inv_cout = 1.0f / (float)cout;
     {
         constexpr int N1 = split1(N), N2 = N / N1;
-        constexpr int TW = kTableN / N;
         auto at_in = [&](int c, int e) -> float2& { return in[(c >> ws) * TS + e * W + (c & (W - 1))]; };
         auto at_out = [&](int c, int e) -> float2& { return out[(c >> ws) * TS + e * W + (c & (W - 1))]; };
         // forward x transform of the densities
@@ -241,7 +240,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
         // ph)_t with ph = H phi / M, weighted by the multiplicity
         for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
             const int p = e >> ws, w = e & (W - 1);
-            const int ix = fx.freq(p);
+            const int ix = fx::freq(p);
             const ColInfo ci = col[w];
             const bool origin = ix == 0 && ci.origin;
             const float kx = (ix <= N / 2 ? ix : ix - N) * kf0;
@@ -295,7 +294,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
 #pragma unroll
             for (int i = 0; i < N1; ++i) {
                 const int ix = N2 * i + n2;
-                const float2 v = vt[fx.pos(ix) * W];
+                const float2 v = vt[fx::pos(ix) * W];
                 const float gx = ix == N / 2 ? 0.0f : (ix <= N / 2 ? ix : ix - N) * kf0;
                 a[i] = e ? v : make_float2(gx * v.y, -gx * v.x);
             }
@@ -303,7 +302,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             if (N2 > 1) {
 #pragma unroll
                 for (int k1 = 1; k1 < N1; ++k1) {
-                    const float2 tw1 = __ldg(tw + n2 * k1 * TW);
+                    const float2 tw1 = __ldg(tw + Tw<N>::off + n2 * k1 * Tw<N>::stride);
                     a[k1] = c_mul(a[k1], make_float2(tw1.x, -tw1.y));
                 }
             }
@@ -347,7 +346,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     float2* in = sm;        // [Nx][W]
     float2* out = sm + TS;  // [2][Nx][W]: -i g_x psi, psi
     tile_columns(col, g, j0, bs);
-    const FftIdx fx = fft_idx(N);
+    using fx = Idx<N>;
     const float kf0 = bs->kf[0];
     const float invM = (float)bs->inv_M;
     const float s2h = fun->sigma2_half;
@@ -356,7 +355,6 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     const float inv_w = 1.0f / (float)W, inv_cout = 1.0f / (float)cout;
     {
         constexpr int N1 = split1(N), N2 = N / N1;
-        constexpr int TW = kTableN / N;
         auto ld = [&](int c, int n) { return __ldg(rho + n * plane + j0 + c); };
         auto st = [&](int c, int p, float2 v) { in[p * W + c] = v; };
         auto fin = [&](int c, int k, int p, float2 v) { in[p * W + c] = v; };
@@ -382,7 +380,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                 float k2 = kx * kx + ci.ky * ci.ky + ci.kz * ci.kz;
                 const float Hk = expf(-s2h * k2);
                 if (ix == 0 && ci.origin) k2 = 1.0f;  // k.normp(p=2, zeromode=1)
-                const float2 r = in[fx.pos(ix) * W + w];
+                const float2 r = in[fx::pos(ix) * W + w];
                 const float2 rq = make_float2(r.x * invM, r.y * invM);
                 const float sc = four_pi_fac * Hk / k2;
                 const float2 v = make_float2(rq.x * sc, rq.y * sc);
@@ -395,7 +393,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             if (N2 > 1) {
 #pragma unroll
                 for (int k1 = 1; k1 < N1; ++k1) {
-                    const float2 tw1 = __ldg(tw + n2 * k1 * TW);
+                    const float2 tw1 = __ldg(tw + Tw<N>::off + n2 * k1 * Tw<N>::stride);
                     a[k1] = c_mul(a[k1], make_float2(tw1.x, -tw1.y));
                 }
             }
@@ -440,12 +438,12 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                const BoxState* __restrict__ bs, const float2* __restrict__ tw, int first,
                int pic) {
     extern __shared__ __align__(16) float2 sm[];
-    constexpr int Ny = NY, H = HZ, Nzc = H + 1, Ls = plane_ls(H), PZ = plane_pz(H);
-    constexpr int step = kTableN / (2 * H);
+    constexpr int Ny = NY, H = HZ, Nzc = H + 1, Ls = plane_ls(H), PN = plane_n2(H);
+    constexpr int zoff = Tw<2 * H>::off, step = Tw<2 * H>::stride;
     const int x = blockIdx.x, gi = blockIdx.y + first;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const FftIdx fy = fft_idx(Ny);
-    auto zs = [](int e) { return e + (e >> PZ); };
+    using fy = Idx<Ny>;
+    auto zs = [](int e) { return PN > 1 ? e + e / PN : e; };
     int src, mul;  // mul: 0 none, 1 -i g_y, 2 -i g_z
     if (pic) {
         src = gi == 1 ? 0 : 1;
@@ -483,11 +481,11 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     }
     __syncthreads();
     {
-        constexpr int N1 = split1(H), N2 = H / N1, TW = kTableN / H;
+        constexpr int N1 = split1(H), N2 = H / N1;
         constexpr int RPW = 32 / N2;  // rows per warp
         for (int r0 = warp * RPW; r0 < Ny; r0 += kSpecWarps * RPW) {
-            const int r = r0 + lane / N2, n2 = lane & (N2 - 1);
-            const bool active = r < Ny;
+            const int r = r0 + lane / N2, n2 = lane % N2;
+            const bool active = lane < RPW * N2 && r < Ny;
             float2* row = sm + (active ? r : 0) * Ls;
             float2 a[N1];
 #pragma unroll
@@ -496,7 +494,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                 const float2 xk = row[m], xp = row[H - m];
                 const float2 A = make_float2(xk.x + xp.x, xk.y - xp.y);
                 const float2 B = make_float2(xk.x - xp.x, xk.y + xp.y);
-                const float2 w = __ldg(tw + m * step);
+                const float2 w = __ldg(tw + zoff + m * step);
                 const float2 vB = c_mul(B, make_float2(w.x, -w.y));
                 a[i] = make_float2(A.x - vB.y, A.y + vB.x);
             }
@@ -504,7 +502,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             if (N2 > 1) {
 #pragma unroll
                 for (int k1 = 1; k1 < N1; ++k1) {
-                    const float2 tw1 = __ldg(tw + n2 * k1 * TW);
+                    const float2 tw1 = __ldg(tw + Tw<H>::off + n2 * k1 * Tw<H>::stride);
                     a[k1] = c_mul(a[k1], make_float2(tw1.x, -tw1.y));
                 }
             }
@@ -516,7 +514,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             __syncwarp();
         }
         __syncthreads();
-        auto fin = [&](int r, int m, int p, float2 v) { out[fy.freq(r) * H + m] = v; };
+        auto fin = [&](int r, int m, int p, float2 v) { out[fy::freq(r) * H + m] = v; };
         if (N2 > 1) {
             auto ld2 = [&](int r, int p) { return sm[r * Ls + zs(p)]; };
             fft_step2<H, true, false>(Ny, inv_rows, ld2, fin);
@@ -526,8 +524,6 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
         }
     }
 }
-
-bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
 // The k-space kernels are instantiated per x length (their register
 // transforms are sized by it); f(kernel pointer) for this mesh.
@@ -540,6 +536,10 @@ int with_kspace(int nx, F f) {
         case 64: return f(k_spec_kspace<64>, k_spec_kspace_pic<64>);
         case 128: return f(k_spec_kspace<128>, k_spec_kspace_pic<128>);
         case 256: return f(k_spec_kspace<256>, k_spec_kspace_pic<256>);
+        case 24: return f(k_spec_kspace<24>, k_spec_kspace_pic<24>);
+        case 48: return f(k_spec_kspace<48>, k_spec_kspace_pic<48>);
+        case 96: return f(k_spec_kspace<96>, k_spec_kspace_pic<96>);
+        case 192: return f(k_spec_kspace<192>, k_spec_kspace_pic<192>);
         default: return HPF_ERR_ARG;
     }
 }
@@ -572,7 +572,8 @@ size_t plane_smem(const hpf_ctx* c) {
 }
 
 // The plane kernels are instantiated per (n1, n2 / 2): n1 and n2 in
-// {16, 32, 64, 128}.  f(fwd kernel, inv kernel) for this mesh.
+// {16, 32, 64, 128}, and the cubic 24, 48, 96.  f(fwd kernel, inv kernel)
+// for this mesh.
 template <class F>
 int with_planes(int n1, int h, F f) {
 #define HPF_PLANE(NY, HZ) \
@@ -582,6 +583,9 @@ int with_planes(int n1, int h, F f) {
     HPF_PLANES(32)
     HPF_PLANES(64)
     HPF_PLANES(128)
+    HPF_PLANE(24, 12)
+    HPF_PLANE(48, 24)
+    HPF_PLANE(96, 48)
 #undef HPF_PLANES
 #undef HPF_PLANE
     return HPF_ERR_ARG;
@@ -598,9 +602,7 @@ size_t tile_smem(const hpf_ctx* c, int W) {
 // Whether the fused passes apply to this context's mesh and type count.
 bool spectral_eligible(const hpf_ctx* c) {
     if (c->T > kSpecMaxT) return false;
-    if (!is_pow2(c->n0) || !is_pow2(c->n1) || !is_pow2(c->n2)) return false;
-    if (c->n0 < 8 || c->n0 > 256 || c->n1 < 8 || c->n1 > 256 || c->n2 < 8 || c->n2 > 512)
-        return false;
+    if (with_kspace(c->n0, [](auto, auto) { return HPF_OK; }) != HPF_OK) return false;
     if (plane_smem(c) > kSpecMaxSmem) return false;
     if (with_planes(c->n1, c->n2 / 2, [](auto, auto) { return HPF_OK; }) != HPF_OK) return false;
     return tile_smem(c, 4) <= kSpecTileSmem;
@@ -613,14 +615,20 @@ int spectral_setup(hpf_ctx* c) {
     // budget and leaves a block for every SM
     int W = 16;
     const int64_t cols = (int64_t)c->n1 * (c->n2 / 2 + 1);
-    while (W > 4 && (W > c->n1 || tile_smem(c, W) > kSpecTileSmem || cols / W < 152)) W >>= 1;
-    if (W > c->n1) return HPF_OK;
+    while (W > 4 &&
+           (c->n1 % W != 0 || tile_smem(c, W) > kSpecTileSmem || cols / W < 152))
+        W >>= 1;
+    if (c->n1 % W != 0) return HPF_OK;
     c->spec_W = W;
     c->spec_tiles = (int)(cols / W);
-    float2 h_tw[kTableN];
-    for (int m = 0; m < kTableN; ++m) {
-        const double a = -2.0 * 3.14159265358979323846 * (double)m / (double)kTableN;
+    float2 h_tw[kTableTotal];
+    for (int m = 0; m < kTable2; ++m) {
+        const double a = -2.0 * 3.14159265358979323846 * (double)m / (double)kTable2;
         h_tw[m] = make_float2((float)cos(a), (float)sin(a));
+    }
+    for (int m = 0; m < kTable3; ++m) {
+        const double a = -2.0 * 3.14159265358979323846 * (double)m / (double)kTable3;
+        h_tw[kTable2 + m] = make_float2((float)cos(a), (float)sin(a));
     }
     if (cudaMalloc(&c->d_tw, sizeof(h_tw)) != cudaSuccess) return HPF_ERR_CUDA;
     if (cudaMemcpy(c->d_tw, h_tw, sizeof(h_tw), cudaMemcpyHostToDevice) != cudaSuccess)

@@ -123,8 +123,9 @@ int hpf_ctx_set_box(hpf_ctx* ctx, const double box[3], void* stream);
 /* Device pointer to the box state (double L[3], V, dV at offsets 0..4). */
 int hpf_ctx_box_state(hpf_ctx* ctx, void** d_state);
 /* Transform path of hpf_field_step and hpf_pic_step (same arithmetic, FP32
- * either way): on a mesh whose axes are powers of two (n0 8..256, n1 and n2
- * 16..128; n_types <= 8) the default is this library's fused passes
+ * either way): on a mesh with n0 a power of two in 8..256 or one of 24, 48,
+ * 96, 192, and (n1, n2) both powers of two in 16..128 or n1 = n2 in {24, 48,
+ * 96} (n_types <= 8), the default is this library's fused passes
  * (shared-memory FFTs, the k-space map inside the x transform, the paint's
  * accumulators read directly);
  * fused = 0 selects the cuFFT path.  fused = 1 on a mesh that does not

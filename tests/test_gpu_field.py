@@ -260,7 +260,8 @@ def test_gaussian_core_energy_known_answer():
 @pytest.mark.parametrize("mesh,T", [
     ((32, 32, 32), 3), ((8, 16, 32), 2), ((16, 16, 16), 1), ((64, 32, 16), 5),
     ((32, 64, 128), 3), ((128, 16, 16), 2), ((16, 128, 64), 4), ((256, 16, 32), 1),
-    ((16, 32, 16), 8)])
+    ((16, 32, 16), 8), ((48, 48, 48), 3), ((24, 24, 24), 2), ((96, 48, 48), 4),
+    ((48, 96, 96), 1), ((24, 16, 32), 5), ((192, 24, 24), 2)])
 def test_fused_spectral_path_matches_oracle_and_library_path(mesh, T):
     """hpf_field_step through this library's shared-memory transforms (the
     default on power-of-two meshes) and through cuFFT, against the FP64
@@ -301,14 +302,15 @@ def test_fused_spectral_path_availability():
     from hymd_gb300.field import ParticleMesh
     assert ParticleMesh((64, 64, 64), (10.0, 10.0, 10.0), 5).spectral == "fused"
     for mesh, T in [((24, 24, 26), 3), ((32, 32, 32), 9), ((512, 32, 32), 1),
-                    ((16, 256, 16), 2), ((16, 16, 512), 1)]:
+                    ((16, 256, 16), 2), ((16, 16, 512), 1), ((48, 32, 48), 2),
+                    ((40, 32, 32), 1)]:
         pm = ParticleMesh(mesh, (10.0, 10.0, 10.0), T)
         assert not pm.spectral_available and pm.spectral == "cufft"
         with pytest.raises(_lib.HPFError):
             pm.spectral = "fused"
 
 
-@pytest.mark.parametrize("mesh", [(32, 32, 32), (64, 16, 32), (16, 128, 64)])
+@pytest.mark.parametrize("mesh", [(32, 32, 32), (64, 16, 32), (16, 128, 64), (48, 48, 48)])
 def test_fused_pic_step_matches_oracle_and_library_path(mesh):
     """hpf_pic_step as the MD step calls it (no grids requested back) on the
     fused spectral passes, against the FP64 oracle and against the cuFFT path:
