@@ -219,6 +219,11 @@ __device__ __forceinline__ int div_inv(int n, int d, float inv) {
 // position it came from.
 // CFAST: neighbouring threads take neighbouring transforms c (for layouts
 // where c is the unit stride); else neighbouring elements of one transform.
+template <int V>
+struct IntC {
+    static constexpr int value = V;
+};
+
 struct NoPre {
     template <int R>
     __device__ __forceinline__ void operator()(int, int, float2 (&)[R]) const {}

@@ -237,46 +237,56 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
         // k-space map in place, one thread per mode (p, w): v_t = H^2 (Q
         // phi)_t / M (+ H b_t at k = 0) over the T densities phi; and the
         // Parseval sums of the energy and the pressure, q = sum_t ph_t . (Q
-        // ph)_t with ph = H phi / M, weighted by the multiplicity
-        for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
-            const int p = e >> ws, w = e & (W - 1);
-            const int ix = fx::freq(p);
-            const ColInfo ci = col[w];
-            const bool origin = ix == 0 && ci.origin;
-            const float kx = (ix <= N / 2 ? ix : ix - N) * kf0;
-            const float k2 = kx * kx + ci.ky * ci.ky + ci.kz * ci.kz;
-            const float Hk = expf(-s2h * k2);
-            const float hm = Hk * invM;
-            float2 ph[kSpecMaxT];
+        // ph)_t with ph = H phi / M, weighted by the multiplicity.  The type
+        // count is a compile-time constant of each variant (its loops fully
+        // unrolled to T^2 products).
+        auto map = [&](auto tc) {
+            constexpr int TT = decltype(tc)::value;
+            for (int e = threadIdx.x; e < N * W; e += blockDim.x) {
+                const int p = e >> ws, w = e & (W - 1);
+                const int ix = fx::freq(p);
+                const ColInfo ci = col[w];
+                const bool origin = ix == 0 && ci.origin;
+                const float kx = (ix <= N / 2 ? ix : ix - N) * kf0;
+                const float k2 = kx * kx + ci.ky * ci.ky + ci.kz * ci.kz;
+                const float Hk = expf(-s2h * k2);
+                const float hm = Hk * invM;
+                float2 ph[TT];
 #pragma unroll
-            for (int jj = 0; jj < kSpecMaxT; ++jj)
-                if (jj < T) ph[jj] = in[jj * TS + p * W + w];
-            float qq = 0.0f;
+                for (int jj = 0; jj < TT; ++jj) ph[jj] = in[jj * TS + p * W + w];
+                float qq = 0.0f;
 #pragma unroll
-            for (int tt = 0; tt < kSpecMaxT; ++tt) {
-                if (tt < T) {
+                for (int tt = 0; tt < TT; ++tt) {
                     float2 u = make_float2(0.0f, 0.0f);
 #pragma unroll
-                    for (int jj = 0; jj < kSpecMaxT; ++jj) {
-                        if (jj < T) {
-                            const float Qtj = sQ[tt * kSpecMaxT + jj];
-                            u.x = fmaf(Qtj, ph[jj].x, u.x);
-                            u.y = fmaf(Qtj, ph[jj].y, u.y);
-                        }
+                    for (int jj = 0; jj < TT; ++jj) {
+                        const float Qtj = sQ[tt * kSpecMaxT + jj];
+                        u.x = fmaf(Qtj, ph[jj].x, u.x);
+                        u.y = fmaf(Qtj, ph[jj].y, u.y);
                     }
                     qq = fmaf(ph[tt].x, u.x, fmaf(ph[tt].y, u.y, qq));
                     float2 v = make_float2(Hk * hm * u.x, Hk * hm * u.y);
                     if (origin) v.x += Hk * sb[tt];
                     in[tt * TS + p * W + w] = v;
                 }
+                if (sums && !origin) {
+                    const float wq = ci.wk * qq * hm * hm;
+                    acc[0] += wq;
+                    acc[1] = fmaf(wq, kx * kx, acc[1]);
+                    acc[2] = fmaf(wq, ci.ky * ci.ky, acc[2]);
+                    acc[3] = fmaf(wq, ci.kz * ci.kz, acc[3]);
+                }
             }
-            if (sums && !origin) {
-                const float wq = ci.wk * qq * hm * hm;
-                acc[0] += wq;
-                acc[1] = fmaf(wq, kx * kx, acc[1]);
-                acc[2] = fmaf(wq, ci.ky * ci.ky, acc[2]);
-                acc[3] = fmaf(wq, ci.kz * ci.kz, acc[3]);
-            }
+        };
+        switch (T) {
+            case 1: map(IntC<1>()); break;
+            case 2: map(IntC<2>()); break;
+            case 3: map(IntC<3>()); break;
+            case 4: map(IntC<4>()); break;
+            case 5: map(IntC<5>()); break;
+            case 6: map(IntC<6>()); break;
+            case 7: map(IntC<7>()); break;
+            default: map(IntC<8>()); break;
         }
         __syncthreads();
         // inverse x transforms, step 1; item (grid 2 to + e, w, n2): e = 0

@@ -344,3 +344,29 @@ def test_fused_pic_step_matches_oracle_and_library_path(mesh):
     np.testing.assert_allclose(out["fused"][1], out["cufft"][1], rtol=1e-6)
     assert np.array_equal(out["fused"][0], out["fused2"][0])  # accumulators cleared
     pm.check_errors()
+
+
+@pytest.mark.parametrize("path", ["fused", "cufft"])
+def test_field_step_without_beads(path):
+    """An empty system: hpf_field_step with n = 0 paints nothing and returns
+    zero k-space sums on both transform paths (the accumulators stay clear
+    for the next, non-empty call, which must match the oracle)."""
+    from hymd_gb300 import _lib
+    cfg, ham, fun, r, types = make_system(21, n=2000, T=2, mesh=(32, 32, 32))
+    gf, pm, fl, _, _, R, Ty = _setup(cfg, ham, r, types)
+    pm.set_functional(ham)
+    pm.spectral = path
+    sums = _lib.new_workspace(R.device)
+    _lib.call("hpf_field_step", pm._h, None, None, 0, _lib.dvec(cfg.m), None, _lib.ptr(sums),
+              None, None, _lib.stream_ptr())
+    torch.cuda.synchronize()
+    assert np.all(sums[:4].cpu().numpy() == 0.0)
+    F = torch.zeros_like(R)
+    _lib.call("hpf_field_step", pm._h, _lib.ptr(R), _lib.ptr(Ty), R.shape[0], _lib.dvec(cfg.m),
+              _lib.ptr(F), None, None, None, _lib.stream_ptr())
+    ref = of.update_field(r.astype(np.float64), types, cfg.n_types, cfg.mesh(), cfg.box(), cfg.m,
+                          fun, cfg.sigma)
+    Fref = of.compute_field_force(ref["force_mesh"], r.astype(np.float64), types, cfg.n_types,
+                                  cfg.mesh(), cfg.box())
+    assert rel_rms(F.cpu().numpy(), Fref) < FORCE_RTOL
+    pm.check_errors()
