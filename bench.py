@@ -20,6 +20,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -68,12 +69,15 @@ def _config_block(cfg, n, workload=WORKLOAD, extra=None):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling during the timed region (the raw
+    samples go to BENCH_CLOCK_DIR, default the system temp directory; the
+    JSON line carries their summary)."""
 
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        d = os.environ.get("BENCH_CLOCK_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
