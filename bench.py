@@ -479,7 +479,9 @@ def run_gpu(args):
                 "config": _config_block(cfg, n, args.workload,
                                         {"bead_order": "sorted by mesh cell at setup",
                                          "respa_groups": md.plan_info(),
-                                         "respa_group_tuning_us": md.block_timings}),
+                                         "respa_group_tuning_us": md.block_timings,
+                                         "kspace_tile": md.pm.spectral_tile,
+                                         "kspace_tile_tuning_us": md.spectral_tile_timings}),
                 "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "steps/s",
                         "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 12 * n},
                 "gpu_launches": md.launches_per_step * args.steps,
@@ -559,6 +561,60 @@ def run_replicas(args):
             "clocks": clk.summary()}
     if rank == 0:
         print(json.dumps(line))
+    return 0
+
+
+def run_topology(args):
+    """prepare_bonds (hymd/force.py:325-505 + 573-728) on the device for the
+    1.3M-bead membrane (108k lipids + W, every bead its own molecule id when
+    free): wall time per call, inputs on the host and the packed arrays back
+    on the host as the reference returns them, checked against the tiled
+    per-molecule result.  Beside it, the host restatement (the reference's
+    traversals in Python without networkx) on the 162k-bead membrane."""
+    import time
+    import torch
+    from hymd_gb300 import systems
+    from hymd_gb300.force import prepare_bonds
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(0)
+    n_total = 1_300_000
+    n_lipids = int(round(0.444 * n_total / 12))
+    s = systems.lipid_membrane(seed=7, n_lipids=n_lipids, n_water=n_total - 12 * n_lipids,
+                               box=54.0, mesh=128)
+    n = len(s["names"])
+    idx = np.arange(n)
+    call = lambda: prepare_bonds(s["molecules"], s["names"], s["bonds"], idx, s["config"],
+                                 device="cuda")
+    for _ in range(max(args.warmup, 1)):
+        packed = call()
+    assert all(x.dtype == y.dtype and np.array_equal(x, y) for x, y in zip(packed, s["topology"]))
+    times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        call()
+        times.append(time.perf_counter() - t0)
+    dev_s = float(np.median(times))
+    m = systems.lipid_membrane()
+    t0 = time.perf_counter()
+    host = prepare_bonds(m["molecules"], m["names"], m["bonds"], np.arange(len(m["names"])),
+                         m["config"])
+    host_s = time.perf_counter() - t0
+    assert all(np.array_equal(x, y) for x, y in zip(host, m["topology"]))
+    line = {"metric": "bonded-term discovery time (prepare_bonds), 1.3M-bead membrane",
+            "value": dev_s, "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 1), "higher_is_better": False, "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic",
+            "terms": {"bonds": len(packed[0]), "angles": len(packed[4]),
+                      "dihedrals": len(packed[9])},
+            "host_restatement": {"value": host_s, "unit": "s", "cores": 1,
+                                 "sample": f"162k-bead membrane ({len(m['names'])} beads, "
+                                           "6000 lipids), Python traversal"},
+            "config": {"workload": f"lipid membrane {n} beads ({n_lipids} lipids + W), "
+                                   "box 54 nm", "timed": "host inputs -> packed host arrays"}}
+    print(json.dumps(line))
     return 0
 
 
@@ -694,6 +750,8 @@ def main():
     ap.add_argument("--reverse", action="store_true",
                     help="reverse-mode chi gradient on the 1.3M-bead membrane")
     ap.add_argument("--reverse-steps", type=int, default=200)
+    ap.add_argument("--topology", action="store_true",
+                    help="bonded-term discovery (prepare_bonds) on the device, 1.3M-bead membrane")
     args = ap.parse_args()
     if args.profile_stage:
         return profile_stage(args)
@@ -701,6 +759,8 @@ def main():
         return run_replicas(args)
     if args.reverse:
         return run_reverse(args)
+    if args.topology:
+        return run_topology(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

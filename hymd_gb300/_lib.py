@@ -43,6 +43,11 @@ _SIGNATURES = {
     "hpf_ctx_box_state": [P, ctypes.POINTER(P)],
     "hpf_ctx_set_spectral": [P, I],
     "hpf_ctx_get_spectral": [P, ctypes.POINTER(I), ctypes.POINTER(I)],
+    "hpf_topology_scratch_ints": [I64],  # returns int64 (restype set in lib())
+    "hpf_topology_terms": [I64, I, P, P, P, P, P, P, I, P, I, P, I, P, P, P, I, P, P, P, P, P, P,
+                           P, P, P],
+    "hpf_ctx_set_spectral_tile": [P, I],
+    "hpf_ctx_get_spectral_tile": [P, ctypes.POINTER(I), ctypes.POINTER(I)],
     "hpf_ctx_set_functional": [P, ctypes.POINTER(D), ctypes.POINTER(D), D, D],
     "hpf_get_error": [P, P, ctypes.POINTER(I)],
     "hpf_paint": [P, P, P, I64, ctypes.POINTER(D), P, P],
@@ -117,7 +122,8 @@ _LIB = None
 def header_symbols():
     """Names of every entry point declared in include/hpf_gb300.h."""
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"^(?:int|const char\*)\s+(hpf_\w+)\s*\(", txt, re.M)))
+    return sorted(set(re.findall(r"^(?:int|int64_t|const char\*)\s+(hpf_\w+)\s*\(", txt,
+                                 re.M)))
 
 
 def lib():
@@ -132,6 +138,7 @@ def lib():
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = ctypes.c_int
+        L.hpf_topology_scratch_ints.restype = ctypes.c_int64
         L.hpf_status_string.argtypes = [ctypes.c_int]
         L.hpf_status_string.restype = ctypes.c_char_p
         _LIB = L

@@ -1006,6 +1006,24 @@ int hpf_ctx_get_spectral(const hpf_ctx* c, int* fused, int* available) {
     return HPF_OK;
 }
 
+int hpf_ctx_set_spectral_tile(hpf_ctx* c, int width) {
+    if (!c) return HPF_ERR_ARG;
+    return spectral_set_tile(c, width);
+}
+
+int hpf_ctx_get_spectral_tile(const hpf_ctx* c, int* width, int* allowed_mask) {
+    if (!c) return HPF_ERR_ARG;
+    if (width) *width = c->spec_ok ? c->spec_W : 0;
+    if (allowed_mask) {
+        int m = 0;
+        if (c->spec_ok)
+            for (int w = 4; w <= 16; w *= 2)
+                if (spectral_tile_ok(c, w)) m |= w;
+        *allowed_mask = m;
+    }
+    return HPF_OK;
+}
+
 int hpf_ctx_box_state(hpf_ctx* c, void** d_state) {
     if (!c || !d_state) return HPF_ERR_ARG;
     *d_state = c->d_box;

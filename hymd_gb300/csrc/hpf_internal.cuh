@@ -74,7 +74,7 @@ struct hpf_ctx {
     // exp(-2 pi i m / 768), k-space tile width, partial sums + ticket
     float2* d_tw;
     double* d_spec_ws;
-    int spec_W, spec_tiles;
+    int spec_W, spec_tiles, spec_max_tiles;
     int spec_ok;     // the mesh qualifies and the scratch exists
     int spec_fused;  // use them (default when spec_ok)
 };
@@ -97,6 +97,8 @@ __device__ __forceinline__ float fix_to_float(long long x) {
 // creation, and accumulators -> force mesh (c->d_grid, [3T][M]).
 bool spectral_eligible(const hpf_ctx* c);
 int spectral_setup(hpf_ctx* c);
+bool spectral_tile_ok(const hpf_ctx* c, int W);
+int spectral_set_tile(hpf_ctx* c, int W);
 int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cudaStream_t st);
 int spectral_pic(hpf_ctx* c, float four_pi_fac, bool want_psi, double* sums, cudaStream_t st);
 

@@ -618,17 +618,31 @@ bool spectral_eligible(const hpf_ctx* c) {
     return tile_smem(c, 4) <= kSpecTileSmem;
 }
 
+// Whether pass B can run tiles of W columns on this context: W in {4, 8,
+// 16} (the tile's column table holds 16), dividing n1 (so that the n1 * (n2/2
+// + 1) columns split into whole tiles), within the shared-memory budget.
+bool spectral_tile_ok(const hpf_ctx* c, int W) {
+    if (W != 4 && W != 8 && W != 16) return false;
+    return c->n1 % W == 0 && tile_smem(c, W) <= kSpecTileSmem;
+}
+
+// Select the k-space tile width (the autotuner's knob); the partials were
+// sized for the narrowest tile at setup.
+int spectral_set_tile(hpf_ctx* c, int W) {
+    if (!c->spec_ok || !spectral_tile_ok(c, W)) return HPF_ERR_ARG;
+    c->spec_W = W;
+    c->spec_tiles = (int)((int64_t)c->n1 * (c->n2 / 2 + 1) / W);
+    return HPF_OK;
+}
+
 // Twiddle table, tile width and reduction scratch (at context creation).
 int spectral_setup(hpf_ctx* c) {
     if (!spectral_eligible(c)) return HPF_OK;
-    // widest tile (<= 16 columns, dividing n1) that fits the shared-memory
-    // budget and leaves a block for every SM
+    // default: the widest tile that leaves a block for every SM
     int W = 16;
     const int64_t cols = (int64_t)c->n1 * (c->n2 / 2 + 1);
-    while (W > 4 &&
-           (c->n1 % W != 0 || tile_smem(c, W) > kSpecTileSmem || cols / W < 152))
-        W >>= 1;
-    if (c->n1 % W != 0) return HPF_OK;
+    while (W > 4 && (!spectral_tile_ok(c, W) || cols / W < 152)) W >>= 1;
+    if (!spectral_tile_ok(c, W)) return HPF_OK;
     c->spec_W = W;
     c->spec_tiles = (int)(cols / W);
     float2 h_tw[kTableTotal];
@@ -643,8 +657,10 @@ int spectral_setup(hpf_ctx* c) {
     if (cudaMalloc(&c->d_tw, sizeof(h_tw)) != cudaSuccess) return HPF_ERR_CUDA;
     if (cudaMemcpy(c->d_tw, h_tw, sizeof(h_tw), cudaMemcpyHostToDevice) != cudaSuccess)
         return HPF_ERR_CUDA;
-    // partials: 4 values x tiles (double-float pairs), then the ticket
-    const size_t words = 4 * (size_t)c->spec_tiles + 8;
+    // partials: 4 values x tiles (double-float pairs), then the ticket; room
+    // for the narrowest tile, so that the width can change later
+    c->spec_max_tiles = (int)(cols / 4);
+    const size_t words = 4 * (size_t)c->spec_max_tiles + 8;
     if (cudaMalloc(&c->d_spec_ws, sizeof(double) * words) != cudaSuccess) return HPF_ERR_CUDA;
     if (cudaMemset(c->d_spec_ws, 0, sizeof(double) * words) != cudaSuccess) return HPF_ERR_CUDA;
     // the kernels' shared-memory ceilings are process-wide attributes: set
@@ -686,7 +702,7 @@ int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cuda
     });
     HPF_LAUNCH_CHECK();
     double* part = c->d_spec_ws;
-    unsigned int* tick = reinterpret_cast<unsigned int*>(c->d_spec_ws + 4 * (size_t)c->spec_tiles);
+    unsigned int* tick = reinterpret_cast<unsigned int*>(c->d_spec_ws + 4 * (size_t)c->spec_max_tiles);
     int r = with_kspace(c->n0, [&](auto kd, auto) {
         kd<<<c->spec_tiles, kSpecThreads, ts, st>>>(c->d_spec_phi, c->d_spec, g, c->T, c->d_box,
                                                     c->d_fun, c->d_tw, sums, part, tick);
@@ -717,7 +733,7 @@ int spectral_pic(hpf_ctx* c, float four_pi_fac, bool want_psi, double* sums, cud
     });
     HPF_LAUNCH_CHECK();
     double* part = c->d_spec_ws;
-    unsigned int* tick = reinterpret_cast<unsigned int*>(c->d_spec_ws + 4 * (size_t)c->spec_tiles);
+    unsigned int* tick = reinterpret_cast<unsigned int*>(c->d_spec_ws + 4 * (size_t)c->spec_max_tiles);
     int r = with_kspace(c->n0, [&](auto, auto kp) {
         kp<<<c->spec_tiles, kSpecThreads, ts, st>>>(c->d_spec_phi, c->d_spec, g, c->d_box,
                                                     c->d_fun, four_pi_fac, c->d_tw, sums, part,

@@ -112,6 +112,27 @@ class ParticleMesh:
         _lib.call("hpf_ctx_get_spectral", self._h, _lib.ctypes.byref(f), _lib.ctypes.byref(a))
         return bool(a.value)
 
+    @property
+    def spectral_tile(self):
+        """Columns per block of the fused k-space pass (4, 8 or 16; 0 without
+        the fused path).  Forces do not depend on it; the energy sums only
+        through their summation order."""
+        w, m = _lib.ctypes.c_int(0), _lib.ctypes.c_int(0)
+        _lib.call("hpf_ctx_get_spectral_tile", self._h, _lib.ctypes.byref(w),
+                  _lib.ctypes.byref(m))
+        return w.value
+
+    @spectral_tile.setter
+    def spectral_tile(self, width):
+        _lib.call("hpf_ctx_set_spectral_tile", self._h, int(width))
+
+    @property
+    def spectral_tiles_allowed(self):
+        w, m = _lib.ctypes.c_int(0), _lib.ctypes.c_int(0)
+        _lib.call("hpf_ctx_get_spectral_tile", self._h, _lib.ctypes.byref(w),
+                  _lib.ctypes.byref(m))
+        return [x for x in (4, 8, 16) if m.value & x]
+
     def check_errors(self):
         code = _lib.ctypes.c_int(0)
         _lib.call("hpf_get_error", self._h, _lib.stream_ptr(), _lib.ctypes.byref(code))

@@ -156,11 +156,30 @@ def _simple_paths(adj, u, n):
     return out
 
 
+def _dihedral_classes(dihedral_types):
+    """Class of each dihedral type: the index of the first type with equal
+    coefficients and dihedral type.  The reference's duplicate test
+    (force.py:476-487) compares a reversed term by its indices, coefficients
+    and type, so types equal in both are one type for it."""
+    cls = []
+    for i, a in enumerate(dihedral_types):
+        c = i
+        for j in range(i):
+            b = dihedral_types[j]
+            if (a.dih_type == b.dih_type and np.shape(a.coeffs) == np.shape(b.coeffs)
+                    and np.array_equal(np.asarray(a.coeffs), np.asarray(b.coeffs))):
+                c = cls[j]
+                break
+        cls.append(c)
+    return cls
+
+
 def prepare_bonds_old(molecules, names, bonds, indices, config):
     """hymd/force.py:325-505 -> (bonds_2, bonds_3, bonds_4, bb_index)."""
     bonds_2, bonds_3, bonds_4, bb_index = [], [], [], []
     seen4 = set()
     dihedral_types = list(config.dihedrals)
+    dcls = _dihedral_classes(dihedral_types)
     for _, members in _molecule_groups(molecules):
         bb_dihedral = 0
         adj = {}
@@ -199,10 +218,10 @@ def prepare_bonds_old(molecules, names, bonds, indices, config):
                 for ti, a in enumerate(dihedral_types):
                     if (nm[0] == a.atom_1 and nm[1] == a.atom_2 and nm[2] == a.atom_3
                             and nm[3] == a.atom_4):
-                        if (loc[3], loc[2], loc[1], loc[0], ti) in seen4:
+                        if (loc[3], loc[2], loc[1], loc[0], dcls[ti]) in seen4:
                             continue
                         bonds_4.append([loc[0], loc[1], loc[2], loc[3], a.coeffs, a.dih_type])
-                        seen4.add((loc[0], loc[1], loc[2], loc[3], ti))
+                        seen4.add((loc[0], loc[1], loc[2], loc[3], dcls[ti]))
                         if a.dih_type == 1:
                             bb_dihedral = len(bonds_4)
         if bb_dihedral:
@@ -248,11 +267,100 @@ def prepare_index_based_bonds(molecules, topol):
     return bonds_2, bonds_3, bonds_4
 
 
-def prepare_bonds(molecules, names, bonds, indices, config, topol=None):
+def _topology_device(molecules, names, bonds, indices, config, device):
+    """prepare_bonds_old's term discovery on the device (hpf_topology_terms):
+    the host maps names, term types and global indices to small integers
+    (numpy, vectorised); one device thread per molecule walks the molecule's
+    graph in the reference's traversal order.  Returns the packed arrays of
+    prepare_bonds (numpy, same dtypes)."""
+    dev = torch.device(device)
+    molecules = np.asarray(molecules)
+    N = len(molecules)
+    order = np.argsort(molecules, kind="stable")
+    _, starts = np.unique(molecules[order], return_index=True)
+    mol_start = np.append(starts, N).astype(np.int32)
+    n_mol = len(starts)
+    bead_slot = np.empty(N, np.int32)
+    bead_slot[order] = np.arange(N, dtype=np.int32)
+    uniq, name_id = np.unique(np.asarray(names), return_inverse=True)
+    nid = {_name(u): i for i, u in enumerate(uniq)}
+    gidx = np.asarray(indices).astype(np.int64).reshape(N)
+    rows = np.asarray(bonds).astype(np.int64).reshape(N, -1)
+    sorter = np.argsort(gidx, kind="stable")
+    sg = gidx[sorter]
+    valid = rows != -1
+    pos = np.minimum(np.searchsorted(sg, rows), max(N - 1, 0))
+    found = (sg[pos] == rows) if N else valid
+    if np.any(valid & ~found):
+        raise ValueError("prepare_bonds: a bond names a particle index that is not present")
+    partners = np.where(valid, sorter[pos], -1).astype(np.int32)
+    name = lambda x: nid.get(x, -1)
+    bt = np.array([[name(b.atom_1), name(b.atom_2)] for b in config.bonds], np.int32)
+    at = np.array([[name(a.atom_1), name(a.atom_2), name(a.atom_3)] for a in config.angle_bonds],
+                  np.int32)
+    dts = list(config.dihedrals)
+    dt = np.array([[name(a.atom_1), name(a.atom_2), name(a.atom_3), name(a.atom_4)] for a in dts],
+                  np.int32)
+    dcls = np.array(_dihedral_classes(dts), np.int32)
+    dbb = np.array([int(a.dih_type == 1) for a in dts], np.int32)
+    i32 = lambda x: torch.as_tensor(np.ascontiguousarray(x, dtype=np.int32).reshape(-1),
+                                    device=dev)
+    d_ms, d_sb, d_bs = i32(mol_start), i32(order), i32(bead_slot)
+    d_gid = torch.as_tensor(gidx, device=dev)
+    d_nid, d_par = i32(name_id), i32(partners)
+    d_bt, d_at, d_dt, d_cls, d_bb = i32(bt), i32(at), i32(dt), i32(dcls), i32(dbb)
+    scratch = torch.empty(max(int(_lib.lib().hpf_topology_scratch_ints(N)), 1), dtype=torch.int32,
+                          device=dev)
+    counts = torch.zeros((max(n_mol, 1), 3), dtype=torch.int32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    st = _lib.stream_ptr()
+    common = (N, n_mol, _lib.ptr(d_ms), _lib.ptr(d_sb), _lib.ptr(d_bs), _lib.ptr(d_gid),
+              _lib.ptr(d_nid), _lib.ptr(d_par), rows.shape[1], _lib.ptr(d_bt), len(bt),
+              _lib.ptr(d_at), len(at), _lib.ptr(d_dt), _lib.ptr(d_cls), _lib.ptr(d_bb), len(dts),
+              _lib.ptr(scratch))
+    _lib.call("hpf_topology_terms", *common, _lib.ptr(counts), None, None, None, None, None,
+              _lib.ptr(err), st)
+    csum = torch.cumsum(counts.to(torch.int64), dim=0)
+    offsets = (csum - counts).to(torch.int32).contiguous()
+    B, A, D = (int(x) for x in csum[-1].tolist())
+    e = int(err.item())
+    if e:
+        raise _lib.HPFError("hpf_topology_terms", e)
+    t2 = torch.empty((max(B, 1), 3), dtype=torch.int32, device=dev)
+    t3 = torch.empty((max(A, 1), 4), dtype=torch.int32, device=dev)
+    t4 = torch.empty((max(D, 1), 5), dtype=torch.int32, device=dev)
+    bbm = torch.empty(max(n_mol, 1), dtype=torch.int32, device=dev)
+    _lib.call("hpf_topology_terms", *common, _lib.ptr(counts), _lib.ptr(offsets), _lib.ptr(t2),
+              _lib.ptr(t3), _lib.ptr(t4), _lib.ptr(bbm), _lib.ptr(err), st)
+    t2, t3, t4 = t2[:B].cpu().numpy(), t3[:A].cpu().numpy(), t4[:D].cpu().numpy()
+    bbm = bbm[:n_mol].cpu().numpy()
+    e = int(err.item())
+    if e:
+        raise _lib.HPFError("hpf_topology_terms", e)
+    r0 = np.array([b.equilibrium for b in config.bonds], np.float64)
+    kb = np.array([b.strength for b in config.bonds], np.float64)
+    t0 = np.array([np.radians(a.equilibrium) for a in config.angle_bonds], np.float64)
+    ka = np.array([a.strength for a in config.angle_bonds], np.float64)
+    ctab = np.array([np.resize(a.coeffs, (6, 5)) for a in dts], np.float64).reshape(-1, 6, 5)
+    ttab = np.array([a.dih_type for a in dts], int)
+    ix = lambda c: c.astype(int)
+    last = np.zeros(D, dtype=int)
+    last[bbm[bbm >= 0]] = 1
+    return (ix(t2[:, 0]), ix(t2[:, 1]), r0[t2[:, 2]], kb[t2[:, 2]],
+            ix(t3[:, 0]), ix(t3[:, 1]), ix(t3[:, 2]), t0[t3[:, 3]], ka[t3[:, 3]],
+            ix(t4[:, 0]), ix(t4[:, 1]), ix(t4[:, 2]), ix(t4[:, 3]),
+            ctab[t4[:, 4]] if D else np.empty((0, 6, 5)), ttab[t4[:, 4]], last)
+
+
+def prepare_bonds(molecules, names, bonds, indices, config, topol=None, device=None):
     """hymd/force.py:573-728: the 16 packed arrays for the bonded kernels.
 
     Dihedral coefficients are np.resize'd to (6, 5) (a 2- or 4-row set is
-    repeated cyclically, as in the reference)."""
+    repeated cyclically, as in the reference).  With `device` (e.g. "cuda")
+    and no `topol`, the term discovery of prepare_bonds_old runs on that
+    device (one thread per molecule) and gives the same arrays."""
+    if topol is None and device is not None:
+        return _topology_device(molecules, names, bonds, indices, config, device)
     if topol is not None:
         b2, b3, b4 = prepare_index_based_bonds(molecules, topol)
         bb_index = None

@@ -68,6 +68,7 @@ class RespaMD:
             self.transfer = torch.zeros((nd, 6, 3, 3), dtype=torch.float32, device=self.device)
         self.plan = None
         self.block_timings = None
+        self.spectral_tile_timings = None
         self._packed = packed
         self.block_beads = None
         self.perm = None  # memory order -> input order, after sort_particles()
@@ -413,10 +414,43 @@ class RespaMD:
                       self.n, float(self.elec_factor), _lib.ptr(self.f_elec), None, None, None,
                       None, None, kick, st)
 
+    # autotune the fused k-space pass's tile width in prime()
+    TUNE_SPECTRAL_TILE = True
+
+    def _tune_spectral_tile(self, reps=5):
+        """Tile width of the fused k-space pass picked by timing the field
+        step (CUDA events, `reps` steps per width after one warm-up) on the
+        current positions; the fastest is kept.  Timings (us) are kept in
+        `spectral_tile_timings`.  The forces are the same for every width."""
+        widths = self.pm.spectral_tiles_allowed if self.pm.spectral == "fused" else []
+        self.spectral_tile_timings = {}
+        if len(widths) < 2:
+            return
+        st = _lib.stream_ptr()
+        scratch = torch.zeros_like(self.field_sums)
+        best = None
+        for w in widths:
+            self.pm.spectral_tile = w
+            self._field(st, scratch)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                self._field(st, scratch)
+            e1.record()
+            e1.synchronize()
+            t = e0.elapsed_time(e1) * 1000.0 / reps
+            self.spectral_tile_timings[w] = t
+            if best is None or t < best[0]:
+                best = (t, w)
+        self.pm.spectral_tile = best[1]
+
     def prime(self):
         """Bonded and slow forces at the initial positions (main.py:494-588).
         With the fused plan the bonded forces come from its deterministic
-        gather (hpf_respa_forces), so that runs are bit-reproducible."""
+        gather (hpf_respa_forces), so that runs are bit-reproducible.  The
+        k-space tile width is tuned first (`TUNE_SPECTRAL_TILE`)."""
+        if self.TUNE_SPECTRAL_TILE and self.graph is None:
+            self._tune_spectral_tile()
         st = _lib.stream_ptr()
         self._bonded(st, 0)
         if self.topo is not None:

@@ -12,6 +12,8 @@ Velocities are Maxwell-Boltzmann at the stated temperature for mass 72.
 Topologies are built with the host topology code (force.prepare_bonds) on
 one molecule and tiled, which gives the same arrays as running it on the
 whole system (the per-molecule lists are concatenated in molecule order).
+Each builder also returns the whole system's bond rows (`bonds`, the
+reference's (N, M) input form) for prepare_bonds on the full system.
 """
 import numpy as np
 
@@ -43,6 +45,18 @@ def _tile_topology(template, n_mol, mol_size, n_total):
             tile_i(b3a), tile_i(b3b), tile_i(b3c), tile_f(b3t), tile_f(b3k),
             tile_i(b4a), tile_i(b4b), tile_i(b4c), tile_i(b4d),
             np.tile(coeff, (n_mol, 1, 1)), tile_f(b4t), tile_f(last))
+
+
+def _tile_rows(conn, n_mol, mol_size, n_total):
+    """Bond rows of the whole system in the reference's input form (N, M):
+    identical molecules at consecutive index blocks, -1 for no partner and
+    for the beads after the molecules."""
+    conn = np.asarray(conn)
+    rows = np.full((n_total, conn.shape[1]), -1, dtype=np.int64)
+    off = (np.arange(n_mol) * mol_size)[:, None, None]
+    rows[:n_mol * mol_size] = np.where(conn[None] >= 0, conn[None] + off, -1).reshape(-1,
+                                                                                    conn.shape[1])
+    return rows
 
 
 def _config(**kw):
@@ -79,7 +93,7 @@ def homopolymer_melt(seed=1, n_chains=1000, length=10, box=10.0, mesh=32, chi_ab
     topo = _tile_topology(tmpl, n_chains, length, N)
     v = _velocities(rng, N, 323.0, 72.0)
     return dict(positions=r, velocities=v, types=types, names=names, molecules=molecules,
-                topology=topo, config=cfg)
+                topology=topo, config=cfg, bonds=_tile_rows(conn, n_chains, length, N))
 
 
 # dppc-like lipid: N(0)-P(1)-G(2)-C(4)-C(5)-C(6)-C(7); G(2)-G(3)-C(8)-C(9)-C(10)-C(11)
@@ -144,7 +158,7 @@ def lipid_membrane(seed=2, n_lipids=6000, n_water=90000, box=27.0, mesh=64, chi_
     cfg.rho0 = N / float(np.prod(L))
     cfg.a = cfg.rho0
     return dict(positions=r, velocities=v, types=types, names=names, molecules=molecules,
-                topology=topo, config=cfg)
+                topology=topo, config=cfg, bonds=_tile_rows(_LIPID_CONN, n_lipids, 12, N))
 
 
 def charged_peptides(seed=3, n_chains=200, n_res=50, n_total=500_000, box=40.0, mesh=128):
@@ -212,7 +226,8 @@ def charged_peptides(seed=3, n_chains=200, n_res=50, n_total=500_000, box=40.0, 
     cfg.rho0 = n_total / float(np.prod(L))
     cfg.a = cfg.rho0
     return dict(positions=r, velocities=v, types=types, names=names, molecules=molecules,
-                topology=topo, config=cfg, charges=q)
+                topology=topo, config=cfg, charges=q,
+                bonds=_tile_rows(conn, n_chains, per, n_total))
 
 
 BUILDERS = {"melt10k": homopolymer_melt, "membrane162k": lipid_membrane,

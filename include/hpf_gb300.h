@@ -133,6 +133,16 @@ int hpf_ctx_box_state(hpf_ctx* ctx, void** d_state);
  * whether the fused path is available (either pointer may be NULL). */
 int hpf_ctx_set_spectral(hpf_ctx* ctx, int fused);
 int hpf_ctx_get_spectral(const hpf_ctx* ctx, int* fused, int* available);
+/* Column-tile width of the fused k-space pass (4, 8 or 16 (y, kz) columns
+ * per block; the knob of the k-space autotuner, no counterpart in the
+ * reference, whose transforms are pfft's).  The width changes the tiling and
+ * the order of the energy/virial partial sums, not the force arithmetic.
+ * The setter returns HPF_ERR_ARG for a width this mesh does not allow (or
+ * without the fused path); allowed_mask gets the allowed widths OR'ed
+ * together (0 without the fused path).  A graph captured before a change
+ * keeps the width it was captured with. */
+int hpf_ctx_set_spectral_tile(hpf_ctx* ctx, int width);
+int hpf_ctx_get_spectral_tile(const hpf_ctx* ctx, int* width, int* allowed_mask);
 /* Quadratic interaction functional w = 1/2 phi.Q.phi + b.phi + c and filter
  * width sigma (hymd/hamiltonian.py:74-486, H at :57-71).  Q is T*T row-major. */
 int hpf_ctx_set_functional(hpf_ctx* ctx, const double* Q, const double* b, double c,
@@ -464,6 +474,48 @@ int hpf_sum_v2(const float* v, int64_t n, double* out, void* stream);
 int hpf_paint_static(const float* pos, const int32_t* types, int64_t n, int T, int n0, int n1,
                      int n2, const double box[3], const double* type_mass, float* phi_out,
                      int* d_err, void* stream);
+
+/* ---- topology preparation (hymd/force.py:325-505, prepare_bonds_old) ------
+ * Finds the bonds, angles and dihedrals of every molecule from the bond rows
+ * and the configured term types, in the order the reference's traversals
+ * produce them (node insertion order; breadth-first depth 1 / 2 for bonds /
+ * angles with gid(end) > gid(start); depth-first 4-node paths for
+ * dihedrals, skipping a path whose reversed term is listed already), one
+ * device thread per molecule.  All arrays are DEVICE arrays:
+ *   mol_start  int[n_mol+1]  slot ranges of the molecules (ascending id);
+ *   slot_bead  int[n_beads]  local bead at each slot (ascending within a
+ *                            molecule, the reference's enumerate order);
+ *   bead_slot  int[n_beads]  its inverse;
+ *   gid        int64[n_beads] global index of each local bead (node key);
+ *   name_id    int[n_beads]  small integer per distinct name;
+ *   partners   int[n_beads][max_partners] bonded partners as LOCAL bead
+ *                            indices, -1 for none (the bonds rows mapped
+ *                            from global indices by the caller);
+ *   bond_types int[nbt][2], angle_types int[nat][3], dih_types int[ndt][4]:
+ *                            name ids of each configured type (-1 for a
+ *                            name no bead has); dih_class: equal for types
+ *                            with equal coefficients and dihedral type (the
+ *                            reference's duplicate test compares those);
+ *                            dih_bb: 1 where the dihedral type is 1;
+ *   scratch    int[hpf_topology_scratch_ints(n_beads)].
+ * offsets == NULL: counting pass, counts[n_mol][3] = (bonds, angles,
+ * dihedrals) per molecule.  Otherwise the writing pass: offsets[n_mol][3]
+ * (exclusive prefix sums of counts) place each molecule's terms in
+ * bonds[B][3] = (i, j, type), angles[A][4] = (i, mid, j, type),
+ * dihedrals[D][5] = (a, b, c, d, type) as local bead indices and indices into
+ * the type arrays, and bb[n_mol] = index of the molecule's last type-1
+ * dihedral or -1 (force.py:501-502).  d_err receives HPF_ERR_INDEX for a
+ * partner outside its molecule and HPF_ERR_NOT_IMPLEMENTED for a node with
+ * more than HPF_TOPO_MAX_DEGREE distinct neighbours. */
+#define HPF_TOPO_MAX_DEGREE 8
+int64_t hpf_topology_scratch_ints(int64_t n_beads);
+int hpf_topology_terms(int64_t n_beads, int n_mol, const int* mol_start, const int* slot_bead,
+                       const int* bead_slot, const long long* gid, const int* name_id,
+                       const int* partners, int max_partners, const int* bond_types, int n_bond_types,
+                       const int* angle_types, int n_angle_types, const int* dih_types,
+                       const int* dih_class, const int* dih_bb, int n_dih_types, int* scratch,
+                       int* counts, const int* offsets, int* bonds, int* angles, int* dihedrals,
+                       int* bb, int* d_err, void* stream);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,9 @@ Outputs (all small .npz files):
                    DefaultWithChi evaluated by the reference lambdas on seeded grids
   misc.npz         dipole_forces_redistribution, propensity_potential_coeffs,
                    integrator and CSVR thermostat outputs of the reference
+  topology_random.npz  prepare_bonds_old / prepare_bonds on seeded random
+                   molecules (branches, rings, scrambled ids, duplicate and
+                   reversed term types; random_molecules())
 """
 import ast
 import importlib.util
@@ -265,5 +268,102 @@ def main(ref):
     print("wrote golden fixtures to", HERE)
 
 
+def random_molecules(seed=7, n_mol=60):
+    """Seeded random molecules for the topology fixture: 1-16 beads each,
+    random trees plus extra edges (rings), names from A-D, molecule ids and
+    global indices scrambled, members interleaved in the local order, bond
+    rows with -1 anywhere, edges listed from one or both ends, some
+    self-bonds.  Returns molecules, names (bytes), bonds (global indices),
+    indices, and the term types (plain tuples)."""
+    rng = np.random.default_rng(seed)
+    alphabet = ["A", "B", "C", "D"]
+    sizes = rng.integers(1, 17, n_mol)
+    N = int(sizes.sum())
+    mol_of = np.repeat(rng.permutation(10 * n_mol)[:n_mol], sizes)
+    molecules = mol_of[rng.permutation(N)]
+    indices = rng.permutation(N) + 500
+    names = np.array([alphabet[x].encode() for x in rng.integers(0, 4, N)])
+    rows = [[] for _ in range(N)]
+    deg = np.zeros(N, int)
+
+    def link(u, v):
+        deg[u] += 1
+        deg[v] += 1
+        c = rng.integers(0, 3)
+        if c != 1:
+            rows[u].append(int(indices[v]))
+        if c != 0:
+            rows[v].append(int(indices[u]))
+
+    for m in np.unique(molecules):
+        mem = rng.permutation(np.where(molecules == m)[0])
+        for i in range(1, len(mem)):
+            cand = [j for j in range(i) if deg[mem[j]] < 4]
+            link(mem[i], mem[cand[rng.integers(0, len(cand))]] if cand else mem[i - 1])
+        for _ in range(len(mem) // 5):
+            u, v = rng.choice(mem, 2, replace=False)
+            if deg[u] < 6 and deg[v] < 6:
+                link(u, v)
+        if len(mem) > 2 and rng.uniform() < 0.2:
+            rows[mem[0]].append(int(indices[mem[0]]))
+    M = max(len(r) for r in rows) + 1
+    bonds = -np.ones((N, M), dtype=np.int64)
+    for i, r in enumerate(rows):
+        slots = np.sort(rng.permutation(M)[:len(r)])
+        bonds[i, slots] = r
+    bond_types = [("A", "B", 0.40, 1000.0), ("A", "A", 0.45, 1100.0), ("B", "C", 0.50, 1200.0),
+                  ("C", "D", 0.30, 900.0), ("A", "B", 0.41, 800.0), ("D", "A", 0.33, 700.0),
+                  ("E", "A", 0.2, 100.0)]
+    angle_types = [("A", "B", "C", 120.0, 25.0), ("C", "B", "A", 110.0, 20.0),
+                   ("A", "A", "A", 180.0, 30.0), ("B", "C", "D", 100.0, 15.0),
+                   ("D", "D", "B", 90.0, 10.0), ("A", "E", "A", 90.0, 10.0)]
+    c0 = [[1.0, 2.0, 3.0, 4.0, 5.0], [0.0, 0.0, 0.0, 0.0, 0.0]]
+    c1 = [[0.5] * 5, [1.0] * 5, [2.0] * 5, [3.0] * 5]
+    dihedral_types = [("A", "B", "C", "D", c0, 0), ("D", "C", "B", "A", c0, 0),
+                      ("A", "A", "A", "A", [[1.0] * 5, [0.0, 1.0, 0.0, 1.0, 0.0]], 0),
+                      ("A", "B", "A", "B", c1, 1), ("B", "A", "B", "A", c1, 1),
+                      ("C", "C", "D", "D", [[2.0] * 5, [0.0] * 5], 2),
+                      ("A", "B", "C", "D", [[9.0] * 5, [0.0] * 5], 0),
+                      ("B", "B", "A", "C", c0, 0)]
+    return molecules, names, bonds, indices, bond_types, angle_types, dihedral_types
+
+
+def random_topology(ref):
+    """topology_random.npz: the reference's prepare_bonds_old / prepare_bonds
+    on random_molecules() (inputs, term types and outputs)."""
+    _install_stubs()
+    pkg = _types.ModuleType("hymd")
+    pkg.__path__ = [os.path.join(ref, "hymd")]
+    sys.modules["hymd"] = pkg
+    logger = _load("hymd.logger", os.path.join(ref, "hymd", "logger.py"), "hymd")
+    force = _load("hymd.force", os.path.join(ref, "hymd", "force.py"), "hymd")
+    force.Logger = logger.Logger
+    molecules, names, bonds, indices, bt, at, dt = random_molecules()
+
+    class Cfg:
+        pass
+    cfg = Cfg()
+    cfg.bonds = [force.Bond(a, b, r0, k) for a, b, r0, k in bt]
+    cfg.angle_bonds = [force.Angle(atom_1=a, atom_2=b, atom_3=c, equilibrium=e, strength=k)
+                       for a, b, c, e, k in at]
+    cfg.dihedrals = [force.Dihedral(atom_1=a, atom_2=b, atom_3=c, atom_4=d, coeffs=co,
+                                    dih_type=t) for a, b, c, d, co, t in dt]
+    b2, b3, b4, bbi = force.prepare_bonds_old(molecules, names, bonds, indices, cfg)
+    packed = force.prepare_bonds(molecules, names, bonds, indices, cfg)
+    out = {"molecules": molecules, "names": names, "bonds": bonds, "indices": indices,
+           "b4_idx": np.array([[x[0], x[1], x[2], x[3], x[5]] for x in b4],
+                              dtype=np.int64).reshape(-1, 5),
+           "bb_index": np.asarray(bbi, dtype=np.int64)}
+    keys = ["b2a", "b2b", "b2r0", "b2k", "b3a", "b3b", "b3c", "b3t0", "b3k",
+            "b4a", "b4b", "b4c", "b4d", "b4coeff", "b4type", "b4last"]
+    for k, v in zip(keys, packed):
+        out[f"packed/{k}"] = np.asarray(v)
+    np.savez(os.path.join(HERE, "topology_random.npz"), **out)
+    print("wrote", os.path.join(HERE, "topology_random.npz"), "terms:", len(b2), len(b3),
+          len(b4), "bb:", len(bbi))
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    main(ref)
+    random_topology(ref)

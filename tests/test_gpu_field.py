@@ -297,6 +297,61 @@ def test_fused_spectral_path_matches_oracle_and_library_path(mesh, T):
     pm.check_errors()
 
 
+@pytest.mark.parametrize("mesh,T", [((32, 32, 32), 3), ((64, 64, 64), 5), ((24, 24, 24), 2),
+                                    ((128, 128, 128), 3)])
+def test_fused_spectral_tile_widths(mesh, T):
+    """Every k-space tile width the mesh allows gives bit-identical forces
+    (field and PIC); the energy sums change only through the grouping of
+    their per-thread FP32 partials (to 1e-7, well inside the 1e-6 energy
+    tolerance).  A width the mesh does not allow is refused."""
+    from hymd_gb300 import _lib
+    cfg, ham, fun, r, types = make_system(sum(mesh) + T + 1, n=3000, T=T, mesh=mesh)
+    gf, pm, fl, _, _, R, Ty = _setup(cfg, ham, r, types)
+    pm.set_functional(ham)
+    widths = pm.spectral_tiles_allowed
+    assert pm.spectral_tile in widths and len(widths) >= 2
+    for w in (2, 32):
+        with pytest.raises(_lib.HPFError):
+            pm.spectral_tile = w
+    if mesh[1] % 16:
+        assert 16 not in widths
+    q = torch.as_tensor(np.where(np.arange(len(r)) % 7 == 0, 1.0, 0.0).astype(np.float32)
+                        - np.where(np.arange(len(r)) % 7 == 3, 1.0, 0.0).astype(np.float32),
+                        device="cuda")
+    out = []
+    for w in widths:
+        pm.spectral_tile = w
+        assert pm.spectral_tile == w
+        F, E = torch.zeros_like(R), torch.zeros_like(R)
+        sums, sq = _lib.new_workspace(R.device), _lib.new_workspace(R.device)
+        _lib.call("hpf_field_step", pm._h, _lib.ptr(R), _lib.ptr(Ty), R.shape[0],
+                  _lib.dvec(cfg.m), _lib.ptr(F), _lib.ptr(sums), None, None, _lib.stream_ptr())
+        _lib.call("hpf_pic_step", pm._h, _lib.ptr(R), _lib.ptr(q), R.shape[0], 1.7, _lib.ptr(E),
+                  None, None, None, None, _lib.ptr(sq), None, _lib.stream_ptr())
+        torch.cuda.synchronize()
+        out.append((F.cpu().numpy(), E.cpu().numpy(), sums[:4].cpu().numpy(),
+                    sq[:1].cpu().numpy()))
+    for o in out[1:]:
+        assert np.array_equal(o[0], out[0][0]) and np.array_equal(o[1], out[0][1])
+        np.testing.assert_allclose(o[2], out[0][2], rtol=1e-7)
+        np.testing.assert_allclose(o[3], out[0][3], rtol=1e-7)
+    pm.check_errors()
+
+
+def test_md_prime_tunes_the_spectral_tile():
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.homopolymer_melt()
+    md = RespaMD(s["positions"], s["velocities"], s["types"], s["config"],
+                 get_hamiltonian(s["config"]), topology=s["topology"])
+    md.prime()
+    allowed = md.pm.spectral_tiles_allowed
+    assert set(md.spectral_tile_timings) == set(allowed)
+    best = min(md.spectral_tile_timings, key=md.spectral_tile_timings.get)
+    assert md.pm.spectral_tile == best
+
+
 def test_fused_spectral_path_availability():
     from hymd_gb300 import _lib
     from hymd_gb300.field import ParticleMesh
@@ -308,6 +363,9 @@ def test_fused_spectral_path_availability():
         assert not pm.spectral_available and pm.spectral == "cufft"
         with pytest.raises(_lib.HPFError):
             pm.spectral = "fused"
+        assert pm.spectral_tile == 0 and pm.spectral_tiles_allowed == []
+        with pytest.raises(_lib.HPFError):
+            pm.spectral_tile = 8
 
 
 @pytest.mark.parametrize("mesh", [(32, 32, 32), (64, 16, 32), (16, 128, 64), (48, 48, 48)])

@@ -89,6 +89,51 @@ def test_prepare_bonds_molecules_with_solvent(golden):
         assert np.array_equal(v, t["mws/packed/" + k]), k
 
 
+def random_topology_case(golden):
+    """Inputs and reference outputs of topology_random.npz, with the term
+    types rebuilt (as this package's dataclasses) from the generator."""
+    import importlib.util
+    import os
+    from hymd_gb300.force import Angle, Bond, Dihedral
+    path = os.path.join(os.path.dirname(__file__), "golden", "make_golden.py")
+    spec = importlib.util.spec_from_file_location("make_golden", path)
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    molecules, names, bonds, indices, bt, at, dt = mg.random_molecules()
+    t = golden("topology_random.npz")
+    for k, v in (("molecules", molecules), ("names", names), ("bonds", bonds),
+                 ("indices", indices)):
+        assert np.array_equal(t[k], v), k
+
+    class C:
+        pass
+    c = C()
+    c.bonds = [Bond(a, b, r0, k) for a, b, r0, k in bt]
+    c.angle_bonds = [Angle(atom_1=a, atom_2=b, atom_3=x, equilibrium=e, strength=k)
+                     for a, b, x, e, k in at]
+    c.dihedrals = [Dihedral(a, b, x, d, co, ty) for a, b, x, d, co, ty in dt]
+    return t, c
+
+
+PACKED_KEYS = ["b2a", "b2b", "b2r0", "b2k", "b3a", "b3b", "b3c", "b3t0", "b3k",
+               "b4a", "b4b", "b4c", "b4d", "b4coeff", "b4type", "b4last"]
+
+
+def test_prepare_bonds_random_molecules_bit_exact_with_reference(golden):
+    """Branched and ring molecules with scrambled ids, duplicate, reversed and
+    equal-coefficient term types: the packed arrays equal the reference's."""
+    from hymd_gb300.force import prepare_bonds, prepare_bonds_old
+    t, c = random_topology_case(golden)
+    _, _, b4, bbi = prepare_bonds_old(t["molecules"], t["names"], t["bonds"], t["indices"], c)
+    assert np.array_equal(np.array([[x[0], x[1], x[2], x[3], x[5]] for x in b4],
+                                   dtype=np.int64).reshape(-1, 5), t["b4_idx"])
+    assert np.array_equal(np.asarray(bbi, dtype=np.int64), t["bb_index"])
+    packed = prepare_bonds(t["molecules"], t["names"], t["bonds"], t["indices"], c)
+    for k, v in zip(PACKED_KEYS, packed):
+        ref = t["packed/" + k]
+        assert v.dtype == ref.dtype and np.array_equal(v, ref), k
+
+
 def test_traversal_order_matches_networkx_on_random_graphs():
     nx = pytest.importorskip("networkx")
     from hymd_gb300.force import _bfs_paths, _simple_paths
