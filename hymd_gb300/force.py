@@ -159,7 +159,7 @@ def _simple_paths(adj, u, n):
 def _dihedral_classes(dihedral_types):
     """Class of each dihedral type: the index of the first type with equal
     coefficients and dihedral type.  The reference's duplicate test
-    (force.py:476-487) compares a reversed term by its indices, coefficients
+    (force.py:476-487, `... not in bonds_4`) compares a reversed term by its indices, coefficients
     and type, so types equal in both are one type for it."""
     cls = []
     for i, a in enumerate(dihedral_types):
