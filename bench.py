@@ -416,12 +416,11 @@ def run_gpu(args):
     for a, b in e2e_evs:
         flush.zero_()
         a.record(st)
-        md.r.copy_(r_h, non_blocking=True)
-        md.v.copy_(v_h, non_blocking=True)
-        md.run(1)
-        r_out.copy_(md.r, non_blocking=True)
+        md.run_host(r_h, v_h, r_out)
         b.record(st)
     torch.cuda.synchronize()
+    if not torch.equal(r_out, md.r.cpu()):
+        raise RuntimeError("end-to-end step: the positions read back differ from the device's")
     e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_evs) / args.steps
 
     # ---- roofline -------------------------------------------------------------
@@ -483,7 +482,9 @@ def run_gpu(args):
                                          "kspace_tile": md.pm.spectral_tile,
                                          "kspace_tile_tuning_us": md.spectral_tile_timings}),
                 "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "steps/s",
-                        "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 12 * n},
+                        "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 12 * n,
+                        "transfer": "RespaMD.run_host: DMA copies from/to page-locked host "
+                                    "memory"},
                 "gpu_launches": md.launches_per_step * args.steps,
                 "roofline": {"kernel": "k_respa_warp (fused rRESPA inner loop, "
                                        f"{cfg.respa_inner} inner steps per launch)",

@@ -365,7 +365,7 @@ __global__ void k_readout(const float* __restrict__ fm, const float* __restrict_
         }
     }
     if (MODE == 2) {
-        if (grid_reduce_store_f<8>(acc, ws_partials(kd.ws), ws_ticket(kd.ws), kd.ws))
+        if (grid_reduce_store_f<8, kThreads>(acc, ws_partials(kd.ws), ws_ticket(kd.ws), kd.ws))
             csvr_update(kd.a, kd.ws, kd.randoms, kd.counter, kd.state, err);
     }
 }

@@ -402,11 +402,51 @@ __device__ __forceinline__ void warp_df_reduce(DF (&v)[K]) {
     }
 }
 
+// Block sum of K float values per thread for blocks of exactly NT threads:
+// the values are transposed through shared memory, so that each warp sums
+// only its share of the K values (NT/32 elements per lane, then one
+// double-float shuffle tree per value, the trees advancing together) instead
+// of every warp reducing all K and one warp reducing the warps' results.
+// Fixed order, so deterministic.  Writes partials like block_partials_f.
+template <int K, int NT>
+__device__ __forceinline__ void block_partials_ft(float (&vf)[K], double* partials,
+                                                  unsigned int G) {
+    static_assert(NT % 32 == 0 && NT >= 32 && NT <= 1024, "whole warps");
+    constexpr int NW = NT / 32, KW = (K + NW - 1) / NW;
+    __shared__ float tr[K][NT];
+#pragma unroll
+    for (int k = 0; k < K; ++k) tr[k][threadIdx.x] = vf[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    DF v[KW];
+#pragma unroll
+    for (int i = 0; i < KW; ++i) {
+        const int k = warp + i * NW;
+        v[i] = DF{0.0f, 0.0f};
+        if (k < K) {
+            v[i] = DF{tr[k][lane], 0.0f};
+#pragma unroll
+            for (int j = 1; j < NW; ++j) v[i] = df_add(v[i], DF{tr[k][lane + 32 * j], 0.0f});
+        }
+    }
+    warp_df_reduce<KW>(v);
+    if (lane == 0) {
+        float2* part = reinterpret_cast<float2*>(partials);
+#pragma unroll
+        for (int i = 0; i < KW; ++i) {
+            const int k = warp + i * NW;
+            if (k < K) part[(size_t)k * G + blockIdx.x] = make_float2(v[i].hi, v[i].lo);
+        }
+    }
+}
+
 // Block sum of K float values in double-float (TwoSum) arithmetic, written
 // value-major as partials[k * G + blockIdx.x] (float2 hi/lo); G = number of
-// partial slots per value (the grid size).  All threads must call it.
+// partial slots per value (the grid size).  All threads must call it.  Any
+// block size: every warp reduces all K values, then warp 0 the warps' sums.
 template <int K>
-__device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partials, unsigned int G) {
+__device__ __forceinline__ void block_partials_fg(float (&vf)[K], double* partials,
+                                                  unsigned int G) {
     __shared__ float2 red_p[K * 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (blockDim.x + 31) >> 5;
@@ -434,6 +474,14 @@ __device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partial
             for (int k = 0; k < K; ++k) part[(size_t)k * G + blockIdx.x] = make_float2(t[k].hi, t[k].lo);
         }
     }
+}
+
+// block_partials_fg, or with NT > 0 (the block has exactly NT threads) the
+// transposed form block_partials_ft.
+template <int K, int NT = 0>
+__device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partials, unsigned int G) {
+    if constexpr (NT > 0) block_partials_ft<K, NT>(vf, partials, G);
+    else block_partials_fg<K>(vf, partials, G);
 }
 
 // Sum of the G block partials of each of K values (written by
@@ -490,11 +538,11 @@ __device__ __forceinline__ void final_partials_f(const double* partials, unsigne
 // then the last block to finish (ticket) sums them in a fixed order into
 // out[0..K).  Returns true on thread 0 of that last block (out is final
 // there); the ticket is reset for the next launch.
-template <int K>
+template <int K, int NT = 0>
 __device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* partials,
                                                     unsigned int* ticket, double* out) {
     __shared__ bool is_last;
-    block_partials_f<K>(vf, partials, gridDim.x);
+    block_partials_f<K, NT>(vf, partials, gridDim.x);
     if (threadIdx.x == 0) {
         __threadfence();
         unsigned int t = atomicAdd(ticket, 1u);

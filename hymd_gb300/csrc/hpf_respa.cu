@@ -382,7 +382,7 @@ k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     } else if (!forces_only) {
         free_beads(p, blockIdx.x - n_grp_blocks, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
-    if (out) block_partials_f<kOut>(acc, p.partials, gridDim.x);
+    if (out) block_partials_f<kOut, kThreads>(acc, p.partials, gridDim.x);
 }
 
 template <bool DIH>
@@ -402,7 +402,7 @@ k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     } else if (!forces_only) {
         free_beads(p, blockIdx.x - p.n_groups, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
-    if (out) block_partials_f<kOut>(acc, p.partials, gridDim.x);
+    if (out) block_partials_f<kOut, kThreads>(acc, p.partials, gridDim.x);
 }
 
 // Sum of the block partials (fixed order) into out[0..kOut), then the

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             }
         }
     }
-    if (sums) grid_reduce_store_f<4>(acc, partials, ticket, sums);
+    if (sums) grid_reduce_store_f<4, kSpecThreads>(acc, partials, ticket, sums);
 }
 
 // PIC_Spectral variant of pass B (hymd/field.py:241-403, the library path's
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             }
         }
     }
-    if (sums) grid_reduce_store_f<1>(acc, partials, ticket, sums);
+    if (sums) grid_reduce_store_f<1, kSpecThreads>(acc, partials, ticket, sums);
 }
 
 // ------------------------------------------------------------ pass C ---

@@ -569,6 +569,24 @@ class RespaMD:
             else:
                 self.step()
 
+    def run_host(self, r_in, v_in, r_out, steps=1):
+        """`steps` outer steps, each from a host-side state: positions and
+        velocities are copied in from the page-locked host tensors r_in, v_in
+        before the step and the positions copied out to r_out after it
+        (stream-ordered DMA copies; the CPU-GPU link moves about 200 GB/s each
+        way, and a copy kernel reading the mapped host memory was no faster).
+        Host tensors are (N, 3) float32 in this object's bead order
+        (`in_input_order` maps back)."""
+        for t in (r_in, v_in, r_out):
+            if t.device.type != "cpu" or not t.is_pinned() or t.dtype != torch.float32 \
+                    or tuple(t.shape) != (self.n, 3):
+                raise ValueError("run_host: page-locked float32 (N, 3) host tensors")
+        for _ in range(steps):
+            self.r.copy_(r_in, non_blocking=True)
+            self.v.copy_(v_in, non_blocking=True)
+            self.run(1)
+            r_out.copy_(self.r, non_blocking=True)
+
     # ------------------------------------------------------------------
     def energies(self):
         """(bond, angle, dihedral) energies of the last inner step (FP64)."""

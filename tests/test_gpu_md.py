@@ -185,3 +185,28 @@ def test_sorted_bead_order_gives_the_same_trajectory(thermostat):
         assert torch.equal(rb, a.r) and torch.equal(vb, a.v)
     a.check_errors()
     b.check_errors()
+
+
+def test_run_host_matches_device_resident_steps():
+    """RespaMD.run_host (state copied in from page-locked host tensors, the
+    captured step, positions copied out) equals the device-resident replay."""
+    from hymd_gb300.md import RespaMD
+    s, cfg, ham, fun = _melt()
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    for m in (a, b):
+        m.prime()
+        m.capture()
+    torch.cuda.synchronize()
+    r_h = a.r.cpu().pin_memory()
+    v_h = a.v.cpu().pin_memory()
+    r_out = torch.empty_like(r_h).pin_memory()
+    a.run_host(r_h, v_h, r_out)
+    b.run(1)
+    torch.cuda.synchronize()
+    assert torch.equal(r_out, a.r.cpu())
+    assert torch.equal(r_out, b.r.cpu())
+    assert torch.equal(a.v, b.v)
+    with pytest.raises(ValueError):
+        a.run_host(r_h.clone(), v_h, r_out)  # not page-locked
+    a.check_errors()
