@@ -470,6 +470,10 @@ def run_gpu(args):
                "sample": f"2 outer steps of the full workload on the oracle "
                          f"(FP64 numpy field + C bonded), {c_secs:.1f} s"}
     if rank == 0:
+        info = md.plan_info() or {}
+        # one warp per molecule group up to 64 beads, one CTA per group beyond
+        warp = max(md.block_beads or 0, info.get("max_block_beads", 0)) <= 64
+        respa_kernel = "k_respa_warp" if warp else "k_respa_cta"
         line = {"metric": METRIC, "value": sps * ws, "unit": "steps/s", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -486,7 +490,7 @@ def run_gpu(args):
                         "transfer": "RespaMD.run_host: DMA copies from/to page-locked host "
                                     "memory"},
                 "gpu_launches": md.launches_per_step * args.steps,
-                "roofline": {"kernel": "k_respa_warp (fused rRESPA inner loop, "
+                "roofline": {"kernel": f"{respa_kernel} (fused rRESPA inner loop, "
                                        f"{cfg.respa_inner} inner steps per launch)",
                              "bound": "hbm", "achieved": respa_gbs, "peak": peak, "unit": "GB/s",
                              "frac": respa_gbs / peak, "traffic": traffic.get("respa"),

@@ -228,7 +228,7 @@ __global__ void k_kspace_force(const float2* __restrict__ phi_raw, float2* __res
             acc[3] = fmaf(wq, kz * kz, acc[3]);
         }
     }
-    if (sums) grid_reduce_store_f<4>(acc, partials, ticket, sums);
+    if (sums) grid_reduce_store_f<4, kThreads>(acc, partials, ticket, sums);
 }
 
 template <int TT>
@@ -649,7 +649,7 @@ __global__ void k_adjoint_sums(const float2* __restrict__ spec, int64_t Mc, KGeo
         }
         acc[P] = fmaf(wk * k2, q, acc[P]);
     }
-    grid_reduce_store_f<P + 1>(acc, partials, ticket, out);
+    grid_reduce_store_f<P + 1, kThreads>(acc, partials, ticket, out);
 }
 
 // ------------------------------------------------------------ host glue ---
@@ -1571,7 +1571,7 @@ __global__ void k_gpe_pol(const float* __restrict__ eta, const float* __restrict
         if ((threadIdx.x & 31) == 0) atomicMax(max_bits, __float_as_uint(loc));
     } else {
         float acc[1] = {loc};
-        grid_reduce_store_f<1>(acc, ws_partials(ws), ws_ticket(ws), ws);
+        grid_reduce_store_f<1, kThreads>(acc, ws_partials(ws), ws_ticket(ws), ws);
     }
 }
 
@@ -1594,7 +1594,7 @@ __global__ void k_gpe_vbar(const float* __restrict__ E, const float* __restrict_
         if (dot_out) dot_out[e] = d;
         acc[0] = fmaf(pe, d, acc[0]);
     }
-    if (grid_reduce_store_f<1>(acc, ws_partials(ws), ws_ticket(ws), ws) && energy)
+    if (grid_reduce_store_f<1, kThreads>(acc, ws_partials(ws), ws_ticket(ws), ws) && energy)
         *energy = bs->dV * half_e0_d * ws[0];  // the current (device) box
 }
 
@@ -1906,7 +1906,7 @@ __global__ void k_vjp_kspace(const float2* __restrict__ rho_k, float2* phi_k, in
             phi_k[(int64_t)j * Mc + idx] = make_float2(ux * h2m, uy * h2m);
         }
     }
-    if (dQ) grid_reduce_store_f<K>(acc, partials, ticket, dQ);
+    if (dQ) grid_reduce_store_f<K, kThreads>(acc, partials, ticket, dQ);
 }
 
 }  // namespace

@@ -477,11 +477,14 @@ __device__ __forceinline__ void block_partials_fg(float (&vf)[K], double* partia
 }
 
 // block_partials_fg, or with NT > 0 (the block has exactly NT threads) the
-// transposed form block_partials_ft.
+// transposed form block_partials_ft, as long as its shared-memory transpose
+// stays within 16 KB (many values fall back to the per-warp form).
 template <int K, int NT = 0>
 __device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partials, unsigned int G) {
-    if constexpr (NT > 0) block_partials_ft<K, NT>(vf, partials, G);
-    else block_partials_fg<K>(vf, partials, G);
+    if constexpr (NT > 0 && (size_t)K * NT * sizeof(float) <= 16384)
+        block_partials_ft<K, NT>(vf, partials, G);
+    else
+        block_partials_fg<K>(vf, partials, G);
 }
 
 // Sum of the G block partials of each of K values (written by

@@ -81,7 +81,7 @@ __global__ void k_sum_v2(const float* __restrict__ v, int64_t n3, double* out) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n3;
          e += (int64_t)gridDim.x * blockDim.x)
         acc[0] = fmaf(v[e], v[e], acc[0]);
-    grid_reduce_store_f<1>(acc, ws_partials(out), ws_ticket(out), out);
+    grid_reduce_store_f<1, kThreads>(acc, ws_partials(out), ws_ticket(out), out);
 }
 
 // sum_e x[e] (y == NULL) or sum_e x[e] * y[e], accumulated in FP64
@@ -125,7 +125,7 @@ __global__ void k_csvr_sums_alpha(float* __restrict__ v, const int32_t* __restri
         acc[4 * g + 2] += z;
         acc[4 * g + 3] += fmaf(x, x, fmaf(y, y, z * z));
     }
-    if (!grid_reduce_store_f<8>(acc, ws_partials(ws), ws_ticket(ws), ws)) return;
+    if (!grid_reduce_store_f<8, kThreads>(acc, ws_partials(ws), ws_ticket(ws), ws)) return;
     csvr_update(a, ws, randoms, counter, state, err);
 }
 
@@ -163,7 +163,7 @@ __global__ void k_scr_sums_alpha(const float* __restrict__ v, int64_t n3, double
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n3;
          e += (int64_t)gridDim.x * blockDim.x)
         acc[0] = fmaf(v[e], v[e], acc[0]);
-    if (!grid_reduce_store_f<1>(acc, ws_partials(ws), ws_ticket(ws), ws)) return;
+    if (!grid_reduce_store_f<1, kThreads>(acc, ws_partials(ws), ws_ticket(ws), ws)) return;
     scr_update(a, ws[0], field, bonded, randoms, counter, bs, fun, state, err);
 }
 
