@@ -51,13 +51,20 @@ struct TypeScaleD {
 __global__ void k_paint(const float* pos, const int32_t* __restrict__ types,
                         const float* __restrict__ charges, int64_t n, int T,
                         const BoxState* __restrict__ bs, unsigned long long* __restrict__ acc,
-                        int64_t M, int* err, const double* __restrict__ scale) {
+                        int64_t M, int* err, const double* __restrict__ scale,
+                        const int32_t* __restrict__ idx = nullptr, int64_t n_total = 0) {
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
     const float al = scale ? (float)*scale : 1.0f;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        // idx: paint only the listed beads (a compact list of the charged ones)
+        const int64_t i = idx ? (int64_t)idx[j] : j;
+        if (idx && (i < 0 || i >= n_total)) {
+            hpf_flag(err, HPF_ERR_INDEX);
+            continue;
+        }
         float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
         if (scale) {
             x = x * al;
@@ -305,13 +312,20 @@ template <int MODE>
 __global__ void k_readout(const float* __restrict__ fm, const float* __restrict__ pos,
                           const int32_t* __restrict__ types, const float* __restrict__ charges,
                           int64_t n, int T, int64_t M, const BoxState* __restrict__ bs,
-                          float* __restrict__ force, int* err, KickDev kd) {
+                          float* __restrict__ force, int* err, KickDev kd,
+                          const int32_t* __restrict__ idx = nullptr, int64_t n_total = 0) {
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        // idx: read out only the listed beads (MODE 0; the others are untouched)
+        const int64_t i = idx ? (int64_t)idx[j] : j;
+        if (idx && (i < 0 || i >= n_total)) {
+            hpf_flag(err, HPF_ERR_INDEX);
+            continue;
+        }
         const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
         float out[3] = {0.0f, 0.0f, 0.0f};
         int t = types ? types[i] : 0;
@@ -771,14 +785,16 @@ int launch_kspace_force(hpf_ctx* c, const float2* phi_raw, float2* force_k, floa
 
 int do_paint(hpf_ctx* c, const float* pos, const int32_t* types, const float* charges,
              int64_t n, int G, const TypeScale& sc, float* out, cudaStream_t st,
-             const double* scale = nullptr, bool finalize = true) {
+             const double* scale = nullptr, bool finalize = true,
+             const int32_t* idx = nullptr, int64_t n_total = 0) {
     // G = number of grids (T for densities; 1 for charges, painted into the
-    // accumulator slot after the T density slots)
+    // accumulator slot after the T density slots); idx: paint only the n
+    // listed beads of n_total
     unsigned long long* acc = c->d_acc + (charges ? (int64_t)c->T * c->M : 0);
     if (n > 0) {
         k_paint<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, types, charges, n,
                                                            charges ? 1 : c->T, c->d_box, acc,
-                                                           c->M, c->d_err, scale);
+                                                           c->M, c->d_err, scale, idx, n_total);
         HPF_LAUNCH_CHECK();
     }
     if (!finalize) return HPF_OK;  // the fused spectral pass reads the accumulators
@@ -1302,6 +1318,48 @@ int hpf_pic_step(hpf_ctx* c, const float* pos, const float* charges, int64_t n,
     if (n > 0)
         return launch_readout(c, c->d_grid + c->M, pos, nullptr, charges, n, 1, elec_forces, kick,
                               st);
+    return HPF_OK;
+}
+
+int hpf_pic_step_list(hpf_ctx* c, const float* pos, const float* charges, const int32_t* idx,
+                      int64_t count, int64_t n, double elec_factor, float* elec_forces,
+                      double* sums, const HpfKick* kick, void* stream) {
+    if (!c || n < 0 || count < 0 || count > n ||
+        (count > 0 && (!pos || !charges || !idx || !elec_forces)))
+        return HPF_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    TypeScale sc;
+    sc.s[0] = 1.0f;
+    const float four_pi_fac = (float)(4.0 * 3.14159265358979323846 * elec_factor);
+    int r;
+    if ((r = do_paint(c, pos, nullptr, charges, count, 1, sc, c->d_grid, st, nullptr,
+                      !c->spec_fused, idx, n)) != HPF_OK)
+        return r;
+    if (c->spec_fused) {
+        if ((r = spectral_pic(c, four_pi_fac, false, sums, st)) != HPF_OK) return r;
+    } else {
+        if ((r = exec_r2c(c, c->d_grid, c->d_spec_phi, 1, st)) != HPF_OK) return r;
+        KGeom g = kgeom(c);
+        const int kg = sums ? reduce_grid(c->Mc, kThreads) : grid_for(c->Mc, kThreads);
+        k_kspace_pic<<<kg, kThreads, 0, st>>>(c->d_spec_phi, c->d_spec, c->Mc, g, c->d_box,
+                                              c->d_fun, four_pi_fac, sums, ws_partials(c->d_ws),
+                                              ws_ticket(c->d_ws));
+        HPF_LAUNCH_CHECK();
+        if ((r = exec_c2r(c, c->d_spec, c->d_grid, 4, st)) != HPF_OK) return r;
+    }
+    // with a kick every bead is visited (the kick and the CSVR sums cover all;
+    // the readout gathers only where q != 0), as in hpf_pic_step
+    if (kick && n > 0)
+        return launch_readout(c, c->d_grid + c->M, pos, nullptr, charges, n, 1, elec_forces, kick,
+                              st);
+    if (count > 0) {
+        KickDev kd;
+        memset(&kd, 0, sizeof(kd));
+        k_readout<0><<<grid_for(count, kThreads), kThreads, 0, st>>>(
+            c->d_grid + c->M, pos, nullptr, charges, count, 1, c->M, c->d_box, elec_forces,
+            c->d_err, kd, idx, n);
+        HPF_LAUNCH_CHECK();
+    }
     return HPF_OK;
 }
 

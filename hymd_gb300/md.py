@@ -52,9 +52,11 @@ class RespaMD:
             self.topo = BondedTopology(topology, device=self.device)
         self.charges = None
         self.f_elec = None
+        self.charged = None
         if charges is not None:
             self.charges = torch.as_tensor(np.asarray(charges, np.float32), device=self.device)
             self.f_elec = z()
+            self._index_charged()
             self.elec_factor = config.coulomb_constant / config.dielectric_const
         self.ws_bond = _lib.new_workspace(self.device)
         self.ws_angle = _lib.new_workspace(self.device)
@@ -92,8 +94,11 @@ class RespaMD:
         kinds = 0 if t is None else (int(t.n_bonds > 0) + int(t.n_angles > 0)
                                      + int(t.n_dihedrals > 0))
         # kernels of this library per outer step (cuFFT's own kernels and
-        # memsets not counted): field step = paint, finalize, k-space, readout
-        field = 4 + (4 if charges is not None else 0)
+        # memsets not counted): a field evaluation is paint, spectral passes
+        # A, B, C and readout on the fused path, paint, finalize, k-space and
+        # readout around cuFFT otherwise; PIC adds a second one
+        per_field = 5 if self.pm.spectral == "fused" else 4
+        field = per_field * (2 if charges is not None else 1)
         if self.plan is not None:
             # fused inner kernel + its one-block finish (sums, barostat); the
             # second kick is fused into the readout
@@ -212,6 +217,8 @@ class RespaMD:
                 _lib.lib().hpf_respa_plan_destroy(self.plan)
                 self.plan = self._make_plan(self._packed, self.block_beads)
         self.perm = perm if self.perm is None else self.perm[perm]
+        if self.charges is not None:
+            self._index_charged()
         return self.perm
 
     def in_input_order(self, t):
@@ -383,6 +390,11 @@ class RespaMD:
                 _lib.ptr(self.f_angle) if t.n_angles else None,
                 _lib.ptr(self.f_dih) if t.n_dihedrals else None)
 
+    def _index_charged(self):
+        """Indices of the charged beads (int32, device), the only ones the
+        MD loop's charge paint visits."""
+        self.charged = torch.nonzero(self.charges != 0).reshape(-1).to(torch.int32).contiguous()
+
     def _kick_args(self, thermostat):
         """HpfKick for the second outer half kick fused into the last readout
         (with the CSVR sums when the thermostat is on)."""
@@ -410,9 +422,11 @@ class RespaMD:
                   self.masses, _lib.ptr(self.f_field), _lib.ptr(sums),
                   None if pos_scale is None else _lib.ctypes.c_void_p(pos_scale), last_kick, st)
         if self.charges is not None:
-            _lib.call("hpf_pic_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.charges),
-                      self.n, float(self.elec_factor), _lib.ptr(self.f_elec), None, None, None,
-                      None, None, kick, st)
+            # the charge paint visits only the charged beads; the readout (with
+            # the kick and the CSVR sums) visits all
+            _lib.call("hpf_pic_step_list", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.charges),
+                      _lib.ptr(self.charged), self.charged.numel(), self.n,
+                      float(self.elec_factor), _lib.ptr(self.f_elec), None, kick, st)
 
     # autotune the fused k-space pass's tile width in prime()
     TUNE_SPECTRAL_TILE = True

@@ -319,6 +319,17 @@ int hpf_pic_step(hpf_ctx* ctx, const float* pos, const float* charges, int64_t n
                  double elec_factor, float* elec_forces, float* phi_q, float* psi,
                  float* elec_field, void* psi_k, double* sums, const HpfKick* kick,
                  void* stream);
+/* The same PIC step with the charge paint over a compact list of beads (the
+ * charged ones): idx int32[count] (device) holds bead indices in [0, n).
+ * Only those beads are painted (the reference paints every bead,
+ * field.py:356-369, where q = 0 beads add nothing).  Without a kick only the
+ * listed rows of elec_forces are read out and written (the others keep their
+ * values); with a kick every bead is visited, as in hpf_pic_step (zero force
+ * where q = 0), so that the kick and the CSVR sums cover all beads.  No grids
+ * are returned.  sums as for hpf_pic_step. */
+int hpf_pic_step_list(hpf_ctx* ctx, const float* pos, const float* charges, const int32_t* idx,
+                      int64_t count, int64_t n, double elec_factor, float* elec_forces,
+                      double* sums, const HpfKick* kick, void* stream);
 
 /* ---- bonded (f2py calling form, hymd/force.py:8-23, main.py:509-550) ------
  * All three zero their force array first, as the Fortran does.  Indices are
