@@ -14,6 +14,9 @@
 // therefore collapses to one pass over the half spectrum:
 //   F_d(k) = -i k_d H(k)^2 (Q phi(k))/M, with no real-space intermediates.
 #include <math.h>
+#include <stdint.h>
+
+#include <atomic>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -44,7 +47,8 @@ struct TypeScaleD {
 
 // ---------------------------------------------------------------- paint ---
 // One thread per particle; 8 CIC deposits as 64-bit fixed-point integer
-// atomics (weight * 2^32), so the accumulated grid is independent of the
+// atomics (the weight in units of 2^-24, kFixScale, converted to int32 and
+// summed in int64), so the accumulated grid is independent of the
 // order in which deposits land: the density is bit-deterministic.
 // With `scale` (a barostat's alpha, device double), the positions are first
 // rescaled in place, r = float(alpha) * r (hymd/barostat_scr.py:128).
@@ -798,7 +802,9 @@ int do_paint(hpf_ctx* c, const float* pos, const int32_t* types, const float* ch
         HPF_LAUNCH_CHECK();
     }
     if (!finalize) return HPF_OK;  // the fused spectral pass reads the accumulators
-    if (c->M % 4 == 0) {
+    // float4 stores need a 16-byte aligned destination (a caller's view may
+    // start at any element)
+    if (c->M % 4 == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
         dim3 grid(grid_for(c->M / 4, kThreads), G);
         k_paint_finalize<<<grid, kThreads, 0, st>>>(acc, out, c->M, G, sc, c->d_box);
     } else {
@@ -1372,7 +1378,10 @@ int hpf_pic_step_list(hpf_ctx* c, const float* pos, const float* charges, const 
 // The scratch is shared by every call on a device, so calls that overlap (on
 // two streams or two host threads) race.  The first call on a device loads
 // the module and looks up the array's address, so it should come before any
-// stream capture.
+// stream capture.  Every call made outside a capture looks the address up
+// again (a host-side table lookup once the module is loaded), so a context
+// that was destroyed and created again (cudaDeviceReset) is followed; a call
+// under capture uses the address of the last call outside one.
 namespace {
 
 constexpr int64_t kStaticPaintCells = (int64_t)1 << 21;  // T * n0 * n1 * n2 at most (16 MiB)
@@ -1383,21 +1392,26 @@ constexpr int kStaticMaxDevices = 64;
 static __device__ __align__(256) unsigned long long
     g_paint_static_scratch[kStaticBoxBytes / 8 + kStaticPaintCells];
 
-char* g_paint_static_addr[kStaticMaxDevices];  // per device, set by the first call
+// per device: the array's address from the last lookup outside a capture
+std::atomic<char*> g_paint_static_addr[kStaticMaxDevices];
 
 __global__ void k_store_box(BoxState bs, BoxState* dst) { *dst = bs; }
 
-int paint_static_scratch(char** out) {
+int paint_static_scratch(cudaStream_t st, char** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kStaticMaxDevices)
         return HPF_ERR_CUDA;
-    if (!g_paint_static_addr[dev]) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return HPF_ERR_CUDA;
+    if (cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_paint_static_scratch) != cudaSuccess || !p)
             return HPF_ERR_CUDA;
-        g_paint_static_addr[dev] = static_cast<char*>(p);
+        g_paint_static_addr[dev].store(static_cast<char*>(p), std::memory_order_release);
     }
-    *out = g_paint_static_addr[dev];
+    char* p = g_paint_static_addr[dev].load(std::memory_order_acquire);
+    if (!p) return HPF_ERR_ARG;  // first call on this device made under capture
+    *out = p;
     return HPF_OK;
 }
 
@@ -1412,12 +1426,12 @@ extern "C" int hpf_paint_static(const float* pos, const int32_t* types, int64_t 
     if (!(box[0] > 0 && box[1] > 0 && box[2] > 0)) return HPF_ERR_ARG;
     const int64_t M = (int64_t)n0 * n1 * n2;
     if (M > kStaticPaintCells || (int64_t)T * M > kStaticPaintCells) return HPF_ERR_SCRATCH_LIMIT;
+    cudaStream_t st = as_stream(stream);
     char* base = nullptr;
-    int r = paint_static_scratch(&base);
+    int r = paint_static_scratch(st, &base);
     if (r != HPF_OK) return r;
     BoxState* bs = reinterpret_cast<BoxState*>(base);
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(base + kStaticBoxBytes);
-    cudaStream_t st = as_stream(stream);
     BoxState h;
     memset(&h, 0, sizeof(h));
     const int nn[3] = {n0, n1, n2};
@@ -1433,7 +1447,7 @@ extern "C" int hpf_paint_static(const float* pos, const int32_t* types, int64_t 
                                                            d_err, nullptr);
         HPF_LAUNCH_CHECK();
     }
-    if (M % 4 == 0) {
+    if (M % 4 == 0 && (reinterpret_cast<uintptr_t>(phi_out) & 15) == 0) {
         dim3 grid(grid_for(M / 4, kThreads), T);
         k_paint_finalize<<<grid, kThreads, 0, st>>>(acc, phi_out, M, T, sc, bs);
     } else {

@@ -176,11 +176,23 @@ __device__ __forceinline__ void fill_box_state_dev(BoxState& s, float L0, float 
 }
 
 // CSVR scale factors (hymd/thermostat.py:167-219, Bussi-Parrinello 2008 form)
-// from the per-group sums ws[4g..4g+3] = (sum v_x, sum v_y, sum v_z, sum v^2),
-// run by one thread once the sums are final.  state[4g] = alpha,
-// state[4g+1..3] = the group's centre-of-mass velocity, state[8+g] += work.
-// The O(1) quantities have no cancellation and are formed in FP32 (FP64
-// division and square root are long sequences on GB300's FP64 pipe).
+// from the per-group sums ws[4g..4g+3] = (sum v_x, sum v_y, sum v_z, sum v^2)
+// taken before the thermostat, run by one thread once the sums are final.
+// The reference visits the coupling groups in order and each visit changes
+// the velocities the next one sees:
+//   * with centre-of-mass removal (and more than one particle in the group),
+//     K is the group's kinetic energy about its current COM velocity c, and
+//     only the group's particles move: v <- (v - c) alpha + c;
+//   * otherwise K is the whole system's current kinetic energy and every
+//     particle is scaled: v <- alpha v.
+// Each visit is affine in the pre-thermostat velocities, so the composition
+// is tracked per particle group h as v_final = A_h v + B_h, and the current
+// sums of a later visit follow from the pre-thermostat ones.  state[4h] = A_h,
+// state[4h+1..3] = B_h (what hpf_csvr_scale applies), state[8+g] += K (alpha^2 - 1)
+// (config.thermostat_work).  Every particle belongs to exactly one group (the
+// reference's check_thermostat_coupling_groups), so the group sums cover the
+// whole system.  alpha^2 is formed in FP32, as the O(1) factor has no
+// cancellation; K and the composed transforms are FP64.
 __device__ __forceinline__ void csvr_update(const HpfCsvrArgs& a, const double* ws,
                                             const double* randoms, int* counter, double* state,
                                             int* err) {
@@ -188,33 +200,57 @@ __device__ __forceinline__ void csvr_update(const HpfCsvrArgs& a, const double* 
     const bool ok = s >= 0 && s < a.n_steps;
     if (!ok) hpf_flag(err, HPF_ERR_INDEX);
     const bool act = !(a.every > 1 && (s + 1) % a.every != 0);
-    for (int g = 0; g < a.n_groups; ++g) {
-        state[4 * g] = 1.0;
-        for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = 0.0;
-        if (!act) continue;
-        const float N = (float)a.count[g];
-        const float iN = 1.0f / N;
-        float com[3] = {0, 0, 0};
+    const int ng = a.n_groups < 1 ? 1 : (a.n_groups > 2 ? 2 : a.n_groups);
+    double A[2] = {1.0, 1.0};
+    double B[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    for (int g = 0; act && g < ng; ++g) {
+        const double N = a.count[g];
+        const bool com = a.remove_com && N > 1.0;
+        double cnow[3] = {0.0, 0.0, 0.0};
         double K;
-        if (a.remove_com && N > 1) {
-            for (int d = 0; d < 3; ++d) com[d] = (float)ws[4 * g + d] * iN;
-            K = 0.5 * a.mass * (ws[4 * g + 3] - (double)N * (double)(com[0] * com[0] +
-                                                                      com[1] * com[1] +
-                                                                      com[2] * com[2]));
+        if (com) {
+            const double iN = 1.0 / N;
+            double c2 = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                const double c0 = ws[4 * g + d] * iN;
+                c2 += c0 * c0;
+                cnow[d] = A[g] * c0 + B[g][d];
+            }
+            K = 0.5 * a.mass * A[g] * A[g] * (ws[4 * g + 3] - N * c2);
         } else {
-            // without COM removal the reference uses the whole system's K
-            K = 0.5 * a.mass * (ws[3] + (a.n_groups > 1 ? ws[7] : 0.0));
+            K = 0.0;
+            for (int h = 0; h < ng; ++h) {
+                double bs = 0.0, bb = 0.0;
+                for (int d = 0; d < 3; ++d) {
+                    bs += B[h][d] * ws[4 * h + d];
+                    bb += B[h][d] * B[h][d];
+                }
+                K += A[h] * A[h] * ws[4 * h + 3] + 2.0 * A[h] * bs + a.count[h] * bb;
+            }
+            K *= 0.5 * a.mass;
         }
-        const float Kt = (float)(1.5 * a.gas_constant * a.count[g] * a.target_temperature);
-        const float Nf = 3.0f * N;
+        const float Kt = (float)(1.5 * a.gas_constant * N * a.target_temperature);
+        const float Nf = 3.0f * (float)N;
         const float R = ok ? (float)randoms[(int64_t)s * a.stride + a.offset + 2 * g] : 0.0f;
         const float S = ok ? (float)randoms[(int64_t)s * a.stride + a.offset + 2 * g + 1] : Nf - 1.0f;
         const float c = (float)a.c;
         const float q = Kt / (Nf * (float)K);
         const float alpha2 = c + (1.0f - c) * (S + R * R) * q + 2.0f * R * sqrtf(c * (1.0f - c) * q);
-        state[4 * g] = (double)sqrtf(alpha2);
-        for (int d = 0; d < 3; ++d) state[4 * g + 1 + d] = (double)com[d];
-        state[8 + g] += K * ((double)alpha2 - 1.0);  // thermostat work (config.thermostat_work)
+        const double al = (double)sqrtf(alpha2);
+        if (com) {
+            A[g] *= al;
+            for (int d = 0; d < 3; ++d) B[g][d] = al * (B[g][d] - cnow[d]) + cnow[d];
+        } else {
+            for (int h = 0; h < ng; ++h) {
+                A[h] *= al;
+                for (int d = 0; d < 3; ++d) B[h][d] *= al;
+            }
+        }
+        state[8 + g] += K * ((double)alpha2 - 1.0);
+    }
+    for (int h = 0; h < 2; ++h) {
+        state[4 * h] = A[h];
+        for (int d = 0; d < 3; ++d) state[4 * h + 1 + d] = B[h][d];
     }
     if (a.advance) *counter = s + 1;
 }

@@ -129,21 +129,19 @@ __global__ void k_csvr_sums_alpha(float* __restrict__ v, const int32_t* __restri
     csvr_update(a, ws, randoms, counter, state, err);
 }
 
+// v <- A_g v + B_g with the composed per-group transform csvr_update leaves
+// in state (the reference's group-by-group rescaling, thermostat.py:190-219).
+// `remove_com` is carried by the transform and not read here.
 __global__ void k_csvr_scale(float* __restrict__ v, const int32_t* __restrict__ group, int64_t n,
                              const double* __restrict__ state, int remove_com) {
+    (void)remove_com;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int g = group ? group[i] : 0;
         if (g < 0 || g > 1) continue;
         const float al = (float)state[4 * g];
-        for (int d = 0; d < 3; ++d) {
-            if (remove_com) {
-                const float c = (float)state[4 * g + 1 + d];
-                v[3 * i + d] = (v[3 * i + d] - c) * al + c;
-            } else {
-                v[3 * i + d] = v[3 * i + d] * al;
-            }
-        }
+        for (int d = 0; d < 3; ++d)
+            v[3 * i + d] = fmaf(al, v[3 * i + d], (float)state[4 * g + 1 + d]);
     }
 }
 

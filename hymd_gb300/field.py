@@ -431,11 +431,16 @@ def update_field_force_q_GPE(conv_fun, phi, types, charges, phi_q, phi_q_fourier
 
     `conv_fun` is the reference's convergence closure; the measure it stands
     for is taken from config.convergence_type (max_diff when unset, as
-    hymd/main.py:141-165 does).  phi_eps, phi_pol_prev and elec_field_contrib
-    keep their contents between calls, as in the reference; elec_forces is
-    written in place.  psi, elec_field and Vbar_elec are filled; the Fourier
-    grids of the argument list are scratch in the reference and not written.
-    Synchronises once per iteration (the convergence test)."""
+    hymd/main.py:141-165 does).  phi_eps and elec_field_contrib keep their
+    contents between calls where the reference's masked divisions leave them
+    (field.py:980,1066-1071); elec_forces is written in place.  psi,
+    elec_field and Vbar_elec are filled; the Fourier grids of the argument
+    list are scratch in the reference and not written.  The polarisation
+    iteration starts from phi_pol_prev on every call and neither phi_pol_prev
+    nor phi_pol is written: the reference rebinds both names locally
+    (field.py:1010-1024), so its caller's grids keep their initial zeros and
+    every solve starts cold.  Synchronises once per iteration (the
+    convergence test)."""
     T = pm.n_types
     pos = _lib.require_cuda(positions, "positions", torch.float32)
     n = pos.shape[0]
@@ -451,12 +456,16 @@ def update_field_force_q_GPE(conv_fun, phi, types, charges, phi_q, phi_q_fourier
     ef = pm.gpe["elec_field"] if hasattr(pm, "gpe") else pm.real_field(3)
     vb = pm.gpe["vbar"] if hasattr(pm, "gpe") else pm.real_field(T)
     dot = pm.real_field()
+    pol = getattr(pm, "gpe_pol", None)
+    if pol is None:
+        pol = pm.gpe_pol = pm.real_field()
+    pol.copy_(phi_pol_prev)  # the kernel iterates in place on this copy
     it = _lib.ctypes.c_int(0)
     _lib.call("hpf_gpe_step", pm._h, _lib.ptr(pos), _lib.ptr(typ), _lib.ptr(q), n,
               _lib.ptr(phi_all), _lib.dvec(eps), _lib.dvec(qt), float(config.coulomb_constant),
               float(config.conv_crit if config.conv_crit is not None else 1e-6),
               float(config.pol_mixing if config.pol_mixing is not None else 0.6), kind, 100,
-              _lib.ptr(phi_eps), _lib.ptr(phi_pol_prev), _lib.ptr(elec_field_contrib),
+              _lib.ptr(phi_eps), _lib.ptr(pol), _lib.ptr(elec_field_contrib),
               _lib.ptr(elec_forces), _lib.ptr(psi), _lib.ptr(ef), _lib.ptr(dot), _lib.ptr(vb),
               None, _lib.ctypes.byref(it), _lib.stream_ptr())
     for d in range(3):
@@ -465,7 +474,6 @@ def update_field_force_q_GPE(conv_fun, phi, types, charges, phi_q, phi_q_fourier
     for t in range(T):
         if Vbar_elec[t].data_ptr() != vb[t].data_ptr():
             Vbar_elec[t].copy_(vb[t])
-    phi_pol.copy_(phi_pol_prev)
     pm.gpe_iterations = it.value
     return Vbar_elec, phi_eps, dot
 

@@ -242,9 +242,12 @@ int hpf_bonded_hvp(float* out, const float* r, const float* lam, int64_t n, cons
  * psi = eps0^-1 (q + pol) / k^2 with q = rho~/eps, E = -grad psi,
  * V_t = q_t psi - (eps_t - eps) |E|^2 / (2 eps0^-1 sum phi~) and the forces
  * -grad(H * V_t) read out per type into elec_forces (device float[n][3]).
- * phi_eps, pol_prev and contrib (device float[M]) carry the reference's
- * persistent grids between calls (its masked divisions keep old values;
- * zero them before the first call).  Optional outputs (NULL to skip): psi,
+ * phi_eps and contrib (device float[M]) carry the reference's persistent
+ * grids between calls (its masked divisions keep old values; zero them
+ * before the first call).  pol_prev (device float[M]) is the starting
+ * polarisation and is overwritten with the converged one; the reference
+ * starts every solve from its caller's unchanged grid (field.py:1010-1024),
+ * so the drop-in passes a copy.  Optional outputs (NULL to skip): psi,
  * elec_field (float[3][M]), elec_dot (|E|^2, float[M]), vbar (float[T][M]),
  * energy (device double: dV eps0/2 sum eps |E|^2).  The convergence test
  * after each update reads 4-8 bytes back, so this call synchronises the
@@ -402,16 +405,22 @@ int hpf_respa_plan_info(const hpf_respa_plan* plan, int* n_mol_blocks, int* n_fr
 
 
 /* csvr_thermostat (hymd/thermostat.py:111-219) for up to two coupling groups.
- * state: device double[16] ([4g] alpha, [4g+1..3] COM velocity, [8+g]
- * accumulated thermostat work).  ws: workspace (HPF_OUT_DOUBLES). */
+ * The groups are visited in order, as the reference does: with COM removal
+ * (and more than one particle) a group's particles are rescaled about the
+ * group's COM velocity; otherwise K is the whole system's current kinetic
+ * energy and every particle is scaled.  state: device double[16] ([4g] A_g,
+ * [4g+1..3] B_g, the composed transform v <- A_g v + B_g of group g's
+ * particles; [8+g] accumulated thermostat work).  ws: workspace
+ * (HPF_OUT_DOUBLES). */
 int hpf_csvr(float* v, const int32_t* group, int64_t n, const float* const* kick_forces,
              int n_kick, double kick_dt, const HpfCsvrArgs* args, const double* randoms,
              int* counter, double* state, double* ws, int* d_err, void* stream);
 /* kick_forces (n_kick arrays, may be 0): the second outer half kick
  * v += 0.5 kick_dt F/mass (hymd/main.py:1143-1169) applied in the same pass,
  * before the kinetic energy is taken. */
-/* The scaling half of hpf_csvr: v = (v - com_g) alpha_g + com_g (or
- * v alpha_g without COM removal) from state (hymd/thermostat.py:210-217). */
+/* The scaling half of hpf_csvr: v = A_g v + B_g from state
+ * (hymd/thermostat.py:210-217); remove_com is carried by the transform in
+ * state and is not read. */
 int hpf_csvr_scale(float* v, const int32_t* group, int64_t n, const double* state,
                    int remove_com, void* stream);
 /* Stochastic cell rescaling (hymd/barostat_scr.py): args->mode 0 isotropic
@@ -479,7 +488,11 @@ int hpf_sum_v2(const float* v, int64_t n, double* out, void* stream);
  * HPF_ERR_SCRATCH_LIMIT.  It clears the accumulators itself on every call.
  * All calls on a device share that scratch, so calls that overlap in time (two
  * streams, two host threads) race; the first call on a device looks up the
- * array's address and should come before any stream capture.
+ * array's address and should come before any stream capture (a first call
+ * under capture returns HPF_ERR_ARG).  Each call outside a capture looks
+ * the address up again, so after cudaDeviceReset one call outside a capture
+ * makes later captured calls use the new context's array.  phi_out may
+ * start at any 4-byte boundary.
  * box: host double[3]; type_mass: host double[T]; phi_out: float[T][M];
  * d_err: device int (may be NULL).                                         */
 int hpf_paint_static(const float* pos, const int32_t* types, int64_t n, int T, int n0, int n1,

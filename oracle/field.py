@@ -305,8 +305,11 @@ def gpe_step(phi_tilde, charges, positions, types, n_types, mesh, box, sigma, ep
     phi_tilde: list of the filtered type densities (what update_field leaves
     in phi).  state: dict of the grids the reference keeps between calls --
     phi_eps, pol_prev, contrib (its masked divisions leave old values where
-    the mask is false) -- updated in place.  Returns dict(forces, psi,
-    elec_field, phi_eps, elec_dot, Vbar, energy, iterations)."""
+    the mask is false) -- phi_eps and contrib are updated in place; pol_prev
+    is the starting polarisation and is not written, because the reference
+    rebinds phi_pol_prev and phi_pol locally (field.py:1010-1024) and its
+    caller's grids never change.  Returns dict(forces, psi, elec_field,
+    phi_eps, elec_dot, Vbar, energy, iterations)."""
     n = _mesh(mesh)
     box = np.asarray(box, dtype=np.float64)
     M = n[0] * n[1] * n[2]
@@ -346,7 +349,6 @@ def gpe_step(phi_tilde, charges, positions, types, n_types, mesh, box, sigma, ep
         delta = _conv(np.abs(pol - pol_prev), conv_kind)
         pol_prev = pol.copy()
         it += 1
-    state["pol_prev"][...] = pol_prev
     eps0_inv = coulomb_constant * 4.0 * np.pi
     psik = r2c(eps0_inv * (q + pol_prev)) / knorm
     psi = c2r(psik, n)

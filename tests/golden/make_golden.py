@@ -1,8 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the HyMD reference.
 
-Run in a container that has the reference checkout (read-only is fine):
+Run in a container that has the reference checkout (read-only is fine),
+passing its root directory (or setting HYMD_REFERENCE):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path-to-HyMD-checkout>
 
 It imports the reference's own pure-Python modules by file path (bypassing
 hymd/__init__.py, which pulls in MPI/HDF5/pmesh), with these stubs:
@@ -18,8 +19,9 @@ Outputs (all small .npz files):
   bonded_kat.npz   the test_force.py expected energies/forces (1e-13 KATs)
   hamiltonian.npz  w_0 / v_ext / V_bar_0 of SquaredPhi, DefaultNoChi and
                    DefaultWithChi evaluated by the reference lambdas on seeded grids
-  misc.npz         dipole_forces_redistribution, propensity_potential_coeffs,
-                   integrator and CSVR thermostat outputs of the reference
+  misc.npz         dipole_forces_redistribution, propensity_potential_coeffs
+                   and integrator outputs of the reference (the CSVR thermostat
+                   is pinned by make_field_ref.py)
   topology_random.npz  prepare_bonds_old / prepare_bonds on seeded random
                    molecules (branches, rings, scrambled ids, duplicate and
                    reversed term types; random_molecules())
@@ -36,8 +38,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 class _Comm:
-    def allreduce(self, x, op=None):
-        return x
+    def allreduce(self, sendobj=None, op=None):
+        return sendobj
 
     def bcast(self, x, root=0):
         return x
@@ -74,6 +76,8 @@ def _install_stubs():
     pytest.fixture = lambda *a, **k: (a[0] if a and callable(a[0]) else (lambda f: f))
     if not hasattr(np, "string_"):
         np.string_ = np.bytes_
+    if not hasattr(np, "VisibleDeprecationWarning"):  # moved to np.exceptions in numpy 2
+        np.VisibleDeprecationWarning = np.exceptions.VisibleDeprecationWarning
 
 
 def _load(name, path, package=None):
@@ -363,7 +367,15 @@ def random_topology(ref):
           len(b4), "bb:", len(bbi))
 
 
+def reference_root():
+    """The HyMD checkout: first command-line argument, else $HYMD_REFERENCE."""
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HYMD_REFERENCE")
+    if not ref or not os.path.isdir(os.path.join(ref, "hymd")):
+        sys.exit("usage: make_golden.py <HyMD checkout> (or set HYMD_REFERENCE)")
+    return ref
+
+
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = reference_root()
     main(ref)
     random_topology(ref)

@@ -54,3 +54,31 @@ def test_static_paint_rejects_oversized_mesh():
     r, ty = _particles(3, 100, 2, np.array([5.0, 5.0, 5.0]))
     with pytest.raises(_lib.HPFError, match="HPF_ERR_SCRATCH_LIMIT"):
         paint_static(r, ty, [1.0, 1.0], (128, 128, 128), (5.0, 5.0, 5.0))
+
+
+def test_static_paint_into_offset_view():
+    """Destinations that start 4 bytes past a 16-byte boundary (a contiguous
+    view into a larger buffer) take the scalar store path: same grids, bit for
+    bit, from both paints."""
+    from hymd_gb300 import _lib
+    from hymd_gb300.field import ParticleMesh, paint_static
+
+    T, mesh = 2, (32, 32, 32)
+    box = np.array([6.0, 6.0, 6.0])
+    masses = [72.0, 36.0]
+    M = int(np.prod(mesh))
+    r, ty = _particles(21, 8000, T, box)
+    ref = paint_static(r, ty, masses, mesh, box)
+    buf = torch.zeros(T * M + 1, dtype=torch.float32, device="cuda")
+    view = buf[1:].view(T, *mesh)
+    assert view.data_ptr() % 16 == 4
+    paint_static(r, ty, masses, mesh, box, out=view)
+    pm = ParticleMesh(mesh, box, T)
+    buf2 = torch.zeros(T * M + 1, dtype=torch.float32, device="cuda")
+    view2 = buf2[1:].view(T, *mesh)
+    _lib.call("hpf_paint", pm._h, _lib.ptr(r), _lib.ptr(ty), r.shape[0], _lib.dvec(masses),
+              _lib.ptr(view2), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(view, ref) and torch.equal(view2, ref)
+    assert float(buf[0]) == 0.0 and float(buf2[0]) == 0.0
+    pm.check_errors()
