@@ -1,19 +1,24 @@
 """Benchmark: MD steps/s and ns/day of the hybrid particle-field rRESPA step.
 
-Workload (default): the 162k-bead lipid membrane -- 6000 twelve-bead lipids +
-90k W, box 27 nm, mesh 64^3, sigma 0.5, kappa 0.05, chi as in the membrane
-recipe, bonds + angles, time_step 0.03 ps, respa_inner 10.  One step = one
-outer rRESPA step (10 inner bonded steps + one field evaluation), run from a
-CUDA graph.  Inputs (the system state) are resident in HBM; the working set
-(~70 MB) fits in L2, so L2 is flushed between timed steps (a 256 MB write, then
-a 256 MB read so that the evicted lines are clean),
-outside the per-step CUDA-event windows.
+Workload (default): the 500k-bead charged-peptide system -- 200 chains of 50
+residues (backbone + side chain, harmonic bonds, 120-degree angles, cosine +
+combined bending-torsion dihedrals), 20% of side chains charged +-1 e with
+counter-ions, W solvent to 500 000 beads, box 40 nm, mesh 128^3, 3 types,
+PIC_Spectral electrostatics (eps_r 80), CSVR thermostat at 323 K,
+time_step 0.03 ps, respa_inner 10.  One step = one outer rRESPA step (10
+inner bonded steps + the density and charge field evaluations), run from a
+CUDA graph.  Inputs (the system state) are resident in HBM; L2 is flushed
+between timed steps (a 256 MB write, then a 256 MB read so that the evicted
+lines are clean), outside the per-step CUDA-event windows.  --workload
+melt10k / membrane162k select the other two single-system configurations.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl hpf|reference]
 
---impl reference times the CPU restatement of the same step (oracle/, the
-reference's own CPU code cannot be built here) on the host cores.
-N > 1 (torchrun): independent replicas, one per GPU; value = sum over ranks.
+--impl reference times the CPU restatement of the same step (oracle/cpu_md.py:
+FP32, the reference's order of operations, OpenMP + threaded FFTs over all
+host cores; the reference's own CPU code cannot be built here or on the GPU
+box).  N > 1 (torchrun): independent replicas, one per GPU; value = sum over
+ranks.
 """
 import argparse
 import json
@@ -30,7 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MD steps/s & ns/day per GB300 vs plain GPU form at <=1e-5 force rel-RMS vs FP64"
-WORKLOAD = "membrane162k"
+WORKLOAD = "peptide500k"
 
 # workload -> description and coupling (thermostat / barostat)
 WORKLOADS = {
@@ -143,29 +148,29 @@ def _traffic(workload):
     return json.load(open(p)).get(workload, {})
 
 
-def cpu_baseline(sys_, steps=2, workers=1):
-    """The oracle (FP64 numpy field + C bonded) on the host: a bounded sample
-    of `steps` outer steps of the same workload."""
-    from oracle import field as of
+def cpu_step(sys_, seed=0):
+    """The FP32 multi-core CPU restatement of one outer step (oracle/cpu_md.py)
+    on the workload's own system, with the same thermostat."""
+    from oracle import cpu_md
     from oracle import hamiltonian as oh
-    from oracle import md as omd
-    of.FFT_WORKERS = workers
-    cfg = sys_["config"]
-    T = cfg.n_types
-    names = cfg.unique_names
-    chi = np.zeros((T, T))
-    for c in cfg.chi:
-        i, j = names.index(c.atom_1), names.index(c.atom_2)
-        chi[i, j] = chi[j, i] = c.interaction_energy
-    fun = oh.quadratic_from_params("DefaultWithChi", T, cfg.kappa, cfg.rho0, cfg.a, chi)
-    r = sys_["positions"].copy()
-    v = sys_["velocities"].copy()
-    ff = omd.field_forces(r, sys_["types"], cfg, fun)
+    fun = oh.functional_of_config(sys_["config"])
+    return cpu_md.CpuStep(sys_, fun.Q, fun.b, workers=os.cpu_count() or 1, seed=seed)
+
+
+def cpu_baseline(sys_, steps=2, budget_s=60.0):
+    """A bounded sample of the CPU step: one untimed step, then up to `steps`
+    timed steps within `budget_s` seconds.  Returns (steps/s, seconds, done,
+    threads)."""
+    from oracle import cpu_md
+    cs = cpu_step(sys_)
+    cs.step()
     t0 = time.perf_counter()
-    for _ in range(steps):
-        r, v, ff = omd.respa_step(r, v, ff, sys_["types"], sys_["topology"], cfg, fun)
+    done = 0
+    while done < max(1, steps) and (done == 0 or time.perf_counter() - t0 < budget_s):
+        cs.step()
+        done += 1
     dt = time.perf_counter() - t0
-    return steps / dt, dt
+    return done / dt, dt, done, cpu_md.threads()
 
 
 def run_reference(args):
@@ -173,29 +178,37 @@ def run_reference(args):
     if rank != 0:
         return 0
     from hymd_gb300 import systems
-    s = systems.BUILDERS[args.workload]()
+    s = systems.BUILDERS[args.workload](seed=2)
     cfg = s["config"]
-    workers = os.cpu_count() or 1
-    cpu_baseline(s, steps=1, workers=workers)  # warm-up (one step)
-    # bounded sample: at most K steps and at most ~90 s of host work
+    from oracle import cpu_md
+    cs = cpu_step(s)
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.warmup)):
+        cs.step()
+        if time.perf_counter() - t0 > 30.0:
+            break
+    # bounded sample: K steps, at most ~90 s of host work
     t0 = time.perf_counter()
     done = 0
-    secs = 0.0
-    while done < max(1, args.steps) and time.perf_counter() - t0 < 90.0:
-        _, dt = cpu_baseline(s, steps=1, workers=workers)
-        secs += dt
+    while done < max(1, args.steps) and (done == 0 or time.perf_counter() - t0 < 90.0):
+        cs.step()
         done += 1
+    secs = time.perf_counter() - t0
     sps = done / secs
+    threads = cpu_md.threads()
     ns_day = sps * cfg.respa_inner * cfg.time_step * 86400 / 1000.0
     line = {"impl": "reference", "metric": METRIC, "value": sps, "unit": "steps/s",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": ws, "steps": done, "warmup": args.warmup,
             "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 field / f32 bonded", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "ns_per_day": ns_day,
             "config": _config_block(cfg, len(s["positions"]), args.workload),
-            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": workers, "kind": "port",
-                             "sample": f"{done} outer steps of the full workload "
-                                       f"({secs:.1f} s); FFTs threaded over {workers} cores"},
+            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{done} outer steps of the full workload ({secs:.1f} s) "
+                                       "on the FP32 restatement of the reference's step "
+                                       f"(oracle/cpu_md.py): OpenMP over {threads} threads, "
+                                       f"FFTs over {os.cpu_count()} workers; restatement, "
+                                       "not the reference"},
             "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -281,12 +294,29 @@ def step_breakdown(md, flush, torch, reps=10):
             tot[k] += x / reps
     if fused:
         del tot["kspace"], tot["c2r"]
+    for _ in range(reps):
         flush.zero_()
         a.record(st)
         g_scale.replay()
         b.record(st)
         b.synchronize()
         tot["thermostat_scale"] += a.elapsed_time(b) * 1000.0 / reps
+    if md.charges is not None:
+        # the charge path of the step (paint of the charged beads, transforms
+        # with the Poisson map, readout of q E), without the kick it carries
+        # in the step
+        g_pic = graph(lambda: _lib.call(
+            "hpf_pic_step_list", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.charges),
+            _lib.ptr(md.charged), md.charged.numel(), md.n, float(md.elec_factor),
+            _lib.ptr(md.f_elec), None, None, _lib.stream_ptr()))
+        tot["pic"] = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            a.record(st)
+            g_pic.replay()
+            b.record(st)
+            b.synchronize()
+            tot["pic"] += a.elapsed_time(b) * 1000.0 / reps
     return tot
 
 
@@ -336,6 +366,227 @@ def adjoint_cost(md, flush, torch, reps=10):
         out[name] = tot
     out["params_over_forward"] = out["dW_dparams_us"] / out["forward_force_us"]
     return out
+
+
+def accuracy(md, sys_, ham, torch):
+    """Errors of the state the timed region left, against the FP64 oracle:
+    the field and electrostatic forces, field energy, electrostatic energy
+    and pressure vector through the drop-in API (hymd_gb300.field /
+    pressure, a fresh mesh context) and the bonded forces of the fused plan
+    (hpf_respa_forces) against the real(8) C restatement of the Fortran
+    kernels, all at the positions and velocities of the last timed step."""
+    from hymd_gb300 import _lib
+    from hymd_gb300 import field as gf
+    from hymd_gb300.pressure import comp_pressure
+    from oracle import bonded as ob
+    from oracle import field as of
+    from oracle import hamiltonian as oh
+    of.FFT_WORKERS = os.cpu_count() or 1
+    cfg = sys_["config"]
+    T = cfg.n_types
+    R, V, Ty = md.r, md.v, md.types
+    pm, fl, ecl, cl = gf.initialize_pm(None, cfg)
+    phi, phi_fourier, force_on_grid, v_ext_fourier, v_ext, phi_transfer, phi_lap = fl
+    gf.update_field(phi, phi_lap, phi_transfer, None, force_on_grid, ham, pm, R, Ty, cfg, v_ext,
+                    phi_fourier, v_ext_fourier, cfg.m)
+    F = torch.zeros_like(R)
+    gf.compute_field_force(None, R, force_on_grid, F, Ty, T)
+    psi = phi_q = None
+    Fq = None
+    if md.charges is not None:
+        phi_q, phi_q_fourier, psi, elec_field = ecl
+        elec_field_fourier, psi_fourier = cl
+        Fq = torch.zeros_like(R)
+        gf.update_field_force_q(md.charges, phi_q, phi_q_fourier, psi, psi_fourier,
+                                elec_field_fourier, elec_field, Fq, None, ham, pm, R, cfg)
+    W, _, Wq = gf.compute_field_and_kinetic_energy(phi, phi_q, psi, V, ham, R, Ty, v_ext, cfg,
+                                                   None)
+    zero3 = np.zeros(3)
+    P = comp_pressure(phi, phi_q, psi, ham, V, cfg, phi_fourier, phi_lap, phi_transfer, R,
+                      zero3, zero3)
+    fb = torch.zeros_like(R)
+    if md.plan is not None:
+        _lib.call("hpf_respa_forces", md.plan, _lib.ptr(R), _lib.ptr(fb), _lib.ptr(md.box), None,
+                  _lib.ptr(md.err), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    md.check_errors()
+    pm.check_errors()
+
+    # the oracle works in the caller's bead order
+    r64 = md.in_input_order(R).cpu().numpy().astype(np.float64)
+    v32 = md.in_input_order(V).cpu().numpy()
+    types = sys_["types"]
+    fun = oh.functional_of_config(cfg)
+    ref = of.update_field(r64, types, T, cfg.mesh(), cfg.box(), cfg.m, fun, cfg.sigma)
+    Fref = of.compute_field_force(ref["force_mesh"], r64, types, T, cfg.mesh(), cfg.box())
+
+    def rel_rms(a, b):
+        return float(np.sqrt(np.mean((np.asarray(a, np.float64) - b) ** 2))
+                     / np.sqrt(np.mean(b ** 2)))
+
+    out = {"reference": "FP64 oracle (oracle/field.py, pinned to the reference's own field.py "
+                        "through tests/golden/field_ref.npz) at the last timed state",
+           "force_rel_rms": rel_rms(md.in_input_order(F).cpu().numpy(), Fref)}
+    Wref = of.field_energy(ref["phi"], fun, cfg.mesh(), cfg.box())
+    out["energy_rel_err"] = abs(W - Wref) / abs(Wref)
+    kw = {}
+    if Fq is not None:
+        q = sys_["charges"].astype(np.float64)
+        qr = of.update_field_force_q(q, r64, cfg.mesh(), cfg.box(), cfg.sigma,
+                                     cfg.dielectric_const)
+        out["elec_force_rel_rms"] = rel_rms(md.in_input_order(Fq).cpu().numpy(), qr["forces"])
+        es = float(cfg.self_energy or 0.0)
+        Wq_ref = of.field_q_energy(qr["phi_q"], qr["psi"], es, cfg.mesh(), cfg.box())
+        out["elec_energy_rel_err"] = abs(Wq - Wq_ref) / abs(Wq_ref)
+        kw = dict(phi_q=qr["phi_q"], psi=qr["psi"], self_energy=es,
+                  type_charges=list(cfg.type_charges))
+    Pref = of.comp_pressure(ref["phi"], ref["phi_fourier"], fun, v32, cfg.mass, cfg.mesh(),
+                            cfg.box(), cfg.sigma, zero3, zero3, **kw)
+    out["pressure_rel_err"] = float(np.max(np.abs(P - Pref)) / np.max(np.abs(Pref[:6])))
+    topo = sys_.get("topology")
+    if md.plan is not None and topo is not None:
+        (b2a, b2b, b2r, b2k, b3a, b3b, b3c, b3t, b3k, b4a, b4b, b4c, b4d, b4coeff, b4type,
+         b4last) = topo
+        box = cfg.box()
+        fsum = np.zeros_like(r64)
+        for fn, argv in ((ob.compute_bond_forces, (b2a, b2b, b2r, b2k)),
+                         (ob.compute_angle_forces, (b3a, b3b, b3c, b3t, b3k))):
+            if len(argv[0]):
+                f = np.zeros_like(r64)
+                fn(f, r64, box, *argv, precision="double")
+                fsum += f
+        if len(b4a):
+            f = np.zeros_like(r64)
+            nd = len(b4a)
+            ob.compute_dihedral_forces(f, r64, np.zeros((nd, 4, 3)), np.zeros((nd, 6, 3, 3)), box,
+                                       b4a, b4b, b4c, b4d, b4coeff, b4type, b4last, 0,
+                                       precision="double")
+            fsum += f
+        bonded_beads = np.zeros(len(r64), bool)
+        for idx in (b2a, b2b, b3a, b3b, b3c, b4a, b4b, b4c, b4d):
+            bonded_beads[np.asarray(idx, np.int64)] = True
+        got = md.in_input_order(fb).cpu().numpy()
+        out["bonded_force_rel_rms"] = rel_rms(got[bonded_beads], fsum[bonded_beads])
+        out["bonded_reference"] = "real(8) C restatement of cbf_d / caf_d / cdf_d"
+    return out
+
+
+def e2e_wall(md, flush, torch, steps):
+    """Steps/s of RespaMD.run_host on the host wall clock: each step copies the
+    positions and velocities in from page-locked host memory, runs the
+    captured step and copies the positions out; time.perf_counter around the
+    call and a synchronize, with the GPU idle at the start of each step (the
+    L2 flush before it has finished)."""
+    n = md.n
+    r_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    v_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    r_out = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    r_h.copy_(md.r.cpu())
+    v_h.copy_(md.v.cpu())
+    md.run_host(r_h, v_h, r_out)
+    torch.cuda.synchronize()
+    tot = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        md.run_host(r_h, v_h, r_out)
+        torch.cuda.synchronize()
+        tot += time.perf_counter() - t0
+    if not torch.equal(r_out, md.r.cpu()):
+        raise RuntimeError("end-to-end step: the positions read back differ from the device's")
+    return steps / tot, 24 * n, 12 * n
+
+
+def e2e_dropin(sys_, ham, torch, dev, steps):
+    """Steps/s of a main.py-style outer step written with the drop-in calls
+    (hymd/main.py:802-887, 975-1004, 1143-1169), numpy arrays in and out:
+    positions and velocities copied in, integrate_velocity /
+    integrate_position, compute_bond/angle/dihedral_forces for each inner
+    step, update_field + compute_field_force + update_field_force_q, the
+    second kick, positions and velocities copied out.  No thermostat (the
+    reference's thermostat is host code outside the drop-in boundary).
+    Host wall clock per step."""
+    from hymd_gb300 import field as gf
+    from hymd_gb300 import force as gfo
+    from hymd_gb300.integrator import integrate_position, integrate_velocity
+    cfg = sys_["config"]
+    T = cfg.n_types
+    n = len(sys_["positions"])
+    mass = float(cfg.mass)
+    dt, k = float(cfg.time_step), int(cfg.respa_inner)
+    box_t = torch.as_tensor(cfg.box().astype(np.float32), device=dev)
+    box = torch.as_tensor(cfg.box(), device=dev)  # device float64, as the kernels take it
+    # term arrays on the device once, in the dtypes the entry points use
+    # (int32 indices, float32 parameters), so no call converts them again
+    real = {2, 3, 7, 8, 13}
+    topo = [torch.as_tensor(np.asarray(x, np.float32 if i in real else np.int32), device=dev)
+            for i, x in enumerate(sys_["topology"])]
+    (b2a, b2b, b2r, b2k, b3a, b3b, b3c, b3t, b3k, b4a, b4b, b4c, b4d, b4coeff, b4type,
+     b4last) = topo
+    nd = b4a.numel()
+    dip = torch.zeros((nd, 4, 3), dtype=torch.float32, device=dev)
+    tr = torch.zeros((nd, 6, 3, 3), dtype=torch.float32, device=dev)
+    types = torch.as_tensor(sys_["types"], device=dev)
+    q = sys_.get("charges")
+    Q = None if q is None else torch.as_tensor(q, device=dev)
+    pm, fl, ecl, cl = gf.initialize_pm(None, cfg)
+    phi, phi_fourier, force_on_grid, v_ext_fourier, v_ext, phi_transfer, phi_lap = fl
+    z = lambda: torch.zeros((n, 3), dtype=torch.float32, device=dev)  # noqa: E731
+    fb, fa, fdh, ff, fq = z(), z(), z(), z(), z()
+
+    def bonded(r):
+        fb.zero_(), fa.zero_(), fdh.zero_()
+        gfo.compute_bond_forces(fb, r, box, b2a, b2b, b2r, b2k, sync=False)
+        gfo.compute_angle_forces(fa, r, box, b3a, b3b, b3c, b3t, b3k, sync=False)
+        if nd:
+            gfo.compute_dihedral_forces(fdh, r, dip, tr, box, b4a, b4b, b4c, b4d, b4coeff,
+                                        b4type, b4last, 0, sync=False)
+        return fb + fa + fdh
+
+    def field(r):
+        gf.update_field(phi, phi_lap, phi_transfer, None, force_on_grid, ham, pm, r, types, cfg,
+                        v_ext, phi_fourier, v_ext_fourier, cfg.m)
+        gf.compute_field_force(None, r, force_on_grid, ff, types, T)
+        if Q is not None:
+            phi_q, phi_q_fourier, psi, elec_field = ecl
+            elec_field_fourier, psi_fourier = cl
+            gf.update_field_force_q(Q, phi_q, phi_q_fourier, psi, psi_fourier,
+                                    elec_field_fourier, elec_field, fq, None, ham, pm, r, cfg)
+            return ff + fq
+        return ff.clone()
+
+    r_np = np.ascontiguousarray(sys_["positions"], np.float32).copy()
+    v_np = np.ascontiguousarray(sys_["velocities"], np.float32).copy()
+    r = torch.as_tensor(r_np, device=dev)
+    f_slow = field(r)
+    f_bond = bonded(r)
+
+    def step():
+        nonlocal f_slow, f_bond
+        r = torch.as_tensor(r_np, device=dev)
+        v = torch.as_tensor(v_np, device=dev)
+        v = integrate_velocity(v, f_slow / mass, k * dt)
+        for _ in range(k):
+            v = integrate_velocity(v, f_bond / mass, dt)
+            r = torch.remainder(integrate_position(r, v, dt), box_t)
+            f_bond = bonded(r)
+            v = integrate_velocity(v, f_bond / mass, dt)
+        f_slow = field(r)
+        v = integrate_velocity(v, f_slow / mass, k * dt)
+        r_np[...] = r.cpu().numpy()
+        v_np[...] = v.cpu().numpy()
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize()
+    sps = steps / (time.perf_counter() - t0)
+    pm.check_errors()
+    return sps, 24 * n, 24 * n
 
 
 def run_gpu(args):
@@ -405,23 +656,17 @@ def run_gpu(args):
     sps = 1000.0 / ms_step
     md.check_errors()
 
-    # ---- end to end through the public API with host buffers -------------
-    r_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
-    v_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
-    r_out = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
-    r_h.copy_(md.r.cpu())
-    v_h.copy_(md.v.cpu())
-    e2e_evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(args.steps)]
-    for a, b in e2e_evs:
-        flush.zero_()
-        a.record(st)
-        md.run_host(r_h, v_h, r_out)
-        b.record(st)
-    torch.cuda.synchronize()
-    if not torch.equal(r_out, md.r.cpu()):
-        raise RuntimeError("end-to-end step: the positions read back differ from the device's")
-    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_evs) / args.steps
+    # ---- end to end, host wall clock --------------------------------------
+    e2e_sps, e2e_h2d, e2e_d2h = e2e_wall(md, flush, torch, args.steps)
+    dropin = None
+    if not args.no_dropin:
+        d_sps, d_h2d, d_d2h = e2e_dropin(s, ham, torch, dev, max(3, min(args.steps, 20)))
+        dropin = {"value": d_sps * ws, "unit": "steps/s", "h2d_bytes_per_step": d_h2d,
+                  "d2h_bytes_per_step": d_d2h,
+                  "path": "main.py-style outer step over the drop-in calls (integrate_*, "
+                          "compute_*_forces, update_field, compute_field_force, "
+                          "update_field_force_q), numpy in / out, no thermostat, "
+                          "host wall clock"}
 
     # ---- roofline -------------------------------------------------------------
     # dominant kernel: the fused rRESPA inner loop.  Algorithmic bytes are
@@ -445,14 +690,16 @@ def run_gpu(args):
     if args.breakdown and rank == 0:
         print(json.dumps({"breakdown_us": bd}), file=sys.stderr)
     adj = adjoint_cost(md, flush, torch)
-    # paint: positions and types read; the float densities written (library
-    # path) or the int64 accumulators (fused path, no finalize pass)
-    paint_b = 16 * n + (8 if "spectral_fused" in bd else 4) * T * M
-    stage_bytes = {"paint": paint_b, "kspace": 32 * T * Mc,
-                   # fused passes: accumulators read and cleared, force mesh
-                   # written (the two intermediate spectra are extra traffic)
-                   "spectral_fused": 28 * T * M,
-                   "readout_kick": 28 * n + 12 * T * M + 36 * n}
+    # algorithmic bytes per launch as the path's contract defines them (FP32
+    # grids, cuFFT traffic excluded): paint reads r + type and writes T
+    # grids; the k-space work reads T spectra and writes 3T; the readout
+    # reads r + type and 3T grids once and writes F; the charge path of the
+    # charged beads N_q is 44 N_q + 16 M + 32 Mc
+    nq = int(md.charged.numel()) if md.charged is not None else 0
+    stage_bytes = {"paint": 16 * n + 4 * T * M, "kspace": 32 * T * Mc,
+                   "spectral_fused": 32 * T * Mc,
+                   "readout_kick": 28 * n + 12 * T * M,
+                   "pic": 44 * nq + 16 * M + 32 * Mc}
     kernels = {}
     for k, b_ in stage_bytes.items():
         if k not in bd:
@@ -465,10 +712,12 @@ def run_gpu(args):
     # CPU baseline (rank 0, N=1 only): bounded oracle sample
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        c_sps, c_secs = cpu_baseline(s, steps=2, workers=1)
-        cpu = {"value": c_sps, "unit": "steps/s", "cores": 1, "kind": "port",
-               "sample": f"2 outer steps of the full workload on the oracle "
-                         f"(FP64 numpy field + C bonded), {c_secs:.1f} s"}
+        c_sps, c_secs, c_done, c_thr = cpu_baseline(s, steps=3, budget_s=30.0)
+        cpu = {"value": c_sps, "unit": "steps/s", "cores": c_thr, "kind": "port",
+               "sample": f"{c_done} outer steps of the full workload ({c_secs:.1f} s) on the "
+                         "FP32 restatement of the reference's step (oracle/cpu_md.py), OpenMP "
+                         f"over {c_thr} threads and FFTs over {os.cpu_count()} workers"}
+    acc = accuracy(md, s, ham, torch) if rank == 0 and not args.no_accuracy else None
     if rank == 0:
         info = md.plan_info() or {}
         # one warp per molecule group up to 64 beads, one CTA per group beyond
@@ -479,16 +728,18 @@ def run_gpu(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 (f64 energies/virial)", "data": "synthetic",
                 "ns_per_day": ns_day * ws,
-                "config": _config_block(cfg, n, args.workload,
-                                        {"bead_order": "sorted by mesh cell at setup",
-                                         "respa_groups": md.plan_info(),
-                                         "respa_group_tuning_us": md.block_timings,
-                                         "kspace_tile": md.pm.spectral_tile,
-                                         "kspace_tile_tuning_us": md.spectral_tile_timings}),
-                "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "steps/s",
-                        "h2d_bytes_per_step": 2 * 12 * n, "d2h_bytes_per_step": 12 * n,
-                        "transfer": "RespaMD.run_host: DMA copies from/to page-locked host "
-                                    "memory"},
+                "config": _config_block(cfg, n, args.workload),
+                "gpu_setup": {"bead_order": "sorted by mesh cell at setup",
+                              "respa_groups": md.plan_info(),
+                              "respa_group_tuning_us": md.block_timings,
+                              "kspace_tile": md.pm.spectral_tile,
+                              "kspace_tile_tuning_us": md.spectral_tile_timings},
+                "e2e": {"value": e2e_sps * ws, "unit": "steps/s",
+                        "h2d_bytes_per_step": e2e_h2d, "d2h_bytes_per_step": e2e_d2h,
+                        "transfer": "RespaMD.run_host (r, v in; r out; page-locked host "
+                                    "memory), host wall clock around the call + synchronize"},
+                "e2e_dropin": dropin,
+                "accuracy": acc,
                 "gpu_launches": md.launches_per_step * args.steps,
                 "roofline": {"kernel": f"{respa_kernel} (fused rRESPA inner loop, "
                                        f"{cfg.respa_inner} inner steps per launch)",
@@ -745,6 +996,10 @@ def main():
     ap.add_argument("--impl", default="hpf", choices=["hpf", "reference"])
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP64-oracle accuracy check of the timed state")
+    ap.add_argument("--no-dropin", action="store_true",
+                    help="skip the drop-in-API end-to-end measurement")
     ap.add_argument("--breakdown", action="store_true",
                     help="also print per-phase step times (us) to stderr")
     ap.add_argument("--profile-stage", choices=["paint", "field", "respa", "step"],

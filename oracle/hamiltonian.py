@@ -69,3 +69,19 @@ def quadratic_from_params(kind, n_types, kappa, rho0, a=None, chi=None):
 def filter_H(k2, sigma):
     """Gaussian filter exp(-sigma^2 k^2 / 2) (hamiltonian.py:57-71)."""
     return np.exp(-0.5 * sigma * sigma * k2)
+
+
+def functional_of_config(cfg):
+    """The quadratic functional of a configuration's Hamiltonian
+    (cfg.hamiltonian, chi list, kappa; rho0 = a = N / V unless set, as
+    Hamiltonian._setup does without a barostat)."""
+    T = int(cfg.n_types)
+    names = list(cfg.unique_names)
+    chi = np.zeros((T, T))
+    for c in cfg.chi:
+        i, j = names.index(c.atom_1), names.index(c.atom_2)
+        chi[i, j] = chi[j, i] = c.interaction_energy
+    V = float(np.prod(np.asarray(cfg.box_size, dtype=np.float64)))
+    rho0 = cfg.rho0 or cfg.n_particles / V
+    a = cfg.a if cfg.a is not None else rho0
+    return quadratic_from_params(cfg.hamiltonian or "DefaultWithChi", T, cfg.kappa, rho0, a, chi)
