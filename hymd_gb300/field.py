@@ -347,12 +347,16 @@ def energy_fp64(pm, positions, types, masses, hamiltonian, charges=None, type_ch
     _lib.call("hpf_energy_fp64", pm._h, _lib.ptr(pos), _lib.ptr(typ), n,
               _lib.dvec(_masses(masses, T)), _lib.ptr(q), qt, float(elec_factor), _lib.ptr(out),
               _lib.stream_ptr())
-    o = out.cpu().numpy()
-    V = float(np.prod(pm.BoxSize))
-    means = o[16:16 + T].copy()
+    return decode_energy_sums(out.cpu().numpy(), Q, b, c, sigma, float(np.prod(pm.BoxSize)), T)
+
+
+def decode_energy_sums(o, Q, b, c, sigma, V, T):
+    """The dict of energy_fp64 from the host copy `o` of hpf_energy_fp64's
+    double[32] output, for the functional (Q, b, c, sigma) and volume V."""
+    means = np.array(o[16:16 + T], dtype=np.float64)
     W = V * (0.5 * means @ Q @ means + b @ means + c) + 0.5 * V * o[0]
-    return dict(W=W, A=o[0], B=o[1:4].copy(), Eq=o[4], C0=o[5], C=o[6:9].copy(), means=means,
-                V=V, Q=Q, b=b, sigma=sigma)
+    return dict(W=W, A=o[0], B=np.array(o[1:4]), Eq=o[4], C0=o[5], C=np.array(o[6:9]),
+                means=means, V=V, Q=Q, b=b, sigma=sigma)
 
 
 def compute_field_and_kinetic_energy(phi, phi_q, psi, velocity, hamiltonian, positions, types,

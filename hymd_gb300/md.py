@@ -36,6 +36,7 @@ class RespaMD:
         self.T = int(config.n_types)
         self.pm = ParticleMesh(config.mesh_size, config.box_size, self.T, device=self.device)
         self.pm.set_functional(hamiltonian)
+        self._hamiltonian = hamiltonian
         self.box = self.pm.box_tensor()
         self.masses = _lib.dvec(list(config.m) if config.m else [1.0] * self.T)
         self.mass = float(config.mass)
@@ -90,6 +91,12 @@ class RespaMD:
         self.state = torch.zeros(16, dtype=torch.float64, device=self.device)
         self.ws_md = _lib.new_workspace(self.device)
         self.names = None
+        # PLUMED-style bias (set_bias): a host callback every outer step
+        self.bias = None
+        self.f_bias = None
+        self.bias_indices = None
+        self.plumed_bias = 0.0
+        self.step_count = 0
         t = self.topo
         kinds = 0 if t is None else (int(t.n_bonds > 0) + int(t.n_angles > 0)
                                      + int(t.n_dihedrals > 0))
@@ -181,7 +188,8 @@ class RespaMD:
         return best[1]
 
     # per-bead arrays that sort_particles() permutes together
-    _PER_BEAD = ("r", "v", "types", "charges", "f_field", "f_elec", "f_b", "f_bond", "f_angle",
+    _PER_BEAD = ("r", "v", "types", "charges", "f_field", "f_elec", "f_bias", "f_b", "f_bond",
+                 "f_angle",
                  "f_dih", "group")
 
     def sort_particles(self):
@@ -353,7 +361,55 @@ class RespaMD:
 
     # ------------------------------------------------------------------
     def _slow_forces(self):
-        return [f for f in (self.f_field, self.f_elec) if f is not None]
+        return [f for f in (self.f_field, self.f_elec, self.f_bias) if f is not None]
+
+    # ---- PLUMED-style bias ----------------------------------------------------
+    def set_bias(self, bias, indices=None):
+        """Couple a bias with PlumedBias's prepare/calc interface
+        (hymd_gb300.plumed, hymd/plumed.py:11-235).  After every field
+        evaluation the positions and the current forces (field + bonded +
+        electrostatic, main.py:1097-1141) go to the host in the caller's bead
+        order with `indices` (global indices, default 0..N-1); the returned
+        bias force joins the slow forces of the outer half kicks
+        (main.py:808-812, 1150-1154).  The bias runs on the host between
+        kernel launches, so a run with a bias is not captured in a graph."""
+        if self.graph is not None or self.graph_inner is not None:
+            raise RuntimeError("set_bias() must come before capture()")
+        self.bias = bias
+        self.bias_indices = (np.arange(self.n, dtype=np.intc) if indices is None
+                             else np.asarray(indices, dtype=np.intc))
+        self.f_bias = torch.zeros((self.n, 3), dtype=torch.float32, device=self.device)
+
+    def potential_energy(self):
+        """Bonded energies of the last inner step plus the FP64 field (and
+        PIC electrostatic) energy of the current positions (host sync)."""
+        from .field import energy_fp64
+        cfg = self.config
+        fac = (cfg.coulomb_constant / cfg.dielectric_const) if self.charges is not None else 0.0
+        e = energy_fp64(self.pm, self.r, self.types, list(cfg.m) if cfg.m else [1.0] * self.T,
+                        self._hamiltonian, charges=self.charges, elec_factor=fac)
+        w = e["W"]
+        if self.charges is not None:
+            w += 0.5 * e["V"] * e["Eq"] - float(cfg.self_energy or 0.0)
+        return w + sum(self.energies())
+
+    def _bias_forces(self):
+        """One bias evaluation at the current positions (synchronises)."""
+        f = self.f_field + self.f_b
+        if self.f_elec is not None:
+            f = f + self.f_elec
+        forces = self.in_input_order(f).cpu().numpy()
+        pos = self.in_input_order(self.r).cpu().numpy()
+        cfg = self.config
+        cfg.box_size = self.box_now()
+        q = (self.in_input_order(self.charges).cpu().numpy() if self.charges is not None
+             else np.zeros(self.n))
+        needs = self.bias.prepare(self.step_count, forces, pos, self.bias_indices, cfg, q)
+        pot = self.potential_energy() if needs else 0.0
+        fb, e = self.bias.calc(forces, pot)
+        fb = torch.as_tensor(np.asarray(fb, np.float32), device=self.device)
+        self.f_bias.copy_(fb if self.perm is None else fb[self.perm])
+        self.plumed_bias = e
 
     def _outer_kick(self, st):
         fs = self._slow_forces()
@@ -476,6 +532,8 @@ class RespaMD:
                 self.f_b.add_(self.f_angle)
                 self.f_b.add_(self.f_dih)
         self._field(st, self.field_sums)
+        if self.bias is not None:
+            self._bias_forces()  # the bias of step 0 (main.py:691-724)
         if self.baro_args is not None:
             # the barostat reads the bonded virials of the last inner step
             for k, ws in ((0, self.ws_bond), (4, self.ws_angle)):
@@ -509,8 +567,10 @@ class RespaMD:
                   self.mass, self.dt, 1, 0, None, st)
 
     def step(self):
-        """One outer rRESPA step (launch sequence only; no host sync)."""
+        """One outer rRESPA step (launch sequence only; no host sync unless a
+        bias is set)."""
         st = _lib.stream_ptr()
+        self.step_count += 1
         if self.plan is not None:
             self._inner_fused(st)  # includes the barostat's box update
             self._outer_rest(st)
@@ -534,6 +594,18 @@ class RespaMD:
                 _lib.call("hpf_scr_scale_positions", _lib.ptr(self.r), self.n,
                           _lib.ptr(self.state), 1, st)
         thermo = self.thermo_args is not None
+        if self.bias is not None:
+            # the bias needs the new field forces before the second kick:
+            # field step without the fused kick, the bias on the host, then
+            # the kick with every slow force (and the CSVR in the same pass)
+            self._field(st, self.field_sums, pos_scale=scale)
+            self._bias_forces()
+            st = _lib.stream_ptr()
+            if thermo:
+                self._thermostat(st, kick=True)
+            else:
+                self._outer_kick(st)
+            return
         self._field(st, self.field_sums, pos_scale=scale, kick=self._kick_args(thermo))
         if thermo:
             _lib.call("hpf_csvr_scale", _lib.ptr(self.v), _lib.ptr(self.group), self.n,
@@ -546,6 +618,8 @@ class RespaMD:
         graphs replayed back to back -- `graph_inner` (the fused rRESPA kernel)
         and `graph_field` (field step, kick, thermostat) -- so that a caller
         can put timing events between them."""
+        if self.bias is not None:
+            raise RuntimeError("a bias runs on the host every step: run() steps eagerly")
         s = torch.cuda.Stream(device=self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):

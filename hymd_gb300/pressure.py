@@ -39,23 +39,32 @@ def comp_pressure(phi, phi_q, psi, hamiltonian, velocities, config, phi_fourier,
     e = energy_fp64(pm, positions, types, config.m, hamiltonian, charges=charges,
                     type_charges=qt, elec_factor=fac)
     comp_laplacian(phi_fourier, phi_transfer, phi_laplacian, hamiltonian, config)
+    vel = _lib.require_cuda(velocities, "velocities", torch.float32)
+    _lib.call("hpf_sum_v2", _lib.ptr(vel), vel.shape[0], _lib.ptr(pm.ws), _lib.stream_ptr())
+    ke = 0.5 * float(config.mass) * float(pm.ws[0])
+    self_energy = float(config.self_energy or 0.0) if charges is not None else None
+    return pressure_vector(e, ke, _host(bond_pr), _host(angle_pr), self_energy)
+
+
+def pressure_vector(e, ke, bond_pr, angle_pr, self_energy=None):
+    """The (18,) vector of hymd/pressure.py:155-176 from the FP64 sums `e`
+    (field.energy_fp64 / decode_energy_sums), the kinetic energy and the
+    bond and angle virials; self_energy (not None) adds the electrostatic
+    terms of PIC_Spectral."""
     V = e["V"]
     sigma = e["sigma"]
     means = e["means"]
     p1 = e["A"] + float((e["Q"] @ means + e["b"]) @ means)
-    p2 = -sigma ** 2 * e["B"]
+    p2 = -sigma ** 2 * np.asarray(e["B"])
     w_elec = 0.0
-    if charges is not None:
+    if self_energy is not None:
         p1 += e["C0"]
-        p2 = p2 - sigma ** 2 * e["C"]
-        w_elec = 0.5 * V * e["Eq"] - float(config.self_energy or 0.0)
-    vel = _lib.require_cuda(velocities, "velocities", torch.float32)
-    _lib.call("hpf_sum_v2", _lib.ptr(vel), vel.shape[0], _lib.ptr(pm.ws), _lib.stream_ptr())
-    ke = 0.5 * float(config.mass) * float(pm.ws[0])
+        p2 = p2 - sigma ** 2 * np.asarray(e["C"])
+        w_elec = 0.5 * V * e["Eq"] - self_energy
     p_kin = 2.0 / (3.0 * V) * ke
     p0 = -(e["W"] + w_elec) / V
-    p_bond = np.asarray(_host(bond_pr), dtype=np.float64) / V
-    p_angle = np.asarray(_host(angle_pr), dtype=np.float64) / V
+    p_bond = np.asarray(bond_pr, dtype=np.float64) / V
+    p_angle = np.asarray(angle_pr, dtype=np.float64) / V
     p_dih = np.zeros(3)
     p_tot = p_kin + p0 + p1 + p2 + p_bond + p_angle + p_dih
     return np.array([p_kin, p0, p1, *p2, *p_bond, *p_angle, *p_dih, *p_tot])

@@ -30,12 +30,18 @@ def bonded_forces(r, topo, box):
     return fb, fa
 
 
-def respa_step(r, v, f_field, types, topo, cfg, functional):
-    """One outer step; returns (r, v, f_field)."""
+def respa_step(r, v, f_field, types, topo, cfg, functional, bias=None, f_bias=None, step=1):
+    """One outer step; returns (r, v, f_field), or (r, v, f_field, f_bias)
+    with a bias: `bias(step, r, current_forces)` returns the bias force of the
+    positions after the field update (hymd/main.py:1097-1141), and f_bias
+    (that of the previous step) is kicked with the field force in both outer
+    half kicks (main.py:808-812, 1150-1154)."""
     box = cfg.box()
     dt = cfg.time_step
     mass = cfg.mass
     v = _kick(v, f_field, mass, cfg.respa_inner * dt)
+    if bias is not None:
+        v = _kick(v, f_bias, mass, cfg.respa_inner * dt)
     fb, fa = bonded_forces(r, topo, box)
     for _ in range(cfg.respa_inner):
         v = _kick(v, (fb + fa).astype(np.float32), mass, dt)
@@ -44,5 +50,10 @@ def respa_step(r, v, f_field, types, topo, cfg, functional):
         fb, fa = bonded_forces(r, topo, box)
         v = _kick(v, (fb + fa).astype(np.float32), mass, dt)
     f_field = field_forces(r, types, cfg, functional)
+    if bias is not None:
+        f_bias = np.asarray(bias(step, r, f_field + fb + fa), np.float32)
     v = _kick(v, f_field, mass, cfg.respa_inner * dt)
+    if bias is not None:
+        v = _kick(v, f_bias, mass, cfg.respa_inner * dt)
+        return r, v, f_field, f_bias
     return r, v, f_field

@@ -44,6 +44,12 @@ class _Comm:
     def bcast(self, x, root=0):
         return x
 
+    def gather(self, x, root=0):
+        return [x]
+
+    def allgather(self, x):
+        return [x]
+
     def Get_rank(self):
         return 0
 
