@@ -112,8 +112,11 @@ __global__ void k_dihedrals(float* __restrict__ force, const float* __restrict__
         }
         V3 F[4];
         float e;
+        float trig[30];
+        dih_phase_trig(coeff + 30 * i, trig);
         dihedral_term(load3(r, idx[0]), load3(r, idx[1]), load3(r, idx[2]), load3(r, idx[3]),
-                      coeff + 30 * i, dtype[i], last[i], dipole_flag, bx, F, e, dip, tmx);
+                      coeff + 30 * i, trig, dtype[i], last[i], dipole_flag, bx, F, e, dip, tmx);
+#pragma unroll
         for (int q = 0; q < 4; ++q) add3(force, idx[q], F[q]);
         acc[0] += (double)e;
     }

@@ -145,6 +145,45 @@ __global__ void k_csvr_scale(float* __restrict__ v, const int32_t* __restrict__ 
     }
 }
 
+// One coupling group (no group array): the same v <- A v + B_d as
+// k_csvr_scale over the flat array of 3n floats, four per thread as one
+// 16-byte access (v must be 16-byte aligned); the component of flat element
+// j is j mod 3.  Bit-equal to k_csvr_scale.
+__global__ void k_csvr_scale_flat(float* __restrict__ v, int64_t n3,
+                                  const double* __restrict__ state) {
+    const float al = (float)state[0];
+    const float b0 = (float)state[1], b1 = (float)state[2], b2 = (float)state[3];
+    const int64_t n4 = n3 >> 2;
+    float4* v4 = reinterpret_cast<float4*>(v);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n4; k += stride) {
+        float4 x = v4[k];
+        const int d = (int)((4 * k) % 3);  // components d, d+1, d+2, d of the four
+        const float bd = d == 0 ? b0 : (d == 1 ? b1 : b2);
+        const float be = d == 0 ? b1 : (d == 1 ? b2 : b0);
+        const float bf = d == 0 ? b2 : (d == 1 ? b0 : b1);
+        x.x = fmaf(al, x.x, bd);
+        x.y = fmaf(al, x.y, be);
+        x.z = fmaf(al, x.z, bf);
+        x.w = fmaf(al, x.w, bd);
+        v4[k] = x;
+    }
+    for (int64_t j = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n3; j += stride) {
+        const int d = (int)(j % 3);
+        v[j] = fmaf(al, v[j], d == 0 ? b0 : (d == 1 ? b1 : b2));
+    }
+}
+
+void launch_csvr_scale(float* v, const int32_t* group, int64_t n, const double* state,
+                       int remove_com, cudaStream_t st) {
+    if (!group && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
+        const int64_t n4 = (3 * n + 3) / 4;
+        k_csvr_scale_flat<<<grid_for(n4), kThreads, 0, st>>>(v, 3 * n, state);
+    } else {
+        k_csvr_scale<<<grid_for(n), kThreads, 0, st>>>(v, group, n, state, remove_com);
+    }
+}
+
 // -------------------------------------------------------------- barostat ---
 // Sum of v^2, then (last block) the isotropic SCR step: pressure from the
 // field sums of the last field evaluation, the bonded virials of the last
@@ -237,7 +276,7 @@ int hpf_csvr(float* v, const int32_t* group, int64_t n, const float* const* kick
     k_csvr_sums_alpha<<<reduce_grid_md(n), kThreads, 0, st>>>(
         v, group, n, fl, (float)(0.5 * kick_dt), ws, *args, randoms, counter, state, d_err);
     HPF_LAUNCH_CHECK();
-    k_csvr_scale<<<grid_for(n), kThreads, 0, st>>>(v, group, n, state, args->remove_com);
+    launch_csvr_scale(v, group, n, state, args->remove_com, st);
     HPF_LAUNCH_CHECK();
     return HPF_OK;
 }
@@ -246,7 +285,7 @@ int hpf_csvr_scale(float* v, const int32_t* group, int64_t n, const double* stat
                    int remove_com, void* stream) {
     if (!v || !state || n < 0) return HPF_ERR_ARG;
     if (n == 0) return HPF_OK;
-    k_csvr_scale<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(v, group, n, state, remove_com);
+    launch_csvr_scale(v, group, n, state, remove_com, as_stream(stream));
     HPF_LAUNCH_CHECK();
     return HPF_OK;
 }

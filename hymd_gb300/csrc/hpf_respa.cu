@@ -55,6 +55,7 @@ struct hpf_respa_plan {
     int* grp_dih;
     short4* dih_ijkl;
     float* dih_coeff;  // 30 per term
+    float* dih_trig;   // 30 per term: cos / sin of the phase rows (dih_phase_trig)
     int2* dih_tl;      // (type, last)
     int* dih_gid;      // global dihedral index (dipole / transfer rows)
     int* free_ids;
@@ -196,7 +197,9 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
         const int i = e / 3, d = e - 3 * i;
         const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i] + d;
         float x = forces_only ? 0.0f : v[g];
-        for (int q = 0; q < slow.n; ++q) x = x + h_out * div_m(slow.f[q][g], mass, inv_m);
+#pragma unroll
+        for (int q = 0; q < kMaxSlow; ++q)
+            if (q < slow.n) x = x + h_out * div_m(slow.f[q][g], mass, inv_m);
         reinterpret_cast<float*>(s.vs + i)[d] = x;
         reinterpret_cast<float*>(s.rs + i)[d] = r[g];
         reinterpret_cast<float*>(s.fs + i)[d] = fb[g];
@@ -255,52 +258,21 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
         }
         if (it == respa) break;
         sync();
-        for (int t = lane; t < nbd; t += width) {
-            const int ij = s.bond_ij[t];
-            const int bi = ij & 0xffff, bj = ij >> 16;
-            const float2 pr = s.bond_p[t];
-            float e;
-            V3 vir;
-            const V3 pa = get3(s.rs, bi);
-            const V3 pb = get3(s.rs, bj);
-            put3(s.slot, t, bond_term(pa, pb, pr.x, pr.y, bx, e, vir));
-            if (last_it) {
-                acc[0] += e;
-                acc[1] += vir.x;
-                acc[2] += vir.y;
-                acc[3] += vir.z;
-            }
-        }
-        for (int t = lane; t < na; t += width) {
-            const int2 q = s.ang_ijk[t];
-            const int ai = q.x & 0xffff, aj = q.x >> 16, ak = q.y;
-            const float2 pr = s.ang_p[t];
-            const V3 pa = get3(s.rs, ai);
-            const V3 pb = get3(s.rs, aj);
-            const V3 pc = get3(s.rs, ak);
-            V3 ga, gc, vir;
-            float e;
-            if (!angle_term(pa, pb, pc, pr.x, pr.y, bx, ga, gc, e, vir)) {
-                ga = gc = v3(0.f, 0.f, 0.f);
-                e = 0.0f;
-                vir = ga;
-            }
-            put3(s.slot, nbd + 2 * t, ga);
-            put3(s.slot, nbd + 2 * t + 1, gc);
-            if (last_it) {
-                acc[4] += e;
-                acc[5] += vir.x;
-                acc[6] += vir.y;
-                acc[7] += vir.z;
-            }
-        }
-        if (DIH) {
-            for (int t = lane; t < nd; t += width) {
+        // Term work in chunks of 32 terms of one kind, dealt round-robin to
+        // the group's warps with the dihedrals (the longest) first: with a
+        // whole CTA on a chain no lane computes a dihedral, an angle and a
+        // bond one after the other.  A warp takes its chunks in order; each
+        // term still writes only its own slots.
+        const int wid = lane >> 5, nw = width >> 5, l32 = lane & 31;
+        const int cd = DIH ? (nd + 31) >> 5 : 0, ca = (na + 31) >> 5, cb = (nbd + 31) >> 5;
+        for (int task = wid; task < cd + ca + cb; task += nw) {
+            if (DIH && task < cd) {
+                const int t = (task << 5) + l32;
+                if (t >= nd) continue;
                 const short4 q = p.dih_ijkl[d0 + t];
                 const int2 tl = p.dih_tl[d0 + t];
-                const int li[4] = {q.x, q.y, q.z, q.w};
-                V3 pos[4];
-                for (int j = 0; j < 4; ++j) pos[j] = get3(s.rs, li[j]);
+                const V3 p0 = get3(s.rs, q.x), p1 = get3(s.rs, q.y);
+                const V3 p2 = get3(s.rs, q.z), p3 = get3(s.rs, q.w);
                 float* dip = nullptr;
                 float* tmx = nullptr;
                 if (last_it && dipoles) {
@@ -312,11 +284,54 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                 }
                 V3 F[4];
                 float e;
-                dihedral_term(pos[0], pos[1], pos[2], pos[3],
-                              p.dih_coeff + 30 * (int64_t)(d0 + t), tl.x, tl.y,
+                const int64_t c30 = 30 * (int64_t)(d0 + t);
+                dihedral_term(p0, p1, p2, p3, p.dih_coeff + c30, p.dih_trig + c30, tl.x, tl.y,
                               (last_it && dipoles) ? 1 : 0, bx, F, e, dip, tmx);
-                for (int j = 0; j < 4; ++j) put3(s.slot, nbd + 2 * na + 4 * t + j, F[j]);
+                const int sl = nbd + 2 * na + 4 * t;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) put3(s.slot, sl + j, F[j]);
                 if (last_it) acc[8] += e;
+            } else if (task < cd + ca) {
+                const int t = ((task - cd) << 5) + l32;
+                if (t >= na) continue;
+                const int2 q = s.ang_ijk[t];
+                const int ai = q.x & 0xffff, aj = q.x >> 16, ak = q.y;
+                const float2 pr = s.ang_p[t];
+                const V3 pa = get3(s.rs, ai);
+                const V3 pb = get3(s.rs, aj);
+                const V3 pc = get3(s.rs, ak);
+                V3 ga, gc, vir;
+                float e;
+                if (!angle_term(pa, pb, pc, pr.x, pr.y, bx, ga, gc, e, vir)) {
+                    ga = gc = v3(0.f, 0.f, 0.f);
+                    e = 0.0f;
+                    vir = ga;
+                }
+                put3(s.slot, nbd + 2 * t, ga);
+                put3(s.slot, nbd + 2 * t + 1, gc);
+                if (last_it) {
+                    acc[4] += e;
+                    acc[5] += vir.x;
+                    acc[6] += vir.y;
+                    acc[7] += vir.z;
+                }
+            } else {
+                const int t = ((task - cd - ca) << 5) + l32;
+                if (t >= nbd) continue;
+                const int ij = s.bond_ij[t];
+                const int bi = ij & 0xffff, bj = ij >> 16;
+                const float2 pr = s.bond_p[t];
+                float e;
+                V3 vir;
+                const V3 pa = get3(s.rs, bi);
+                const V3 pb = get3(s.rs, bj);
+                put3(s.slot, t, bond_term(pa, pb, pr.x, pr.y, bx, e, vir));
+                if (last_it) {
+                    acc[0] += e;
+                    acc[1] += vir.x;
+                    acc[2] += vir.y;
+                    acc[3] += vir.z;
+                }
             }
         }
         sync();
@@ -350,7 +365,9 @@ __device__ __forceinline__ void free_beads(const hpf_respa_plan& p, int fblock, 
         const int64_t g = 3 * (int64_t)p.free_ids[j];
         for (int d = 0; d < 3; ++d) {
             float x = v[g + d];
-            for (int q = 0; q < slow.n; ++q) x = x + h_out * div_m(slow.f[q][g + d], mass, inv_m);
+#pragma unroll
+            for (int q = 0; q < kMaxSlow; ++q)
+                if (q < slow.n) x = x + h_out * div_m(slow.f[q][g + d], mass, inv_m);
             float y = r[g + d];
             for (int it = 0; it < respa; ++it) y = wrapf(y + dt * x, bx.L[d]);
             v[g + d] = x;
@@ -385,8 +402,10 @@ k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     if (out) block_partials_f<kOut, kThreads>(acc, p.partials, gridDim.x);
 }
 
+// Four blocks per SM: the chain CTAs share the SMs with the free-bead
+// blocks, which need the occupancy to hide their global loads.
 template <bool DIH>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
 k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
             float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
             int respa, const double* __restrict__ box, float* __restrict__ dipoles,
@@ -403,6 +422,13 @@ k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
         free_beads(p, blockIdx.x - p.n_groups, r, v, slow, mass, h_out, dt, respa, bx, acc);
     }
     if (out) block_partials_f<kOut, kThreads>(acc, p.partials, gridDim.x);
+}
+
+// cos / sin of every dihedral's phase rows, once per plan (dih_phase_trig:
+// the values the per-term kernel computes for itself).
+__global__ void k_dih_trig(const float* __restrict__ coeff, float* __restrict__ trig, int64_t nd) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < nd) dih_phase_trig(coeff + 30 * i, trig + 30 * i);
 }
 
 // Sum of the block partials (fixed order) into out[0..kOut), then the
@@ -520,7 +546,8 @@ int hpf_respa_plan_destroy(hpf_respa_plan* p) {
     if (!p) return HPF_OK;
     void* ptrs[] = {p->grp_bead, p->bead_ids, p->bead_inc, p->inc_list, p->grp_bond,
                     p->bond_ij,  p->bond_p,   p->grp_ang,  p->ang_ijk,  p->ang_p,
-                    p->grp_dih,  p->dih_ijkl, p->dih_coeff, p->dih_tl,  p->dih_gid,
+                    p->grp_dih,  p->dih_ijkl, p->dih_coeff, p->dih_trig, p->dih_tl,
+                    p->dih_gid,
                     p->free_ids, p->partials};
     for (void* q : ptrs) cudaFree(q);
     delete p;
@@ -715,6 +742,18 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
         (st = upload(&p->dih_gid, dih_gid)) || (st = upload(&p->free_ids, free_ids))) {
         hpf_respa_plan_destroy(p);
         return st;
+    }
+    if (cudaMalloc(&p->dih_trig, sizeof(float) * 30 * (size_t)std::max<int64_t>(nd, 1)) !=
+        cudaSuccess) {
+        hpf_respa_plan_destroy(p);
+        return HPF_ERR_CUDA;
+    }
+    if (nd > 0) {
+        k_dih_trig<<<(int)((nd + 127) / 128), 128>>>(p->dih_coeff, p->dih_trig, nd);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+            hpf_respa_plan_destroy(p);
+            return HPF_ERR_CUDA;
+        }
     }
     const int grid = grid_size(p);
     if (cudaMalloc(&p->partials, sizeof(double) * kOut * (size_t)std::max(grid, 1)) != cudaSuccess) {

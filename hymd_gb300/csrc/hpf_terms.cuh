@@ -104,14 +104,118 @@ __device__ __forceinline__ float div_m(float f, float m, float inv_m) {
     return fmaf(r, inv_m, q);
 }
 
-__device__ __forceinline__ void cosine_series(const float* cn, const float* dn, float phi,
+// cos and sin of the phase angles of a four-body term's coefficient rows 1,
+// 3 and 5 (the d_n of the cosine series): trig[5r + q] = cos(row[2r+1][q]),
+// trig[15 + 5r + q] = sin(row[2r+1][q]), r = 0, 1, 2.  They depend on the
+// coefficients only, so the fused kernel's plan holds them once.
+__device__ __forceinline__ void dih_phase_trig(const float* cf, float* trig) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            float sn, cs;
+            sincosf(cf[5 * (2 * r + 1) + q], &sn, &cs);
+            trig[5 * r + q] = cs;
+            trig[15 + 5 * r + q] = sn;
+        }
+    }
+}
+
+// cos(n phi), sin(n phi) for n = 0..4 from cos phi and sin phi by the
+// rotation recurrence (no trigonometric calls).
+__device__ __forceinline__ void multiples(float cphi, float sphi, float (&C)[5], float (&S)[5]) {
+    C[0] = 1.0f;
+    S[0] = 0.0f;
+#pragma unroll
+    for (int n = 1; n < 5; ++n) {
+        C[n] = fmaf(C[n - 1], cphi, -S[n - 1] * sphi);
+        S[n] = fmaf(S[n - 1], cphi, C[n - 1] * sphi);
+    }
+}
+
+// sum_n c_n (1 + cos(n phi - d_n)) into e and its phi-derivative
+// sum_n -n c_n sin(n phi - d_n) into de, with cos(n phi - d) = C cos d +
+// S sin d and sin(n phi - d) = S cos d - C sin d (cd, sd: the phases' cos,
+// sin).
+__device__ __forceinline__ void cosine_series(const float* cn, const float* cd, const float* sd,
+                                              const float (&C)[5], const float (&S)[5],
                                               float& e, float& de) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-        float s, c;
-        sincosf(i * phi - dn[i], &s, &c);
+        const float c = fmaf(C[i], cd[i], S[i] * sd[i]);
+        const float sn = fmaf(S[i], cd[i], -C[i] * sd[i]);
         e = fmaf(cn[i], 1.0f + c, e);
-        de = fmaf(-(float)i * cn[i], s, de);
+        de = fmaf(-(float)i * cn[i], sn, de);
+    }
+}
+
+// The dipole pseudo-charge positions (dipole[0..5]) and the three 3x3
+// transfer matrices (tm[0..26]) of reconstruct (dipole_reconstruction.f90:
+// 107-220), from the unit bond vectors w, v, the angle gamma and the
+// (not yet stiffness-scaled) angle gradients fa, fb, fc.  Only the last
+// inner step asks for them, so this stays out of line.
+static __device__ __noinline__ void dipole_transfer(V3 w, V3 v, V3 rb, V3 rcb, float norm_a,
+                                                    float norm_c, float cos_gamma,
+                                                    float sin_gamma, float gamm, V3 fa, V3 fb,
+                                                    V3 fc, const Box& bx, float* dipole,
+                                                    float* tm) {
+    const float delta = 0.3f;
+    // cos(1.392947) / sin(1.392947): single-precision literals in the Fortran
+    const float cos_psi = cosf(1.392947f), sin_psi = sinf(1.392947f);
+    const float fac = expf((gamm - 1.73f) / 0.025f);
+    const float theta = -1.607f * gamm + 0.094f + 1.883f / (1.0f + fac);
+    const float d_theta = -1.607f - 1.883f / 0.025f * fac / ((1.0f + fac) * (1.0f + fac));
+    float sin_theta, cos_theta;
+    sincosf(theta, &sin_theta, &cos_theta);
+    const V3 nn = (1.0f / sin_gamma) * cross(w, v);
+    const V3 m = cross(nn, v);
+    const V3 r0 = rb + 0.5f * rcb;
+    const V3 d = (0.5f * delta) * (cos_psi * v + sin_psi * (cos_theta * nn + sin_theta * m));
+    const V3 p[2] = {r0 + d, r0 - d};
+    for (int q = 0; q < 2; ++q) {
+        const V3 pw = min_image(p[q], bx);
+        dipole[3 * q] = pw.x;
+        dipole[3 * q + 1] = pw.y;
+        dipole[3 * q + 2] = pw.z;
+    }
+    const float wv[3] = {w.x, w.y, w.z}, vv[3] = {v.x, v.y, v.z};
+    const float nv[3] = {nn.x, nn.y, nn.z}, mv[3] = {m.x, m.y, m.z};
+    const float fav[3] = {fa.x, fa.y, fa.z}, fbv[3] = {fb.x, fb.y, fb.z},
+                fcv[3] = {fc.x, fc.y, fc.z};
+    for (int i = 0; i < 3; ++i) {
+        float Vb[3], Wb[3];
+        for (int j = 0; j < 3; ++j) {
+            Vb[j] = (vv[i] * vv[j] - (i == j ? 1.0f : 0.0f)) / norm_c;
+            Wb[j] = (wv[i] * wv[j] - (i == j ? 1.0f : 0.0f)) / norm_a;
+        }
+        // cross_matrix(Mx, x): row i = cross(Mx(i,:), x); with Vc = -Vb, Wa = -Wb
+        const V3 Wbi = v3(Wb[0], Wb[1], Wb[2]);
+        const V3 Vbi = v3(Vb[0], Vb[1], Vb[2]);
+        const V3 cWb_v = cross(Wbi, v), cVb_w = cross(Vbi, w), cVb_n = cross(Vbi, nn);
+        const V3 Na = (1.0f / sin_gamma) * (cos_gamma * fav[i] * nn - cWb_v);
+        const V3 Nb = (1.0f / sin_gamma) * (cos_gamma * fbv[i] * nn + cWb_v - cVb_w);
+        const V3 Nc = (1.0f / sin_gamma) * (cos_gamma * fcv[i] * nn + cVb_w);
+        const V3 Ma = cross(Na, v);
+        const V3 Mb = cross(Nb, v) - cVb_n;
+        const V3 Mc = cross(Nc, v) + cVb_n;
+        const float Ma_[3] = {Ma.x, Ma.y, Ma.z}, Mb_[3] = {Mb.x, Mb.y, Mb.z},
+                    Mc_[3] = {Mc.x, Mc.y, Mc.z};
+        const float Na_[3] = {Na.x, Na.y, Na.z}, Nb_[3] = {Nb.x, Nb.y, Nb.z},
+                    Nc_[3] = {Nc.x, Nc.y, Nc.z};
+        const float st_dt = sin_theta * d_theta, ct_dt = cos_theta * d_theta;
+        for (int j = 0; j < 3; ++j) {
+            const float FNa = st_dt * fav[i] * nv[j], FMa = ct_dt * fav[i] * mv[j];
+            const float FNb = st_dt * fbv[i] * nv[j], FMb = ct_dt * fbv[i] * mv[j];
+            const float FNc = st_dt * fcv[i] * nv[j], FMc = ct_dt * fcv[i] * mv[j];
+            tm[0 * 9 + i * 3 + j] =
+                0.5f * delta * (sin_psi * (cos_theta * Na_[j] + sin_theta * Ma_[j] + FNa - FMa));
+            tm[1 * 9 + i * 3 + j] =
+                0.5f * delta * (cos_psi * Vb[j] +
+                                sin_psi * (cos_theta * Nb_[j] + sin_theta * Mb_[j] + FNb - FMb));
+            tm[2 * 9 + i * 3 + j] =
+                0.5f * delta * (-cos_psi * Vb[j] +
+                                sin_psi * (cos_theta * Nc_[j] + sin_theta * Mc_[j] + FNc - FMc));
+        }
     }
 }
 
@@ -121,16 +225,20 @@ __device__ __forceinline__ void cosine_series(const float* cn, const float* dn, 
 // (tm[0..26]).  Outputs the positive gradients fa, fb, fc.  Where
 // cos^2(gamma) >= 1 the Fortran leaves its outputs unassigned; here they are
 // zero.
+// The bending stiffness K(phi) is the cosine series of rows 4 (c_k) and 5
+// (phases, as cos cd_k / sin sd_k); gamma_0(phi) = 1.85 - 0.227 cos(phi -
+// 0.785) and its derivative come from cos phi, sin phi and the constants
+// cos(0.785f), sin(0.785f).
 static __device__ void reconstruct(V3 rab, V3 rb, V3 rcb, const Box& bx, const float* c_k,
-                            const float* d_k, float phi, int dipole_flag, float& e_cbt,
-                            float& df_cbt, V3& fa, V3& fb, V3& fc, float* dipole, float* tm) {
-    // cos(1.392947) / sin(1.392947): single-precision literals in the Fortran
-    const float cos_psi = cosf(1.392947f), sin_psi = sinf(1.392947f);
-    const float delta = 0.3f;
+                                   const float* cd_k, const float* sd_k, float cphi, float sphi,
+                                   const float (&C)[5], const float (&S)[5], int dipole_flag,
+                                   float& e_cbt, float& df_cbt, V3& fa, V3& fb, V3& fc,
+                                   float* dipole, float* tm) {
+    constexpr float c785 = 7.073882506e-01f, s785 = 7.068251997e-01f;  // cos, sin of 0.785f
     float k = 0.0f, dk = 0.0f;
-    const float gamma_0 = 1.85f - 0.227f * cosf(phi - 0.785f);
-    const float dg = 0.227f * sinf(phi - 0.785f);
-    cosine_series(c_k, d_k, phi, k, dk);
+    const float gamma_0 = 1.85f - 0.227f * fmaf(cphi, c785, sphi * s785);
+    const float dg = 0.227f * fmaf(sphi, c785, -cphi * s785);
+    cosine_series(c_k, cd_k, sd_k, C, S, k, dk);
     const float norm_a = norm(rab), norm_c = norm(rcb);
     const V3 w = (1.0f / norm_a) * rab, v = (1.0f / norm_c) * rcb;
     const float cos_gamma = dot(w, v);
@@ -148,74 +256,25 @@ static __device__ void reconstruct(V3 rab, V3 rb, V3 rcb, const Box& bx, const f
     const float var_sq = (gamm - gamma_0) * (gamm - gamma_0);
     e_cbt = 0.5f * k * var_sq;
     df_cbt = 0.5f * dk * var_sq - df_ang * dg;
-    if (dipole_flag && dipole) {
-        const float fac = expf((gamm - 1.73f) / 0.025f);
-        const float theta = -1.607f * gamm + 0.094f + 1.883f / (1.0f + fac);
-        const float d_theta = -1.607f - 1.883f / 0.025f * fac / ((1.0f + fac) * (1.0f + fac));
-        float sin_theta, cos_theta;
-        sincosf(theta, &sin_theta, &cos_theta);
-        const V3 nn = (1.0f / sin_gamma) * cross(w, v);
-        const V3 m = cross(nn, v);
-        const V3 r0 = rb + 0.5f * rcb;
-        const V3 d = (0.5f * delta) * (cos_psi * v + sin_psi * (cos_theta * nn + sin_theta * m));
-        const V3 p[2] = {r0 + d, r0 - d};
-        for (int q = 0; q < 2; ++q) {
-            const V3 pw = min_image(p[q], bx);
-            dipole[3 * q] = pw.x;
-            dipole[3 * q + 1] = pw.y;
-            dipole[3 * q + 2] = pw.z;
-        }
-        const float wv[3] = {w.x, w.y, w.z}, vv[3] = {v.x, v.y, v.z};
-        const float nv[3] = {nn.x, nn.y, nn.z}, mv[3] = {m.x, m.y, m.z};
-        const float fav[3] = {fa.x, fa.y, fa.z}, fbv[3] = {fb.x, fb.y, fb.z},
-                    fcv[3] = {fc.x, fc.y, fc.z};
-        for (int i = 0; i < 3; ++i) {
-            float Vb[3], Wb[3];
-            for (int j = 0; j < 3; ++j) {
-                Vb[j] = (vv[i] * vv[j] - (i == j ? 1.0f : 0.0f)) / norm_c;
-                Wb[j] = (wv[i] * wv[j] - (i == j ? 1.0f : 0.0f)) / norm_a;
-            }
-            // cross_matrix(Mx, x): row i = cross(Mx(i,:), x); with Vc = -Vb, Wa = -Wb
-            const V3 Wbi = v3(Wb[0], Wb[1], Wb[2]);
-            const V3 Vbi = v3(Vb[0], Vb[1], Vb[2]);
-            const V3 cWb_v = cross(Wbi, v), cVb_w = cross(Vbi, w), cVb_n = cross(Vbi, nn);
-            const V3 Na = (1.0f / sin_gamma) * (cos_gamma * fav[i] * nn - cWb_v);
-            const V3 Nb = (1.0f / sin_gamma) * (cos_gamma * fbv[i] * nn + cWb_v - cVb_w);
-            const V3 Nc = (1.0f / sin_gamma) * (cos_gamma * fcv[i] * nn + cVb_w);
-            const V3 Ma = cross(Na, v);
-            const V3 Mb = cross(Nb, v) - cVb_n;
-            const V3 Mc = cross(Nc, v) + cVb_n;
-            const float Ma_[3] = {Ma.x, Ma.y, Ma.z}, Mb_[3] = {Mb.x, Mb.y, Mb.z},
-                        Mc_[3] = {Mc.x, Mc.y, Mc.z};
-            const float Na_[3] = {Na.x, Na.y, Na.z}, Nb_[3] = {Nb.x, Nb.y, Nb.z},
-                        Nc_[3] = {Nc.x, Nc.y, Nc.z};
-            const float st_dt = sin_theta * d_theta, ct_dt = cos_theta * d_theta;
-            for (int j = 0; j < 3; ++j) {
-                const float FNa = st_dt * fav[i] * nv[j], FMa = ct_dt * fav[i] * mv[j];
-                const float FNb = st_dt * fbv[i] * nv[j], FMb = ct_dt * fbv[i] * mv[j];
-                const float FNc = st_dt * fcv[i] * nv[j], FMc = ct_dt * fcv[i] * mv[j];
-                tm[0 * 9 + i * 3 + j] =
-                    0.5f * delta * (sin_psi * (cos_theta * Na_[j] + sin_theta * Ma_[j] + FNa - FMa));
-                tm[1 * 9 + i * 3 + j] =
-                    0.5f * delta * (cos_psi * Vb[j] +
-                                    sin_psi * (cos_theta * Nb_[j] + sin_theta * Mb_[j] + FNb - FMb));
-                tm[2 * 9 + i * 3 + j] =
-                    0.5f * delta * (-cos_psi * Vb[j] +
-                                    sin_psi * (cos_theta * Nc_[j] + sin_theta * Mc_[j] + FNc - FMc));
-            }
-        }
-    }
+    if (dipole_flag && dipole)
+        dipole_transfer(w, v, rb, rcb, norm_a, norm_c, cos_gamma, sin_gamma, gamm, fa, fb, fc, bx,
+                        dipole, tm);
     fa = df_ang * fa;
     fb = df_ang * fb;
     fc = df_ang * fc;
 }
 
 // Four-body term a-b-c-d of type ty (0 cosine series, 1 + CBT, 2 improper).
-// coeff: 30 floats (6 rows x 5).  Writes the forces on the four beads
-// (F[0..3]) and the energy; with dipole_flag writes dipole[0..11] and
-// tm[0..53] for type 1 (the caller zeroes them first).
-__device__ __forceinline__ void dihedral_term(V3 pa, V3 pb, V3 pc, V3 pd, const float* cf, int ty,
-                                              int last, int dipole_flag, const Box& bx, V3 F[4],
+// coeff: 30 floats (6 rows x 5); trig: the 30 cos / sin of its phase rows
+// (dih_phase_trig).  Writes the forces on the four beads (F[0..3]) and the
+// energy; with dipole_flag writes dipole[0..11] and tm[0..53] for type 1
+// (the caller zeroes them first).  phi = atan2(sin_phi, cos_phi) of the
+// reference; the cosine series need only cos phi and sin phi, so types 0
+// and 1 take them from the same two dot products without a trigonometric
+// call (the improper, type 2, uses phi itself).
+__device__ __forceinline__ void dihedral_term(V3 pa, V3 pb, V3 pc, V3 pd, const float* cf,
+                                              const float* trig, int ty, int last,
+                                              int dipole_flag, const Box& bx, V3 (&F)[4],
                                               float& e_out, float* dip, float* tmx) {
     const V3 fv = min_image(pa - pb, bx);
     const V3 g = min_image(pb - pc, bx);
@@ -225,44 +284,52 @@ __device__ __forceinline__ void dihedral_term(V3 pa, V3 pb, V3 pc, V3 pd, const 
     const float g_norm = norm(g);
     const float cos_phi = dot(v, w);
     const float sin_phi = dot(w, fv) * g_norm;
-    const float phi = atan2f(sin_phi, cos_phi);
     const float f_dot_g = dot(fv, g), h_dot_g = dot(h, g);
-    float row[6][5];
-    for (int p = 0; p < 6; ++p)
-        for (int q = 0; q < 5; ++q) row[p][q] = cf[5 * p + q];
     float e = 0.0f, df_dih = 0.0f;
     F[0] = F[1] = F[2] = F[3] = v3(0.f, 0.f, 0.f);
     if (ty == 0 || ty == 1) {
-        cosine_series(row[0], row[1], phi, e, df_dih);
-        bool nz_c = false, nz_d = false;
-        for (int q = 0; q < 5; ++q) {
-            nz_c |= row[2][q] != 0.0f;
-            nz_d |= row[3][q] != 0.0f;
+        const float rho2 = fmaf(cos_phi, cos_phi, sin_phi * sin_phi);
+        float cphi = 1.0f, sphi = 0.0f;  // atan2(0, 0) = 0
+        if (rho2 > 0.0f) {
+            const float inv = 1.0f / sqrtf(rho2);
+            cphi = cos_phi * inv;
+            sphi = sin_phi * inv;
         }
-        if (nz_c && nz_d) cosine_series(row[2], row[3], phi, e, df_dih);
-    }
-    if (ty == 1) {
-        float e_cbt, df_cbt;
-        V3 fa, fb, fc, fd;
-        reconstruct(fv, pb, -g, bx, row[4], row[5], phi, dipole_flag, e_cbt, df_cbt, fa, fb, fc,
-                    dip, tmx);
-        e += e_cbt;
-        df_dih += df_cbt;
-        F[0] = F[0] - fa;
-        F[1] = F[1] - fb;
-        F[2] = F[2] - fc;
-        if (last == 1) {
-            reconstruct(g, pc, h, bx, row[4], row[5], phi, dipole_flag, e_cbt, df_cbt, fb, fc, fd,
-                        dip ? dip + 6 : nullptr, tmx ? tmx + 27 : nullptr);
+        float C[5], S[5];
+        multiples(cphi, sphi, C, S);
+        cosine_series(cf, trig, trig + 15, C, S, e, df_dih);
+        bool nz_c = false, nz_d = false;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            nz_c |= cf[10 + q] != 0.0f;
+            nz_d |= cf[15 + q] != 0.0f;
+        }
+        if (nz_c && nz_d) cosine_series(cf + 10, trig + 5, trig + 20, C, S, e, df_dih);
+        if (ty == 1) {
+            float e_cbt, df_cbt;
+            V3 fa, fb, fc, fd;
+            reconstruct(fv, pb, -g, bx, cf + 20, trig + 10, trig + 25, cphi, sphi, C, S,
+                        dipole_flag, e_cbt, df_cbt, fa, fb, fc, dip, tmx);
             e += e_cbt;
             df_dih += df_cbt;
+            F[0] = F[0] - fa;
             F[1] = F[1] - fb;
             F[2] = F[2] - fc;
-            F[3] = F[3] - fd;
+            if (last == 1) {
+                reconstruct(g, pc, h, bx, cf + 20, trig + 10, trig + 25, cphi, sphi, C, S,
+                            dipole_flag, e_cbt, df_cbt, fb, fc, fd, dip ? dip + 6 : nullptr,
+                            tmx ? tmx + 27 : nullptr);
+                e += e_cbt;
+                df_dih += df_cbt;
+                F[1] = F[1] - fb;
+                F[2] = F[2] - fc;
+                F[3] = F[3] - fd;
+            }
         }
     }
     if (ty == 2) {
-        const float eq = row[0][0], kc = row[0][1];
+        const float phi = atan2f(sin_phi, cos_phi);
+        const float eq = cf[0], kc = cf[1];
         df_dih = kc * (phi - eq);
         e += 0.5f * kc * (phi - eq) * (phi - eq);
     }
