@@ -951,6 +951,69 @@ def run_reverse(args):
     return 0
 
 
+def run_locality(args):
+    """Step time (graph replays, CUDA events, L2 flushed before each) against
+    the age of the bead order, for both mesh-cell sort orders: right after
+    the sort, then after more and more unsorted steps; then the device time
+    of resort() (the first one records its graph) and the step time right
+    after the re-sorts.  Diagnostic; prints one JSON object per order."""
+    import torch
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    s = systems.BUILDERS[args.workload](seed=2)
+    cfg = s["config"]
+    flush = L2Flush(torch, dev)
+    st = torch.cuda.current_stream()
+    for order in ("molecule", "bead"):
+        md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, get_hamiltonian(cfg),
+                     topology=s["topology"], charges=s.get("charges"), device=dev)
+        md.sort_particles(order=order)
+        md.couple(seed=100, n_steps=20000, **WORKLOADS[args.workload][1])
+        md.prime()
+        md.capture()
+
+        def timed(k=20):
+            tot = 0.0
+            for _ in range(k):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(st)
+                md.replay()
+                b.record(st)
+                b.synchronize()
+                tot += a.elapsed_time(b)
+            return round(1000.0 * tot / k, 1)
+
+        ages = {}
+        md.run(3)
+        age = 3
+        for target in (3, 50, 200, 1000, 3000):
+            md.run(target - age)
+            age = target
+            ages[str(age)] = timed()
+            age += 20
+        resort = []
+        for _ in range(5):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            md.resort()
+            b.record(st)
+            b.synchronize()
+            resort.append(round(1000.0 * a.elapsed_time(b), 1))
+        after = timed()
+        md.check_errors()
+        print(json.dumps({"workload": args.workload, "order": order, "step_us_by_age": ages,
+                          "step_us_after_resort": after, "resort_us": resort}))
+        del md
+        torch.cuda.empty_cache()
+    return 0
+
+
 def profile_stage(args):
     """Run one stage of the step eagerly (no graph, no timing) `--reps` times
     on the workload and exit: a small program for kernel profilers.
@@ -1010,6 +1073,8 @@ def main():
     ap.add_argument("--reverse", action="store_true",
                     help="reverse-mode chi gradient on the 1.3M-bead membrane")
     ap.add_argument("--reverse-steps", type=int, default=200)
+    ap.add_argument("--locality", action="store_true",
+                    help="diagnostic: step time against the age of the bead order")
     ap.add_argument("--topology", action="store_true",
                     help="bonded-term discovery (prepare_bonds) on the device, 1.3M-bead membrane")
     args = ap.parse_args()
@@ -1021,6 +1086,8 @@ def main():
         return run_reverse(args)
     if args.topology:
         return run_topology(args)
+    if args.locality:
+        return run_locality(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -68,6 +68,8 @@ _SIGNATURES = {
     "hpf_respa_plan_create": [ctypes.POINTER(P), I64, I64, P, P, P, P, I64, P, P, P, P, P, I64,
                               P, P, P, P, P, P, P, I],
     "hpf_respa_plan_destroy": [P],
+    "hpf_respa_plan_permute": [P, P, I64, P, I64, P, P],
+    "hpf_respa_plan_counts": [P, ctypes.POINTER(I64), ctypes.POINTER(I64)],
     "hpf_respa_plan_info": [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
     "hpf_respa_step": [P, P, P, P, ctypes.POINTER(P), I, D, D, I, P, P, P, P, P, P, P, P, P,
                        P, P, P],

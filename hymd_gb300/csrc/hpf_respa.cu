@@ -33,6 +33,7 @@
 struct hpf_respa_plan {
     int64_t n_beads;
     int n_groups;        // molecule groups
+    int n_bonded;        // beads in groups (entries of bead_ids)
     int n_free;
     int n_free_blocks;
     int warp_mode;       // 1: one warp per group, 0: one CTA per group
@@ -424,6 +425,22 @@ k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
     if (out) block_partials_f<kOut, kThreads>(acc, p.partials, gridDim.x);
 }
 
+// ids[k] = inv[ids[k]]: the plan's bead lists follow a permutation of the
+// bead arrays (inv[old index] = new index); an index outside [0, n) is
+// flagged and left as it was.
+__global__ void k_remap_ids(int* __restrict__ ids, int64_t count, const int32_t* __restrict__ inv,
+                            int64_t n, int* err) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = ids[k];
+        if (i < 0 || i >= n) {
+            if (err) atomicCAS(err, 0, HPF_ERR_INDEX);
+            continue;
+        }
+        ids[k] = inv[i];
+    }
+}
+
 // cos / sin of every dihedral's phase rows, once per plan (dih_phase_trig:
 // the values the per-term kernel computes for itself).
 __global__ void k_dih_trig(const float* __restrict__ coeff, float* __restrict__ trig, int64_t nd) {
@@ -541,6 +558,36 @@ int grid_size(const hpf_respa_plan* p) {
 }  // namespace
 
 extern "C" {
+
+int hpf_respa_plan_permute(hpf_respa_plan* p, const int32_t* inv, int64_t n,
+                           const int32_t* free_ids, int64_t n_free, int* d_err, void* stream) {
+    if (!p || !inv || n != p->n_beads || (free_ids && n_free != p->n_free)) return HPF_ERR_ARG;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (p->n_bonded > 0) {
+        const int blocks = (int)std::min<int64_t>((p->n_bonded + 255) / 256, 4 * 152);
+        k_remap_ids<<<blocks, 256, 0, st>>>(p->bead_ids, p->n_bonded, inv, n, d_err);
+        if (cudaGetLastError() != cudaSuccess) return HPF_ERR_CUDA;
+    }
+    if (p->n_free > 0) {
+        if (free_ids) {
+            if (cudaMemcpyAsync(p->free_ids, free_ids, sizeof(int32_t) * (size_t)p->n_free,
+                                cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+                return HPF_ERR_CUDA;
+        } else {
+            const int blocks = (int)std::min<int64_t>((p->n_free + 255) / 256, 4 * 152);
+            k_remap_ids<<<blocks, 256, 0, st>>>(p->free_ids, p->n_free, inv, n, d_err);
+            if (cudaGetLastError() != cudaSuccess) return HPF_ERR_CUDA;
+        }
+    }
+    return HPF_OK;
+}
+
+int hpf_respa_plan_counts(const hpf_respa_plan* p, int64_t* n_bonded, int64_t* n_free) {
+    if (!p) return HPF_ERR_ARG;
+    if (n_bonded) *n_bonded = p->n_bonded;
+    if (n_free) *n_free = p->n_free;
+    return HPF_OK;
+}
 
 int hpf_respa_plan_destroy(hpf_respa_plan* p) {
     if (!p) return HPF_OK;
@@ -709,6 +756,7 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
     memset(p, 0, sizeof(*p));
     p->n_beads = n;
     p->n_groups = G;
+    p->n_bonded = grp_bead[G];
     p->n_free = (int)free_ids.size();
     p->warp_mode = warp_mode;
     p->has_dih = nd > 0;

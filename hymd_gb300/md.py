@@ -75,12 +75,25 @@ class RespaMD:
         self._packed = packed
         self.block_beads = None
         self.perm = None  # memory order -> input order, after sort_particles()
+        # bead order of the mesh-cell sort: "molecule" keeps each molecule's
+        # beads together (ordered by the cell of one bead of the molecule),
+        # "bead" sorts every bead by its own cell
+        self.sort_order = "molecule"
+        self._mol = None  # per bead: a bead of its molecule (int32, device)
+        self._free_ids = None  # the plan's free beads, ascending (int32, device)
+        self._inv_acc = None  # composed re-sorts not yet applied to the host topology
+        self._packed_dirty = False
+        self._resort_graph = None
+        self.resort_every = 0  # run(): re-sort by mesh cell every this many steps
+        self.resorts = 0
+        self.steps_run = 0
         if fused and self.topo is not None and packed is not None:
             if max_block_beads == "auto":
                 self.plan = self._tune_plan(packed)
             else:
                 self.plan = self._make_plan(packed, max_block_beads)
                 self.block_beads = int(max_block_beads)
+            self._index_free()
         self.graph = None
         self.graph_inner = self.graph_field = None
         self.field_sums = torch.zeros(8, dtype=torch.float64, device=self.device)
@@ -192,42 +205,212 @@ class RespaMD:
                  "f_angle",
                  "f_dih", "group")
 
-    def sort_particles(self):
-        """Reorder the beads in memory by the mesh cell of their current
-        position (x-major cell index, stable), so that neighbouring threads of
-        the paint and readout touch neighbouring mesh points.  Every per-bead
-        array is permuted in place and the bonded topology and the fused plan
-        are rebuilt with the new indices; the physics is unchanged.  `perm`
-        maps memory order to the caller's order (`in_input_order`).  Call
-        before capture() (a captured graph holds the old plan)."""
+    def sort_particles(self, order=None):
+        """Reorder the beads in memory by mesh cell (x-major cell index,
+        stable), so that neighbouring threads of the paint and readout touch
+        neighbouring mesh points.  order="molecule" (the default,
+        `sort_order`) keeps the beads of a molecule together, ordered by the
+        cell of one bead of the molecule, so that the bonded kernels still
+        read each molecule from one stretch of memory; order="bead" sorts each
+        bead by its own cell.  Every per-bead array is permuted in place and
+        the bonded topology and the fused plan are rebuilt with the new
+        indices; the physics is unchanged.  `perm` maps memory order to the
+        caller's order (`in_input_order`).  Call before capture() (a captured
+        graph holds the old plan); resort() re-sorts a captured system."""
         if self.graph is not None or self.graph_inner is not None:
             raise RuntimeError("sort_particles() must come before capture()")
-        n0, n1, n2 = self.pm.Nmesh
-        nn = torch.tensor([n0, n1, n2], dtype=torch.float64, device=self.device)
-        c = torch.floor(self.r.double() / self.box * nn).long()
-        c = torch.remainder(c, nn.long())
-        key = (c[:, 0] * n1 + c[:, 1]) * n2 + c[:, 2]
-        perm = torch.argsort(key, stable=True)
+        if order is not None:
+            if order not in ("molecule", "bead"):
+                raise ValueError(f"unknown sort order {order!r}")
+            self.sort_order = order
+        self._sync_packed()
+        self._index_molecules()
+        perm = self._cell_order()
+        inv = torch.empty_like(perm)
+        inv[perm] = torch.arange(self.n, device=self.device)
         for name in self._PER_BEAD:
             t = getattr(self, name, None)
             if t is not None:
                 t.copy_(t[perm])
+        if self._mol is not None:
+            self._mol.copy_(inv[self._mol[perm].long()].to(torch.int32))
         if self._packed is not None:
-            inv = torch.empty_like(perm)
-            inv[perm] = torch.arange(self.n, device=self.device)
-            inv = inv.cpu().numpy()
+            inv_h = inv.cpu().numpy()
             packed = list(self._packed)
-            for k in (0, 1, 4, 5, 6, 9, 10, 11, 12):  # bead index arrays
-                packed[k] = inv[np.asarray(packed[k], dtype=np.int64)].astype(np.int32)
+            for k in self._PACKED_IDS:
+                packed[k] = inv_h[np.asarray(packed[k], dtype=np.int64)].astype(np.int32)
             self._packed = tuple(packed)
             self.topo = BondedTopology(self._packed, device=self.device)
             if self.plan is not None:
                 _lib.lib().hpf_respa_plan_destroy(self.plan)
                 self.plan = self._make_plan(self._packed, self.block_beads)
+                self._index_free()
         self.perm = perm if self.perm is None else self.perm[perm]
         if self.charges is not None:
             self._index_charged()
         return self.perm
+
+    # bead index arrays of the packed topology (bonds a, b; angles a, b, c;
+    # dihedrals a, b, c, d)
+    _PACKED_IDS = (0, 1, 4, 5, 6, 9, 10, 11, 12)
+
+    def _bonded_pairs(self):
+        """Both ends of every bond and of the consecutive bead pairs of every
+        angle and dihedral (device int64), or None without a topology."""
+        t = self.topo
+        if t is None:
+            return None
+        pairs = [(t.bond_a, t.bond_b), (t.ang_a, t.ang_b), (t.ang_b, t.ang_c),
+                 (t.dih_a, t.dih_b), (t.dih_b, t.dih_c), (t.dih_c, t.dih_d)]
+        pairs = [(a, b) for a, b in pairs if a.numel()]
+        if not pairs:
+            return None
+        return (torch.cat([a.long() for a, _ in pairs]), torch.cat([b.long() for _, b in pairs]))
+
+    def _index_molecules(self):
+        """Per bead, the smallest bead index of its molecule (the connected
+        component of the bonded terms), by label propagation with pointer
+        jumping; a free bead is its own molecule.  Kept (and permuted) for the
+        "molecule" sort order."""
+        if self.sort_order != "molecule" or self._mol is not None:
+            return
+        lab = torch.arange(self.n, device=self.device)
+        pairs = self._bonded_pairs()
+        if pairs is not None:
+            a, b = pairs
+            while True:
+                m = torch.minimum(lab[a], lab[b])
+                new = lab.clone()
+                new.scatter_reduce_(0, a, m, "amin")
+                new.scatter_reduce_(0, b, m, "amin")
+                new = new[new]
+                if torch.equal(new, lab):
+                    break
+                lab = new
+        self._mol = lab.to(torch.int32)
+
+    def _index_free(self):
+        """The plan's free beads (in no bonded term) in ascending order, kept
+        beside the plan so that a re-sort hands it the new list in memory
+        order."""
+        if self.plan is None:
+            self._free_ids = None
+            return
+        mask = torch.zeros(self.n, dtype=torch.bool, device=self.device)
+        pairs = self._bonded_pairs()
+        if pairs is not None:
+            mask[pairs[0]] = True
+            mask[pairs[1]] = True
+        self._free_ids = torch.nonzero(~mask).reshape(-1).to(torch.int32).contiguous()
+        nb, nf = _lib.I64(), _lib.I64()
+        _lib.call("hpf_respa_plan_counts", self.plan, _lib.ctypes.byref(nb),
+                  _lib.ctypes.byref(nf))
+        if nf.value != self._free_ids.numel():
+            raise RuntimeError("free-bead count differs from the plan's")
+
+    def _cell_order(self):
+        """Stable permutation of the beads by the x-major index of the mesh
+        cell of their current position; in the "molecule" order by the cell
+        of the molecule's first bead, then by that bead, so that each
+        molecule stays in one stretch.  Capturable (no host copies)."""
+        n1, n2 = self.pm.Nmesh[1], self.pm.Nmesh[2]
+        if getattr(self, "_nmesh", None) is None:
+            self._nmesh = torch.tensor(list(self.pm.Nmesh), dtype=torch.float64,
+                                       device=self.device)
+        nn = self._nmesh
+        c = torch.floor(self.r.double() / self.box * nn).long()
+        c = torch.remainder(c, nn.long())
+        key = (c[:, 0] * n1 + c[:, 1]) * n2 + c[:, 2]
+        if self.sort_order == "molecule" and self._mol is not None:
+            mol = self._mol.long()
+            key = key[mol] * self.n + mol
+        return torch.argsort(key, stable=True)
+
+    def resort(self):
+        """Re-sort the beads by mesh cell between steps (the order the paint
+        and readout want decays as beads move: at ~0.2 nm/ps a bead leaves
+        its 0.3 nm cell within a few outer steps).  Unlike sort_particles()
+        nothing is reallocated or rebuilt: every per-bead buffer is permuted
+        in place, the fused plan's bead lists are remapped on the device
+        (hpf_respa_plan_permute) with its free beads handed over again in
+        ascending order, the bonded index arrays are remapped and the charged
+        beads re-listed in ascending order, so graphs captured before stay
+        valid.  Once the step is captured the re-sort is captured too (its
+        own graph, replayed on later calls).  Per-bead results are
+        unchanged; sums over beads (energies, CSVR) change in their last bits
+        with the summation order.  `perm` follows."""
+        if self.perm is None:
+            self.perm = torch.arange(self.n, device=self.device)
+        if self._inv_acc is None:
+            self._inv_acc = torch.arange(self.n, device=self.device)
+        if self.sort_order == "molecule" and self._mol is None:
+            self._index_molecules()
+        captured = self.graph is not None or self.graph_inner is not None
+        if self._resort_graph is not None:
+            self._resort_graph.replay()
+        elif captured:
+            # the first re-sort of a captured system runs on a side stream and
+            # records the graph that later ones replay
+            s = torch.cuda.Stream(device=self.device)
+            s.wait_stream(torch.cuda.current_stream(self.device))
+            with torch.cuda.stream(s):
+                self._resort_body()
+            torch.cuda.current_stream(self.device).wait_stream(s)
+            torch.cuda.synchronize(self.device)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._resort_body()
+            self._resort_graph = g
+        else:
+            self._resort_body()
+        self._packed_dirty = True
+        self.resorts += 1
+
+    def _resort_body(self):
+        """The device work of one re-sort; static shapes, no host copies."""
+        p = self._cell_order()
+        inv = torch.empty_like(p)
+        inv.scatter_(0, p, torch.arange(self.n, device=self.device))
+        inv32 = inv.to(torch.int32)
+        for name in self._PER_BEAD:
+            t = getattr(self, name, None)
+            if t is not None:
+                t.copy_(t[p])
+        if self._mol is not None:
+            self._mol.copy_(inv32[self._mol[p].long()])
+        st = _lib.stream_ptr()
+        if self.plan is not None:
+            free = None
+            if self._free_ids is not None and self._free_ids.numel():
+                self._free_ids.copy_(torch.sort(inv32[self._free_ids.long()]).values)
+                free = self._free_ids
+            _lib.call("hpf_respa_plan_permute", self.plan, _lib.ptr(inv32), self.n,
+                      None if free is None else _lib.ptr(free),
+                      0 if free is None else free.numel(), _lib.ptr(self.err), st)
+        t = self.topo
+        if t is not None:
+            for name in ("bond_a", "bond_b", "ang_a", "ang_b", "ang_c", "dih_a", "dih_b",
+                         "dih_c", "dih_d"):
+                a = getattr(t, name)
+                if a.numel():
+                    a.copy_(inv32[a.long()])
+        if self.charged is not None and self.charged.numel():
+            self.charged.copy_(torch.sort(inv32[self.charged.long()]).values)
+        self.perm.copy_(self.perm[p])
+        # the host copy of the topology follows when a plan is rebuilt
+        self._inv_acc.copy_(inv[self._inv_acc])
+
+    def _sync_packed(self):
+        """Apply the re-sorts since the last plan build to the host topology."""
+        if self._packed is None or not self._packed_dirty:
+            return
+        inv = self._inv_acc.cpu().numpy()
+        packed = list(self._packed)
+        for k in self._PACKED_IDS:
+            packed[k] = inv[np.asarray(packed[k], dtype=np.int64)].astype(np.int32)
+        self._packed = tuple(packed)
+        self._inv_acc.copy_(torch.arange(self.n, device=self.device))
+        self._packed_dirty = False
 
     def in_input_order(self, t):
         """A per-bead tensor (in memory order) returned in the caller's order."""
@@ -651,11 +834,17 @@ class RespaMD:
             self.graph.replay()
 
     def run(self, steps):
+        """`steps` outer steps (graph replays once captured); with
+        resort_every > 0 the beads are re-sorted by mesh cell after every
+        resort_every-th step."""
         for _ in range(steps):
             if self.graph is not None or self.graph_inner is not None:
                 self.replay()
             else:
                 self.step()
+            self.steps_run += 1
+            if self.resort_every and self.steps_run % self.resort_every == 0:
+                self.resort()
 
     def run_host(self, r_in, v_in, r_out, steps=1):
         """`steps` outer steps, each from a host-side state: positions and

@@ -398,6 +398,21 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n_beads, int64_t nb, con
                           const int32_t* dih_c, const int32_t* dih_d, const float* dih_coeff,
                           const int32_t* dih_type, const int32_t* dih_last, int max_block_beads);
 int hpf_respa_plan_destroy(hpf_respa_plan* plan);
+/* The bead arrays were permuted (a re-sort by mesh cell between steps):
+ * inv (device int32[n], n = the plan's bead count) maps each old bead index
+ * to its new one.  The groups' bead lists are remapped in place; the list of
+ * free beads (in no bonded term) is replaced by free_ids (device
+ * int32[n_free], the free beads' new indices, ascending, so that the free
+ * beads are read in memory order), or remapped in place when free_ids is
+ * NULL.  Graphs captured with this plan stay valid.  No counterpart in the
+ * reference (its beads move between MPI ranks in domain_decomposition,
+ * field.py:1115-1194, which rebuilds the bonded lists instead).  d_err
+ * (device int, may be NULL) receives HPF_ERR_INDEX for an index outside
+ * [0, n).  Stream-ordered; does not synchronise. */
+int hpf_respa_plan_permute(hpf_respa_plan* plan, const int32_t* inv, int64_t n,
+                           const int32_t* free_ids, int64_t n_free, int* d_err, void* stream);
+/* Beads in molecule groups and free beads of a plan (host). */
+int hpf_respa_plan_counts(const hpf_respa_plan* plan, int64_t* n_bonded, int64_t* n_free);
 int hpf_respa_plan_info(const hpf_respa_plan* plan, int* n_mol_blocks, int* n_free,
                         int* max_block_beads);
 /* hpf_respa_step (the launch itself) is declared after the barostat

@@ -289,3 +289,79 @@ def test_md_with_charges_compact_pic_matches_full_pic():
     assert torch.equal(a.r, b.r) and torch.equal(a.v, b.v)
     a.check_errors()
     b.check_errors()
+
+
+@pytest.mark.parametrize("captured", [False, True])
+def test_resort_keeps_trajectory(captured):
+    """RespaMD.resort() between steps (the beads re-sorted by mesh cell in
+    place, the plan's bead lists, the bonded indices and the charged-bead
+    list remapped on the device): in NVE every per-bead result is independent
+    of the memory order, so positions and velocities in the caller's order
+    equal those of the run without re-sorting, bit for bit -- also when the
+    step was captured in graphs before the re-sorts."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.charged_peptides(seed=5, n_chains=12, n_res=30, n_total=6000, box=8.0, mesh=32)
+    cfg = s["config"]
+    ham = get_hamiltonian(cfg)
+    kw = dict(topology=s["topology"], charges=s["charges"])
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    for m in (a, b):
+        m.prime()
+        if captured:
+            m.capture()
+    a.resort_every = 2
+    a.run(6)
+    b.run(6)
+    torch.cuda.synchronize()
+    assert a.resorts == 3 and a.perm is not None
+    assert torch.equal(a.in_input_order(a.r), b.r)
+    assert torch.equal(a.in_input_order(a.v), b.v)
+    assert torch.equal(a.in_input_order(a.f_elec), b.f_elec)
+    a.check_errors()
+    b.check_errors()
+    # the lists handed back in memory order: charged and free beads ascending,
+    # each molecule in one stretch of memory
+    ch = a.charged.long()
+    assert torch.all(ch[1:] > ch[:-1])
+    assert torch.equal(ch, torch.nonzero(a.charges != 0).reshape(-1))
+    fr = a._free_ids.long()
+    assert fr.numel() and torch.all(fr[1:] > fr[:-1])
+    mol = a._mol.long()
+    first = torch.full((a.n,), a.n, dtype=torch.long, device=mol.device)
+    last = torch.full((a.n,), -1, dtype=torch.long, device=mol.device)
+    idx = torch.arange(a.n, device=mol.device)
+    first.scatter_reduce_(0, mol, idx, "amin")
+    last.scatter_reduce_(0, mol, idx, "amax")
+    size = torch.bincount(mol, minlength=a.n)
+    used = size > 0
+    assert torch.equal((last - first + 1)[used], size[used])
+    assert int(size.max()) == 60  # the 30-residue chains (60 beads) are whole molecules
+
+
+def test_bead_sort_order_keeps_trajectory():
+    """The "bead" sort order (every bead by its own cell) gives the same
+    trajectory in the caller's order as the unsorted run."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.charged_peptides(seed=6, n_chains=8, n_res=20, n_total=4000, box=7.0, mesh=28)
+    cfg = s["config"]
+    ham = get_hamiltonian(cfg)
+    kw = dict(topology=s["topology"], charges=s["charges"])
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    a.sort_particles(order="bead")
+    for m in (a, b):
+        m.prime()
+        m.capture()
+    a.resort_every = 3
+    a.run(6)
+    b.run(6)
+    torch.cuda.synchronize()
+    assert a.resorts == 2
+    assert torch.equal(a.in_input_order(a.r), b.r)
+    assert torch.equal(a.in_input_order(a.v), b.v)
+    a.check_errors()
