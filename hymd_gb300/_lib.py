@@ -104,6 +104,8 @@ _SIGNATURES.update({
     "hpf_field_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P, ctypes.POINTER(Kick), P],
     "hpf_pic_step": [P, P, P, I64, D, P, P, P, P, P, P, ctypes.POINTER(Kick), P],
     "hpf_pic_step_list": [P, P, P, P, I64, I64, D, P, P, ctypes.POINTER(Kick), P],
+    "hpf_field_pic_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P, P, P, I64, D, P, P,
+                           ctypes.POINTER(Kick), P],
     "hpf_csvr_scale": [P, P, I64, P, I, P],
     "hpf_field_step_profile": [P, P, P, I64, ctypes.POINTER(D), P, P, P, ctypes.POINTER(Kick), P,
                                ctypes.POINTER(ctypes.c_float)],

@@ -863,6 +863,31 @@ int launch_readout(hpf_ctx* c, const float* fm, const float* pos, const int32_t*
     return HPF_OK;
 }
 
+SpecBufs main_bufs(hpf_ctx* c) { return SpecBufs{c->d_spec_phi, c->d_spec, c->d_grid, c->d_spec_ws}; }
+SpecBufs pic_bufs(hpf_ctx* c) {
+    return SpecBufs{c->pic_spec_phi, c->pic_spec, c->pic_grid, c->pic_spec_ws};
+}
+
+// The charge chain's scratch, stream and events (first use; refused under
+// stream capture, where nothing may be allocated).
+int pic_chain_setup(hpf_ctx* c, cudaStream_t st) {
+    if (c->pic_stream) return HPF_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return HPF_ERR_ARG;
+    const size_t words = spectral_ws_words(c);
+    if (cudaMalloc(&c->pic_spec_phi, sizeof(float2) * (size_t)c->Mc) != cudaSuccess ||
+        cudaMalloc(&c->pic_spec, sizeof(float2) * 2 * (size_t)c->Mc) != cudaSuccess ||
+        cudaMalloc(&c->pic_grid, sizeof(float) * 4 * (size_t)c->M) != cudaSuccess ||
+        cudaMalloc(&c->pic_spec_ws, sizeof(double) * words) != cudaSuccess ||
+        cudaMemset(c->pic_spec_ws, 0, sizeof(double) * words) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->pic_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->pic_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->pic_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return HPF_ERR_CUDA;
+    return HPF_OK;
+}
+
 int exec_r2c(hpf_ctx* c, const float* in, float2* out, int batch, cudaStream_t st) {
     if (batch < 1 || batch > HPF_MAX_TYPES || !c->has_r2c[batch]) return HPF_ERR_ARG;
     cufftHandle p = c->plan_r2c[batch];
@@ -928,6 +953,13 @@ int hpf_ctx_destroy(hpf_ctx* c) {
     cudaFreeHost(c->gpe_host);
     cudaFree(c->d_tw);
     cudaFree(c->d_spec_ws);
+    cudaFree(c->pic_spec_phi);
+    cudaFree(c->pic_spec);
+    cudaFree(c->pic_grid);
+    cudaFree(c->pic_spec_ws);
+    if (c->pic_stream) cudaStreamDestroy(c->pic_stream);
+    if (c->pic_fork) cudaEventDestroy(c->pic_fork);
+    if (c->pic_join) cudaEventDestroy(c->pic_join);
     free(c);
     return HPF_OK;
 }
@@ -1298,7 +1330,8 @@ int hpf_pic_step(hpf_ctx* c, const float* pos, const float* charges, int64_t n,
         if ((r = do_paint(c, pos, nullptr, charges, n, 1, sc, c->d_grid, st, nullptr, false)) !=
             HPF_OK)
             return r;
-        if ((r = spectral_pic(c, four_pi_fac, psi != nullptr, sums, st)) != HPF_OK) return r;
+        if ((r = spectral_pic(c, main_bufs(c), four_pi_fac, psi != nullptr, sums, st)) != HPF_OK)
+            return r;
     } else {
         float* rho = phi_q ? phi_q : c->d_grid;
         if ((r = do_paint(c, pos, nullptr, charges, n, 1, sc, rho, st)) != HPF_OK) return r;
@@ -1342,7 +1375,8 @@ int hpf_pic_step_list(hpf_ctx* c, const float* pos, const float* charges, const 
                       !c->spec_fused, idx, n)) != HPF_OK)
         return r;
     if (c->spec_fused) {
-        if ((r = spectral_pic(c, four_pi_fac, false, sums, st)) != HPF_OK) return r;
+        if ((r = spectral_pic(c, main_bufs(c), four_pi_fac, false, sums, st)) != HPF_OK)
+            return r;
     } else {
         if ((r = exec_r2c(c, c->d_grid, c->d_spec_phi, 1, st)) != HPF_OK) return r;
         KGeom g = kgeom(c);
@@ -1363,6 +1397,72 @@ int hpf_pic_step_list(hpf_ctx* c, const float* pos, const float* charges, const 
         memset(&kd, 0, sizeof(kd));
         k_readout<0><<<grid_for(count, kThreads), kThreads, 0, st>>>(
             c->d_grid + c->M, pos, nullptr, charges, count, 1, c->M, c->d_box, elec_forces,
+            c->d_err, kd, idx, n);
+        HPF_LAUNCH_CHECK();
+    }
+    return HPF_OK;
+}
+
+int hpf_field_pic_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
+                       const double* type_mass, float* force, double* sums,
+                       const double* pos_scale, const float* charges, const int32_t* idx,
+                       int64_t count, double elec_factor, float* elec_forces, double* pic_sums,
+                       const HpfKick* kick, void* stream) {
+    if (!c || !type_mass || n < 0 || count < 0 || count > n ||
+        (n > 0 && (!pos || !types || !force)) ||
+        (count > 0 && (!charges || !idx || !elec_forces)))
+        return HPF_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    int r;
+    if (!c->spec_fused) {
+        // the library-FFT path shares its plans' work area: one chain after
+        // the other
+        if ((r = hpf_field_step(c, pos, types, n, type_mass, force, sums, pos_scale, nullptr,
+                                stream)) != HPF_OK)
+            return r;
+        return hpf_pic_step_list(c, pos, charges, idx, count, n, elec_factor, elec_forces,
+                                 pic_sums, kick, stream);
+    }
+    if ((r = pic_chain_setup(c, st)) != HPF_OK) return r;
+    TypeScale sc, sq;
+    for (int t = 0; t < c->T; ++t) sc.s[t] = (float)type_mass[t];
+    sq.s[0] = 1.0f;
+    const float four_pi_fac = (float)(4.0 * 3.14159265358979323846 * elec_factor);
+    // a barostat's rescaling of the positions happens in the density paint:
+    // the charge chain starts after it
+    if (pos_scale && (r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale,
+                                   false)) != HPF_OK)
+        return r;
+    HPF_CUDA_TRY(cudaEventRecord(c->pic_fork, st));
+    HPF_CUDA_TRY(cudaStreamWaitEvent(c->pic_stream, c->pic_fork, 0));
+    // charge chain (paint of the listed beads, passes A, B, C) on the second
+    // stream; the join below is recorded whatever happened, so that a stream
+    // capture is never left forked
+    r = do_paint(c, pos, nullptr, charges, count, 1, sq, c->pic_grid, c->pic_stream, nullptr,
+                 false, idx, n);
+    if (r == HPF_OK) r = spectral_pic(c, pic_bufs(c), four_pi_fac, false, pic_sums, c->pic_stream);
+    const cudaError_t je = cudaEventRecord(c->pic_join, c->pic_stream);
+    // density chain on the caller's stream
+    int rd = HPF_OK;
+    if (!pos_scale)
+        rd = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, nullptr, false);
+    if (rd == HPF_OK) rd = spectral_field_force(c, sc.s, sums, st);
+    if (rd == HPF_OK && n > 0)
+        rd = launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, nullptr, st);
+    if (je != cudaSuccess) return HPF_ERR_CUDA;
+    HPF_CUDA_TRY(cudaStreamWaitEvent(st, c->pic_join, 0));
+    if (r != HPF_OK) return r;
+    if (rd != HPF_OK) return rd;
+    // charge readout (q E), with the kick and the CSVR sums over every bead
+    // when kicking, as hpf_pic_step_list
+    if (kick && n > 0)
+        return launch_readout(c, c->pic_grid + c->M, pos, nullptr, charges, n, 1, elec_forces,
+                              kick, st);
+    if (count > 0) {
+        KickDev kd;
+        memset(&kd, 0, sizeof(kd));
+        k_readout<0><<<grid_for(count, kThreads), kThreads, 0, st>>>(
+            c->pic_grid + c->M, pos, nullptr, charges, count, 1, c->M, c->d_box, elec_forces,
             c->d_err, kd, idx, n);
         HPF_LAUNCH_CHECK();
     }

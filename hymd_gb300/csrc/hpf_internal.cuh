@@ -77,6 +77,26 @@ struct hpf_ctx {
     int spec_W, spec_tiles, spec_max_tiles;
     int spec_ok;     // the mesh qualifies and the scratch exists
     int spec_fused;  // use them (default when spec_ok)
+    // the charge chain's own scratch, so that it can run beside the density
+    // chain (hpf_field_pic_step; created on first use, outside capture):
+    // spectra float2[1 + 2][Mc], grids float[4][M] (psi, E_x, E_y, E_z),
+    // partial sums + ticket; a second stream and the fork / join events
+    float2* pic_spec_phi;
+    float2* pic_spec;
+    float* pic_grid;
+    double* pic_spec_ws;
+    cudaStream_t pic_stream;
+    cudaEvent_t pic_fork, pic_join;
+};
+
+// Buffers of one chain of the fused spectral passes: spectra in (pass A ->
+// B) and out (B -> C), the real force grids of pass C, and the partial sums
+// + ticket of pass B's reduction.
+struct SpecBufs {
+    float2* spec_phi;
+    float2* spec;
+    float* grid;
+    double* ws;
 };
 
 // Paint deposits are integers in units of 2^-24 of a particle's weight (a
@@ -100,7 +120,10 @@ int spectral_setup(hpf_ctx* c);
 bool spectral_tile_ok(const hpf_ctx* c, int W);
 int spectral_set_tile(hpf_ctx* c, int W);
 int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cudaStream_t st);
-int spectral_pic(hpf_ctx* c, float four_pi_fac, bool want_psi, double* sums, cudaStream_t st);
+int spectral_pic(hpf_ctx* c, const SpecBufs& b, float four_pi_fac, bool want_psi, double* sums,
+                 cudaStream_t st);
+// words of a pass-B partial-sum buffer (partials of the narrowest tile + ticket)
+size_t spectral_ws_words(const hpf_ctx* c);
 
 #define HPF_REDUCE_GRID 304  // blocks of a reduction kernel (2 per SM on 152 SMs)
 

@@ -660,7 +660,7 @@ int spectral_setup(hpf_ctx* c) {
     // partials: 4 values x tiles (double-float pairs), then the ticket; room
     // for the narrowest tile, so that the width can change later
     c->spec_max_tiles = (int)(cols / 4);
-    const size_t words = 4 * (size_t)c->spec_max_tiles + 8;
+    const size_t words = spectral_ws_words(c);
     if (cudaMalloc(&c->d_spec_ws, sizeof(double) * words) != cudaSuccess) return HPF_ERR_CUDA;
     if (cudaMemset(c->d_spec_ws, 0, sizeof(double) * words) != cudaSuccess) return HPF_ERR_CUDA;
     // the kernels' shared-memory ceilings are process-wide attributes: set
@@ -687,6 +687,8 @@ int spectral_setup(hpf_ctx* c) {
     c->spec_ok = 1;
     return HPF_OK;
 }
+
+size_t spectral_ws_words(const hpf_ctx* c) { return 4 * (size_t)c->spec_max_tiles + 8; }
 
 // accumulators (T grids, painted) -> force mesh c->d_grid [3T][M]; sums as
 // k_kspace_force's (out[0..3]) when non-null.
@@ -720,31 +722,31 @@ int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cuda
 }
 
 // charge accumulator (slot T, painted) -> psi (grid 0, when want_psi) and
-// E_d (grids 1..3) in c->d_grid; sums[0] as k_kspace_pic's when non-null.
-int spectral_pic(hpf_ctx* c, float four_pi_fac, bool want_psi, double* sums, cudaStream_t st) {
+// E_d (grids 1..3) in b.grid; sums[0] as k_kspace_pic's when non-null.
+int spectral_pic(hpf_ctx* c, const SpecBufs& b, float four_pi_fac, bool want_psi, double* sums,
+                 cudaStream_t st) {
     const SpecGeom g = spec_geom(c);
     SpecScale sc;
     sc.s[0] = 1.0f;
     const int ps = (int)plane_smem(c), ts = (int)tile_smem(c, g.W);
     with_planes(c->n1, c->n2 / 2, [&](auto kf, auto) {
         kf<<<dim3(c->n0, 1), kSpecThreads, ps, st>>>(c->d_acc + (int64_t)c->T * c->M,
-                                                     c->d_spec_phi, g, sc, c->d_box, c->d_tw);
+                                                     b.spec_phi, g, sc, c->d_box, c->d_tw);
         return HPF_OK;
     });
     HPF_LAUNCH_CHECK();
-    double* part = c->d_spec_ws;
-    unsigned int* tick = reinterpret_cast<unsigned int*>(c->d_spec_ws + 4 * (size_t)c->spec_max_tiles);
+    double* part = b.ws;
+    unsigned int* tick = reinterpret_cast<unsigned int*>(b.ws + 4 * (size_t)c->spec_max_tiles);
     int r = with_kspace(c->n0, [&](auto, auto kp) {
-        kp<<<c->spec_tiles, kSpecThreads, ts, st>>>(c->d_spec_phi, c->d_spec, g, c->d_box,
-                                                    c->d_fun, four_pi_fac, c->d_tw, sums, part,
-                                                    tick);
+        kp<<<c->spec_tiles, kSpecThreads, ts, st>>>(b.spec_phi, b.spec, g, c->d_box, c->d_fun,
+                                                    four_pi_fac, c->d_tw, sums, part, tick);
         return HPF_OK;
     });
     if (r != HPF_OK) return r;
     HPF_LAUNCH_CHECK();
     const int first = want_psi ? 0 : 1;
     with_planes(c->n1, c->n2 / 2, [&](auto, auto ki) {
-        ki<<<dim3(c->n0, 4 - first), kSpecThreads, ps, st>>>(c->d_spec, c->d_grid, g, c->d_box,
+        ki<<<dim3(c->n0, 4 - first), kSpecThreads, ps, st>>>(b.spec, b.grid, g, c->d_box,
                                                              c->d_tw, first, 1);
         return HPF_OK;
     });

@@ -655,11 +655,21 @@ class RespaMD:
         self._kick_keep = k
         return _lib.ctypes.byref(k)
 
+    # charged systems: the density and charge chains of the field step run
+    # on two streams (hpf_field_pic_step) rather than one after the other
+    CONCURRENT_PIC = True
+
     def _field(self, st, sums=None, pos_scale=None, kick=None):
+        scale = None if pos_scale is None else _lib.ctypes.c_void_p(pos_scale)
+        if self.charges is not None and self.CONCURRENT_PIC:
+            _lib.call("hpf_field_pic_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.types),
+                      self.n, self.masses, _lib.ptr(self.f_field), _lib.ptr(sums), scale,
+                      _lib.ptr(self.charges), _lib.ptr(self.charged), self.charged.numel(),
+                      float(self.elec_factor), _lib.ptr(self.f_elec), None, kick, st)
+            return
         last_kick = kick if self.charges is None else None
         _lib.call("hpf_field_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.types), self.n,
-                  self.masses, _lib.ptr(self.f_field), _lib.ptr(sums),
-                  None if pos_scale is None else _lib.ctypes.c_void_p(pos_scale), last_kick, st)
+                  self.masses, _lib.ptr(self.f_field), _lib.ptr(sums), scale, last_kick, st)
         if self.charges is not None:
             # the charge paint visits only the charged beads; the readout (with
             # the kick and the CSVR sums) visits all

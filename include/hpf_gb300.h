@@ -333,6 +333,22 @@ int hpf_pic_step(hpf_ctx* ctx, const float* pos, const float* charges, int64_t n
 int hpf_pic_step_list(hpf_ctx* ctx, const float* pos, const float* charges, const int32_t* idx,
                       int64_t count, int64_t n, double elec_factor, float* elec_forces,
                       double* sums, const HpfKick* kick, void* stream);
+/* Density and charge field step of one outer MD step in one call: the same
+ * results as hpf_field_step(ctx, pos, types, n, type_mass, force, sums,
+ * pos_scale, NULL, stream) followed by hpf_pic_step_list(ctx, pos, charges,
+ * idx, count, n, elec_factor, elec_forces, pic_sums, kick, stream) -- the
+ * reference's update_field + compute_field_force and update_field_force_q
+ * of one step (main.py:606-660) -- with the charge chain (paint, transforms,
+ * Poisson map) run on a second stream of the context beside the density
+ * chain, joined before the charge readout, which carries the kick.  On the
+ * fused spectral path only; otherwise the two calls run one after the other.
+ * The first call allocates the charge chain's scratch (about 3 Mc complex
+ * and 4 M real values) and must not be under stream capture (HPF_ERR_ARG). */
+int hpf_field_pic_step(hpf_ctx* ctx, float* pos, const int32_t* types, int64_t n,
+                       const double* type_mass, float* force, double* sums,
+                       const double* pos_scale, const float* charges, const int32_t* idx,
+                       int64_t count, double elec_factor, float* elec_forces, double* pic_sums,
+                       const HpfKick* kick, void* stream);
 
 /* ---- bonded (f2py calling form, hymd/force.py:8-23, main.py:509-550) ------
  * All three zero their force array first, as the Fortran does.  Indices are

@@ -365,3 +365,36 @@ def test_bead_sort_order_keeps_trajectory():
     assert torch.equal(a.in_input_order(a.r), b.r)
     assert torch.equal(a.in_input_order(a.v), b.v)
     a.check_errors()
+
+
+@pytest.mark.parametrize("barostat", [None, "isotropic"])
+def test_concurrent_charge_chain_matches_sequential(barostat):
+    """hpf_field_pic_step (the charge chain of the field step on a second
+    stream beside the density chain, joined before the charge readout and
+    kick) against hpf_field_step followed by hpf_pic_step_list on one stream:
+    the same kernels on separate scratch, so positions, velocities and both
+    force arrays are bit-identical after captured NVT (CSVR) steps, also when
+    the barostat rescales the positions in the density paint."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.charged_peptides(seed=8, n_chains=10, n_res=25, n_total=5000, box=7.5, mesh=32)
+    cfg = s["config"]
+    cfg.tau_p, cfg.n_b = 1.0, 1
+    ham = get_hamiltonian(cfg)
+    kw = dict(topology=s["topology"], charges=s["charges"])
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    b.CONCURRENT_PIC = False
+    assert a.pm.spectral == "fused"
+    for m in (a, b):
+        m.couple(thermostat=True, barostat=barostat, seed=9, n_steps=20)
+        m.prime()
+        m.capture()
+        m.run(5)
+    torch.cuda.synchronize()
+    for name in ("r", "v", "f_field", "f_elec"):
+        assert torch.equal(getattr(a, name), getattr(b, name)), name
+    assert torch.equal(a.box, b.box)
+    a.check_errors()
+    b.check_errors()
