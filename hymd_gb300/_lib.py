@@ -73,6 +73,8 @@ _SIGNATURES = {
     "hpf_respa_plan_info": [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
     "hpf_respa_step": [P, P, P, P, ctypes.POINTER(P), I, D, D, I, P, P, P, P, P, P, P, P, P,
                        P, P, P],
+    "hpf_respa_step_paint": [P, P, P, P, ctypes.POINTER(P), I, D, D, I, P, P, P, P, P, P, P,
+                             P, P],
     "hpf_sum_dot": [P, P, I64, P, P],
     "hpf_sum_v2": [P, I64, P, P],
 }
@@ -105,7 +107,7 @@ _SIGNATURES.update({
     "hpf_pic_step": [P, P, P, I64, D, P, P, P, P, P, P, ctypes.POINTER(Kick), P],
     "hpf_pic_step_list": [P, P, P, P, I64, I64, D, P, P, ctypes.POINTER(Kick), P],
     "hpf_field_pic_step": [P, P, P, I64, ctypes.POINTER(D), P, P, P, P, P, I64, D, P, P,
-                           ctypes.POINTER(Kick), P],
+                           ctypes.POINTER(Kick), I, P],
     "hpf_csvr_scale": [P, P, I64, P, I, P],
     "hpf_field_step_profile": [P, P, P, I64, ctypes.POINTER(D), P, P, P, ctypes.POINTER(Kick), P,
                                ctypes.POINTER(ctypes.c_float)],

@@ -267,7 +267,11 @@ __device__ __forceinline__ void fft_step1(int count, float inv_count, LD ld, ST 
     }
 }
 
-template <int N, bool INV, bool CFAST, class LD, class FIN>
+// SYNCW: a warp barrier between the loads and the stores of every item, so
+// that fin may overwrite elements other lanes of the warp load (in place,
+// with every transform's items inside one warp: count * N1 a multiple of 32
+// and N1 dividing 32, so that all lanes of a warp run the same iterations).
+template <int N, bool INV, bool CFAST, class LD, class FIN, bool SYNCW = false>
 __device__ __forceinline__ void fft_step2(int count, float inv_count, LD ld, FIN fin) {
     constexpr int N1 = split1(N), N2 = N / N1;
     if (N2 == 1) return;
@@ -285,6 +289,7 @@ __device__ __forceinline__ void fft_step2(int count, float inv_count, LD ld, FIN
 #pragma unroll
         for (int i = 0; i < N2; ++i) a[i] = ld(c, N2 * k1 + i);
         reg_fft<N2, INV>(a);
+        if (SYNCW) __syncwarp();
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) fin(c, k1 + N1 * k2, N2 * k1 + k2, a[k2]);
     }

@@ -57,9 +57,7 @@ __global__ void k_paint(const float* pos, const int32_t* __restrict__ types,
                         const BoxState* __restrict__ bs, unsigned long long* __restrict__ acc,
                         int64_t M, int* err, const double* __restrict__ scale,
                         const int32_t* __restrict__ idx = nullptr, int64_t n_total = 0) {
-    const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
-    const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
-    const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
+    const CicMesh m = cic_mesh(bs);
     const float al = scale ? (float)*scale : 1.0f;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
          j += (int64_t)gridDim.x * blockDim.x) {
@@ -93,32 +91,7 @@ __global__ void k_paint(const float* pos, const int32_t* __restrict__ types,
         }
         const float q = charges ? charges[i] : 1.0f;
         if (q == 0.0f) continue;
-        int ix, iy, iz;
-        float fx, fy, fz;
-        grid_coord(x, h0, l0, n0, ix, fx);
-        grid_coord(y, h1, l1, n1, iy, fy);
-        grid_coord(z, h2, l2, n2, iz, fz);
-        const int jx = ix + 1 == n0 ? 0 : ix + 1;
-        const int jy = iy + 1 == n1 ? 0 : iy + 1;
-        const int jz = iz + 1 == n2 ? 0 : iz + 1;
-        const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy}, wz[2] = {1.0f - fz, fz};
-        const int xs[2] = {ix, jx}, ys[2] = {iy, jy}, zs[2] = {iz, jz};
-        unsigned long long* base = acc + (int64_t)t * M;
-#pragma unroll
-        for (int a = 0; a < 2; ++a)
-#pragma unroll
-            for (int b = 0; b < 2; ++b) {
-                const int64_t row = ((int64_t)xs[a] * n1 + ys[b]) * n2;
-                const float wab = q * wx[a] * wy[b];
-#pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    // fixed point in units of 2^-24 via an FP32 -> int32
-                    // conversion (a 64-bit one runs on the FP64 pipe), summed
-                    // in 64 bits
-                    const long long v = (long long)__float2int_rn(wab * wz[c] * kFixScale);
-                    if (v != 0) atomicAdd(base + row + zs[c], (unsigned long long)v);
-                }
-            }
+        cic_deposit(m, x, y, z, q, acc + (int64_t)t * M);
     }
 }
 
@@ -1407,26 +1380,37 @@ int hpf_field_pic_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
                        const double* type_mass, float* force, double* sums,
                        const double* pos_scale, const float* charges, const int32_t* idx,
                        int64_t count, double elec_factor, float* elec_forces, double* pic_sums,
-                       const HpfKick* kick, void* stream) {
+                       const HpfKick* kick, int painted, void* stream) {
     if (!c || !type_mass || n < 0 || count < 0 || count > n ||
         (n > 0 && (!pos || !types || !force)) ||
-        (count > 0 && (!charges || !idx || !elec_forces)))
+        (count > 0 && (!charges || !idx || !elec_forces)) || (painted && pos_scale))
         return HPF_ERR_ARG;
     cudaStream_t st = as_stream(stream);
     int r;
     if (!c->spec_fused) {
         // the library-FFT path shares its plans' work area: one chain after
-        // the other
-        if ((r = hpf_field_step(c, pos, types, n, type_mass, force, sums, pos_scale, nullptr,
-                                stream)) != HPF_OK)
+        // the other; deposits made elsewhere are not taken
+        if (painted) return HPF_ERR_ARG;
+        if ((r = hpf_field_step(c, pos, types, n, type_mass, force, sums, pos_scale,
+                                charges ? nullptr : kick, stream)) != HPF_OK)
             return r;
+        if (!charges) return HPF_OK;
         return hpf_pic_step_list(c, pos, charges, idx, count, n, elec_factor, elec_forces,
                                  pic_sums, kick, stream);
     }
-    if ((r = pic_chain_setup(c, st)) != HPF_OK) return r;
     TypeScale sc, sq;
     for (int t = 0; t < c->T; ++t) sc.s[t] = (float)type_mass[t];
     sq.s[0] = 1.0f;
+    if (!charges) {
+        // densities only: hpf_field_step, the paint skipped when done already
+        if (!painted && (r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st,
+                                      pos_scale, false)) != HPF_OK)
+            return r;
+        if ((r = spectral_field_force(c, sc.s, sums, st)) != HPF_OK) return r;
+        if (n > 0) return launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, kick, st);
+        return HPF_OK;
+    }
+    if ((r = pic_chain_setup(c, st)) != HPF_OK) return r;
     const float four_pi_fac = (float)(4.0 * 3.14159265358979323846 * elec_factor);
     // a barostat's rescaling of the positions happens in the density paint:
     // the charge chain starts after it
@@ -1438,13 +1422,14 @@ int hpf_field_pic_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
     // charge chain (paint of the listed beads, passes A, B, C) on the second
     // stream; the join below is recorded whatever happened, so that a stream
     // capture is never left forked
-    r = do_paint(c, pos, nullptr, charges, count, 1, sq, c->pic_grid, c->pic_stream, nullptr,
-                 false, idx, n);
+    r = painted ? HPF_OK
+                : do_paint(c, pos, nullptr, charges, count, 1, sq, c->pic_grid, c->pic_stream,
+                           nullptr, false, idx, n);
     if (r == HPF_OK) r = spectral_pic(c, pic_bufs(c), four_pi_fac, false, pic_sums, c->pic_stream);
     const cudaError_t je = cudaEventRecord(c->pic_join, c->pic_stream);
     // density chain on the caller's stream
     int rd = HPF_OK;
-    if (!pos_scale)
+    if (!pos_scale && !painted)
         rd = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, nullptr, false);
     if (rd == HPF_OK) rd = spectral_field_force(c, sc.s, sums, st);
     if (rd == HPF_OK && n > 0)

@@ -393,6 +393,90 @@ __device__ __forceinline__ void grid_coord(float x, float ih_hi, float ih_lo, in
     frac = f;
 }
 
+// Mesh geometry of a CIC deposit, loaded once per thread from a BoxState.
+struct CicMesh {
+    int n0, n1, n2;
+    float h0, h1, h2, l0, l1, l2;  // n_d / L_d as hi + lo floats
+};
+__device__ __forceinline__ CicMesh cic_mesh(const BoxState* bs) {
+    CicMesh m;
+    m.n0 = bs->n[0];
+    m.n1 = bs->n[1];
+    m.n2 = bs->n[2];
+    m.h0 = bs->ih_hi[0];
+    m.h1 = bs->ih_hi[1];
+    m.h2 = bs->ih_hi[2];
+    m.l0 = bs->ih_lo[0];
+    m.l1 = bs->ih_lo[1];
+    m.l2 = bs->ih_lo[2];
+    return m;
+}
+
+// CIC deposit of weight q at (x, y, z) into one grid of int64 accumulators
+// ([n0][n1][n2], units of 2^-24 of a unit weight): the 8 corner weights
+// converted with an FP32 -> int32 rounding (a 64-bit conversion runs on the
+// FP64 pipe) and added with 64-bit atomics, zero deposits skipped.  Integer
+// sums do not depend on the order of the deposits: the grid is
+// bit-deterministic whichever kernel paints and in whatever order.
+__device__ __forceinline__ void cic_deposit(const CicMesh& m, float x, float y, float z, float q,
+                                            unsigned long long* __restrict__ base) {
+    int ix, iy, iz;
+    float fx, fy, fz;
+    grid_coord(x, m.h0, m.l0, m.n0, ix, fx);
+    grid_coord(y, m.h1, m.l1, m.n1, iy, fy);
+    grid_coord(z, m.h2, m.l2, m.n2, iz, fz);
+    const int jx = ix + 1 == m.n0 ? 0 : ix + 1;
+    const int jy = iy + 1 == m.n1 ? 0 : iy + 1;
+    const int jz = iz + 1 == m.n2 ? 0 : iz + 1;
+    const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy}, wz[2] = {1.0f - fz, fz};
+    const int xs[2] = {ix, jx}, ys[2] = {iy, jy}, zs[2] = {iz, jz};
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            const int64_t row = ((int64_t)xs[a] * m.n1 + ys[b]) * m.n2;
+            const float wab = q * wx[a] * wy[b];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const long long v = (long long)__float2int_rn(wab * wz[c] * kFixScale);
+                if (v != 0) atomicAdd(base + row + zs[c], (unsigned long long)v);
+            }
+        }
+}
+
+// A paint fused into another kernel (the rRESPA inner loop): each bead is
+// deposited where that kernel leaves its final position -- its type's
+// density grid and, with charges, the charge grid after the T density
+// grids -- with the deposits of k_paint (cic_deposit), so the accumulators
+// end up bit-identical to those of a separate paint.
+struct PaintFuse {
+    unsigned long long* acc;  // int64 accumulators [T + 1][M]
+    const BoxState* bs;       // mesh of the field context
+    const int32_t* types;     // bead types
+    const float* charges;     // bead charges, or nullptr (no charge grid)
+    int64_t M;
+    int T;
+    int* err;                 // first error code (non-finite position, type)
+};
+
+__device__ __forceinline__ void paint_bead(const PaintFuse& pf, const CicMesh& m, int64_t i,
+                                           float x, float y, float z) {
+    if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+        hpf_flag(pf.err, HPF_ERR_NONFINITE);
+        return;
+    }
+    const int t = pf.types[i];
+    if (t < 0 || t >= pf.T) {
+        hpf_flag(pf.err, HPF_ERR_INDEX);
+        return;
+    }
+    cic_deposit(m, x, y, z, 1.0f, pf.acc + (int64_t)t * pf.M);
+    if (pf.charges) {
+        const float q = pf.charges[i];
+        if (q != 0.0f) cic_deposit(m, x, y, z, q, pf.acc + (int64_t)pf.T * pf.M);
+    }
+}
+
 // Warp + block reduction of K doubles; thread 0 returns the block totals.
 template <int K>
 __device__ __forceinline__ void block_reduce(double (&v)[K], double* smem /* K*32 */) {
@@ -469,7 +553,7 @@ __device__ __forceinline__ void warp_df_reduce(DF (&v)[K]) {
 // Fixed order, so deterministic.  Writes partials like block_partials_f.
 template <int K, int NT>
 __device__ __forceinline__ void block_partials_ft(float (&vf)[K], double* partials,
-                                                  unsigned int G) {
+                                                  unsigned int G, unsigned int slot) {
     static_assert(NT % 32 == 0 && NT >= 32 && NT <= 1024, "whole warps");
     constexpr int NW = NT / 32, KW = (K + NW - 1) / NW;
     __shared__ float tr[K][NT];
@@ -494,7 +578,7 @@ __device__ __forceinline__ void block_partials_ft(float (&vf)[K], double* partia
 #pragma unroll
         for (int i = 0; i < KW; ++i) {
             const int k = warp + i * NW;
-            if (k < K) part[(size_t)k * G + blockIdx.x] = make_float2(v[i].hi, v[i].lo);
+            if (k < K) part[(size_t)k * G + slot] = make_float2(v[i].hi, v[i].lo);
         }
     }
 }
@@ -505,7 +589,7 @@ __device__ __forceinline__ void block_partials_ft(float (&vf)[K], double* partia
 // block size: every warp reduces all K values, then warp 0 the warps' sums.
 template <int K>
 __device__ __forceinline__ void block_partials_fg(float (&vf)[K], double* partials,
-                                                  unsigned int G) {
+                                                  unsigned int G, unsigned int slot) {
     __shared__ float2 red_p[K * 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (blockDim.x + 31) >> 5;
@@ -530,7 +614,7 @@ __device__ __forceinline__ void block_partials_fg(float (&vf)[K], double* partia
         // value-major: the final pass's loads of one value are coalesced
         if (lane == 0) {
 #pragma unroll
-            for (int k = 0; k < K; ++k) part[(size_t)k * G + blockIdx.x] = make_float2(t[k].hi, t[k].lo);
+            for (int k = 0; k < K; ++k) part[(size_t)k * G + slot] = make_float2(t[k].hi, t[k].lo);
         }
     }
 }
@@ -539,11 +623,17 @@ __device__ __forceinline__ void block_partials_fg(float (&vf)[K], double* partia
 // transposed form block_partials_ft, as long as its shared-memory transpose
 // stays within 16 KB (many values fall back to the per-warp form).
 template <int K, int NT = 0>
-__device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partials, unsigned int G) {
+__device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partials, unsigned int G,
+                                                 unsigned int slot) {
     if constexpr (NT > 0 && (size_t)K * NT * sizeof(float) <= 16384)
-        block_partials_ft<K, NT>(vf, partials, G);
+        block_partials_ft<K, NT>(vf, partials, G, slot);
     else
-        block_partials_fg<K>(vf, partials, G);
+        block_partials_fg<K>(vf, partials, G, slot);
+}
+// the block's own slot: blockIdx.x
+template <int K, int NT = 0>
+__device__ __forceinline__ void block_partials_f(float (&vf)[K], double* partials, unsigned int G) {
+    block_partials_f<K, NT>(vf, partials, G, blockIdx.x);
 }
 
 // Sum of the G block partials of each of K values (written by

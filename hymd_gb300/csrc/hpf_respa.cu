@@ -61,6 +61,10 @@ struct hpf_respa_plan {
     int* dih_gid;      // global dihedral index (dipole / transfer rows)
     int* free_ids;
     double* partials;   // [kOut][grid] block partials (float2 hi/lo per slot)
+    // second stream of the split launch (free beads beside the groups) and
+    // its fork / join events
+    cudaStream_t free_stream;
+    cudaEvent_t free_fork, free_join;
 };
 
 namespace {
@@ -171,11 +175,19 @@ __device__ __forceinline__ float comp(const float4& q, int d) {
     return d == 0 ? q.x : (d == 1 ? q.y : q.z);
 }
 
+// The write-back's deposit of a group bead, out of line: the group kernels
+// run near their register limit in the term loop, and the deposit's
+// addresses and weights would add to it.
+__device__ __noinline__ void paint_group_bead(PaintFuse pf, int64_t bead, float x, float y,
+                                              float z) {
+    paint_bead(pf, cic_mesh(pf.bs), bead, x, y, z);
+}
+
 // Group-local work shared by the warp and CTA variants.  `lane`/`width`
 // enumerate the threads of the group; `sync()` separates the phases.  A
 // bead is always handled by the same lane, so the gather of its forces and
 // its next kick need no barrier in between.
-template <bool DIH, typename Sync>
+template <bool DIH, bool PAINT, typename Sync>
 __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int lane, int width,
                                           char* smem_base, float* __restrict__ r,
                                           float* __restrict__ v, float* __restrict__ fb,
@@ -183,7 +195,7 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                                           float hdt, float dt, int respa, const Box& bx,
                                           float* __restrict__ dipoles,
                                           float* __restrict__ transfer, float (&acc)[kOut],
-                                          Sync sync, bool forces_only) {
+                                          Sync sync, bool forces_only, const PaintFuse& pf) {
     // forces_only: bonded forces (and energies) at the current positions
     // only -- no kicks, no drift, v and r untouched (respa is 1 then)
     const GroupSmem s = carve(smem_base, p);
@@ -337,9 +349,10 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
         }
         sync();
     }
-    // write back (each bead by the lane that owns it)
+    // write back (each bead by the lane that owns it); with PAINT the bead is
+    // deposited on the mesh at its final position
     for (int i = lane; i < nb; i += width) {
-        const int64_t g = 3 * (int64_t)p.bead_ids[s0 + i];
+        const int64_t bead = p.bead_ids[s0 + i], g = 3 * bead;
         const float4 fq = s.fs[i];
         if (forces_only) {
             for (int d = 0; d < 3; ++d) fb[g + d] = comp(fq, d);
@@ -353,17 +366,24 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
             fb[g + d] = comp(fq, d);
             acc[9] = fmaf(x, x, acc[9]);
         }
+        if (PAINT) paint_group_bead(pf, bead, rq.x, rq.y, rq.z);
     }
 }
 
+template <bool PAINT>
 __device__ __forceinline__ void free_beads(const hpf_respa_plan& p, int fblock, float* __restrict__ r,
                                            float* __restrict__ v, const SlowForces& slow,
                                            float mass, float h_out, float dt, int respa,
-                                           const Box& bx, float (&acc)[kOut]) {
+                                           const Box& bx, float (&acc)[kOut],
+                                           const PaintFuse& pf) {
     const int stride = p.n_free_blocks * kThreads;
     const float inv_m = 1.0f / mass;
+    CicMesh cm;
+    if (PAINT) cm = cic_mesh(pf.bs);
     for (int j = fblock * kThreads + threadIdx.x; j < p.n_free; j += stride) {
-        const int64_t g = 3 * (int64_t)p.free_ids[j];
+        const int64_t bead = p.free_ids[j], g = 3 * bead;
+        float yr[3];
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
             float x = v[g + d];
 #pragma unroll
@@ -373,17 +393,22 @@ __device__ __forceinline__ void free_beads(const hpf_respa_plan& p, int fblock, 
             for (int it = 0; it < respa; ++it) y = wrapf(y + dt * x, bx.L[d]);
             v[g + d] = x;
             r[g + d] = y;
+            yr[d] = y;
             acc[9] = fmaf(x, x, acc[9]);
         }
+        // a free bead's position is final after its drift: deposit it now,
+        // while the molecule groups are still integrating
+        if (PAINT) paint_bead(pf, cm, bead, yr[0], yr[1], yr[2]);
     }
 }
 
-template <bool DIH>
+template <bool DIH, bool PAINT>
 __global__ void __launch_bounds__(kThreads)
 k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
              float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
              int respa, const double* __restrict__ box, float* __restrict__ dipoles,
-             float* __restrict__ transfer, double* out, int forces_only) {
+             float* __restrict__ transfer, double* out, int forces_only, PaintFuse pf,
+             unsigned int G) {
     extern __shared__ __align__(16) char smem[];
     const Box bx = load_box(box);
     float acc[kOut];
@@ -394,35 +419,57 @@ k_respa_warp(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
         const int grp = blockIdx.x * kWarps + warp;
         if (grp < p.n_groups)
-            run_group<DIH>(p, grp, lane, 32, smem + (size_t)warp * p.smem_group, r, v, fb, slow,
-                           mass, h_out, hdt, dt, respa, bx, dipoles, transfer, acc, WarpSync(),
-                           forces_only != 0);
+            run_group<DIH, PAINT>(p, grp, lane, 32, smem + (size_t)warp * p.smem_group, r, v, fb,
+                                  slow, mass, h_out, hdt, dt, respa, bx, dipoles, transfer, acc,
+                                  WarpSync(), forces_only != 0, pf);
     } else if (!forces_only) {
-        free_beads(p, blockIdx.x - n_grp_blocks, r, v, slow, mass, h_out, dt, respa, bx, acc);
+        free_beads<PAINT>(p, blockIdx.x - n_grp_blocks, r, v, slow, mass, h_out, dt, respa, bx,
+                          acc, pf);
     }
-    if (out) block_partials_f<kOut, kThreads>(acc, p.partials, gridDim.x);
+    if (out) block_partials_f<kOut, kThreads>(acc, p.partials, G);
 }
 
 // Four blocks per SM: the chain CTAs share the SMs with the free-bead
 // blocks, which need the occupancy to hide their global loads.
-template <bool DIH>
+template <bool DIH, bool PAINT>
 __global__ void __launch_bounds__(kThreads, 4)
 k_respa_cta(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v,
             float* __restrict__ fb, SlowForces slow, float mass, float h_out, float hdt, float dt,
             int respa, const double* __restrict__ box, float* __restrict__ dipoles,
-            float* __restrict__ transfer, double* out, int forces_only) {
+            float* __restrict__ transfer, double* out, int forces_only, PaintFuse pf,
+            unsigned int G) {
     extern __shared__ __align__(16) char smem[];
     const Box bx = load_box(box);
     float acc[kOut];
 #pragma unroll
     for (int k = 0; k < kOut; ++k) acc[k] = 0.0f;
     if ((int)blockIdx.x < p.n_groups) {
-        run_group<DIH>(p, blockIdx.x, threadIdx.x, kThreads, smem, r, v, fb, slow, mass, h_out,
-                       hdt, dt, respa, bx, dipoles, transfer, acc, CtaSync(), forces_only != 0);
+        run_group<DIH, PAINT>(p, blockIdx.x, threadIdx.x, kThreads, smem, r, v, fb, slow, mass,
+                              h_out, hdt, dt, respa, bx, dipoles, transfer, acc, CtaSync(),
+                              forces_only != 0, pf);
     } else if (!forces_only) {
-        free_beads(p, blockIdx.x - p.n_groups, r, v, slow, mass, h_out, dt, respa, bx, acc);
+        free_beads<PAINT>(p, blockIdx.x - p.n_groups, r, v, slow, mass, h_out, dt, respa, bx,
+                          acc, pf);
     }
-    if (out) block_partials_f<kOut, kThreads>(acc, p.partials, gridDim.x);
+    if (out) block_partials_f<kOut, kThreads>(acc, p.partials, G);
+}
+
+// The free beads of a split launch, beside the group kernel (on a second
+// stream): the free-bead blocks of k_respa_warp / k_respa_cta with the same
+// beads per block, without the groups' dynamic shared memory, so that they
+// fill the SMs around the group blocks; partials at slots slot0 + block, as
+// in the single launch.
+template <bool PAINT>
+__global__ void __launch_bounds__(kThreads)
+k_respa_free(hpf_respa_plan p, float* __restrict__ r, float* __restrict__ v, SlowForces slow,
+             float mass, float h_out, float dt, int respa, const double* __restrict__ box,
+             double* out, PaintFuse pf, unsigned int G, unsigned int slot0) {
+    const Box bx = load_box(box);
+    float acc[kOut];
+#pragma unroll
+    for (int k = 0; k < kOut; ++k) acc[k] = 0.0f;
+    free_beads<PAINT>(p, blockIdx.x, r, v, slow, mass, h_out, dt, respa, bx, acc, pf);
+    if (out) block_partials_f<kOut, kThreads>(acc, p.partials, G, slot0 + blockIdx.x);
 }
 
 // ids[k] = inv[ids[k]]: the plan's bead lists follow a permutation of the
@@ -597,6 +644,9 @@ int hpf_respa_plan_destroy(hpf_respa_plan* p) {
                     p->dih_gid,
                     p->free_ids, p->partials};
     for (void* q : ptrs) cudaFree(q);
+    if (p->free_stream) cudaStreamDestroy(p->free_stream);
+    if (p->free_fork) cudaEventDestroy(p->free_fork);
+    if (p->free_join) cudaEventDestroy(p->free_join);
     delete p;
     return HPF_OK;
 }
@@ -804,19 +854,30 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
         }
     }
     const int grid = grid_size(p);
-    if (cudaMalloc(&p->partials, sizeof(double) * kOut * (size_t)std::max(grid, 1)) != cudaSuccess) {
+    if (cudaMalloc(&p->partials, sizeof(double) * kOut * (size_t)std::max(grid, 1)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&p->free_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->free_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p->free_join, cudaEventDisableTiming) != cudaSuccess) {
         hpf_respa_plan_destroy(p);
         return HPF_ERR_CUDA;
     }
     if (p->smem > 48 * 1024) {
-        const void* fn = warp_mode ? (p->has_dih ? (const void*)k_respa_warp<true>
-                                                 : (const void*)k_respa_warp<false>)
-                                   : (p->has_dih ? (const void*)k_respa_cta<true>
-                                                 : (const void*)k_respa_cta<false>);
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem) !=
-            cudaSuccess) {
-            hpf_respa_plan_destroy(p);
-            return HPF_ERR_CUDA;
+        // both variants (with and without the fused paint) of this plan's kernel
+        const void* fns[2] = {
+            warp_mode ? (p->has_dih ? (const void*)k_respa_warp<true, false>
+                                    : (const void*)k_respa_warp<false, false>)
+                      : (p->has_dih ? (const void*)k_respa_cta<true, false>
+                                    : (const void*)k_respa_cta<false, false>),
+            warp_mode ? (p->has_dih ? (const void*)k_respa_warp<true, true>
+                                    : (const void*)k_respa_warp<false, true>)
+                      : (p->has_dih ? (const void*)k_respa_cta<true, true>
+                                    : (const void*)k_respa_cta<false, true>)};
+        for (const void* fn : fns) {
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->smem) != cudaSuccess) {
+                hpf_respa_plan_destroy(p);
+                return HPF_ERR_CUDA;
+            }
         }
     }
     *out = p;
@@ -832,12 +893,16 @@ int hpf_respa_plan_info(const hpf_respa_plan* p, int* n_groups, int* n_free,
     return HPF_OK;
 }
 
-int hpf_respa_step(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
-                   const float* const* slow_forces, int n_slow, double mass, double dt,
-                   int respa_inner, const double* box, float* dipoles, float* transfer,
-                   double* out, hpf_ctx* baro_ctx, const HpfScrArgs* baro,
-                   const double* field_sums, const double* randoms, int* counter, double* state,
-                   int* d_err, void* stream) {
+}  // extern "C"
+
+namespace {
+
+int respa_run(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
+              const float* const* slow_forces, int n_slow, double mass, double dt,
+              int respa_inner, const double* box, float* dipoles, float* transfer, double* out,
+              hpf_ctx* baro_ctx, const HpfScrArgs* baro, const double* field_sums,
+              const double* randoms, int* counter, double* state, int* d_err, void* stream,
+              const PaintFuse* pf) {
     if (!p || !r || !v || !f_bonded || !box || n_slow < 0 || n_slow > kMaxSlow ||
         (n_slow > 0 && !slow_forces) || !(mass > 0) || respa_inner < 1 ||
         (dipoles != nullptr) != (transfer != nullptr))
@@ -867,23 +932,96 @@ int hpf_respa_step(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
     if (grid == 0) return HPF_OK;
     cudaStream_t st = as_stream(stream);
     const float h_out = (float)(0.5 * respa_inner * dt), hdt = (float)(0.5 * dt);
+    PaintFuse pfv;
+    memset(&pfv, 0, sizeof(pfv));
+    if (pf) pfv = *pf;
+    // with the paint fused in, the free beads run as a kernel of their own on
+    // the plan's second stream, beside the group kernel, which is launched
+    // first so that its blocks are placed before the free ones
+    const bool split = pf && p->n_free_blocks > 0;
+    const int ggrid = split ? grid - p->n_free_blocks : grid;
+    const unsigned int G = (unsigned int)grid;
+    if (split) HPF_CUDA_TRY(cudaEventRecord(p->free_fork, st));
+    int rc = HPF_OK;
+    if (ggrid > 0) {
 #define HPF_RESPA(K)                                                                          \
-    K<<<grid, kThreads, p->smem, st>>>(*p, r, v, f_bonded, sf, (float)mass, h_out, hdt,        \
-                                       (float)dt, respa_inner, box, dipoles, transfer, out, 0)
-    if (p->warp_mode) {
-        if (p->has_dih) HPF_RESPA(k_respa_warp<true>);
-        else HPF_RESPA(k_respa_warp<false>);
-    } else {
-        if (p->has_dih) HPF_RESPA(k_respa_cta<true>);
-        else HPF_RESPA(k_respa_cta<false>);
-    }
+    K<<<ggrid, kThreads, p->smem, st>>>(*p, r, v, f_bonded, sf, (float)mass, h_out, hdt,       \
+                                        (float)dt, respa_inner, box, dipoles, transfer, out, 0, \
+                                        pfv, G)
+        if (p->warp_mode) {
+            if (pf) {
+                if (p->has_dih) HPF_RESPA((k_respa_warp<true, true>));
+                else HPF_RESPA((k_respa_warp<false, true>));
+            } else {
+                if (p->has_dih) HPF_RESPA((k_respa_warp<true, false>));
+                else HPF_RESPA((k_respa_warp<false, false>));
+            }
+        } else {
+            if (pf) {
+                if (p->has_dih) HPF_RESPA((k_respa_cta<true, true>));
+                else HPF_RESPA((k_respa_cta<false, true>));
+            } else {
+                if (p->has_dih) HPF_RESPA((k_respa_cta<true, false>));
+                else HPF_RESPA((k_respa_cta<false, false>));
+            }
+        }
 #undef HPF_RESPA
-    HPF_LAUNCH_CHECK();
+        if (cudaGetLastError() != cudaSuccess) rc = HPF_ERR_CUDA;
+    }
+    if (split) {
+        // the join is recorded whatever happens, so that a stream capture is
+        // never left forked
+        cudaError_t e = cudaStreamWaitEvent(p->free_stream, p->free_fork, 0);
+        if (e == cudaSuccess) {
+            k_respa_free<true><<<p->n_free_blocks, kThreads, 0, p->free_stream>>>(
+                *p, r, v, sf, (float)mass, h_out, (float)dt, respa_inner, box, out, pfv, G,
+                (unsigned int)ggrid);
+            e = cudaGetLastError();
+        }
+        HPF_CUDA_TRY(cudaEventRecord(p->free_join, p->free_stream));
+        if (e != cudaSuccess) rc = HPF_ERR_CUDA;
+    }
+    if (split) HPF_CUDA_TRY(cudaStreamWaitEvent(st, p->free_join, 0));
+    if (rc != HPF_OK) return rc;
     if (out) {
-        k_respa_finish<<<1, kFinishThreads, 0, st>>>(p->partials, (unsigned int)grid, out, bf, d_err);
+        k_respa_finish<<<1, kFinishThreads, 0, st>>>(p->partials, G, out, bf, d_err);
         HPF_LAUNCH_CHECK();
     }
     return HPF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hpf_respa_step(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
+                   const float* const* slow_forces, int n_slow, double mass, double dt,
+                   int respa_inner, const double* box, float* dipoles, float* transfer,
+                   double* out, hpf_ctx* baro_ctx, const HpfScrArgs* baro,
+                   const double* field_sums, const double* randoms, int* counter, double* state,
+                   int* d_err, void* stream) {
+    return respa_run(p, r, v, f_bonded, slow_forces, n_slow, mass, dt, respa_inner, box, dipoles,
+                     transfer, out, baro_ctx, baro, field_sums, randoms, counter, state, d_err,
+                     stream, nullptr);
+}
+
+int hpf_respa_step_paint(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
+                         const float* const* slow_forces, int n_slow, double mass, double dt,
+                         int respa_inner, const double* box, float* dipoles, float* transfer,
+                         double* out, hpf_ctx* field_ctx, const int32_t* types,
+                         const float* charges, int* d_err, void* stream) {
+    if (!field_ctx || !types || (p && field_ctx->M <= 0)) return HPF_ERR_ARG;
+    PaintFuse pf;
+    pf.acc = field_ctx->d_acc;
+    pf.bs = field_ctx->d_box;
+    pf.types = types;
+    pf.charges = charges;
+    pf.M = field_ctx->M;
+    pf.T = field_ctx->T;
+    pf.err = d_err ? d_err : field_ctx->d_err;
+    return respa_run(p, r, v, f_bonded, slow_forces, n_slow, mass, dt, respa_inner, box, dipoles,
+                     transfer, out, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, d_err,
+                     stream, &pf);
 }
 
 int hpf_respa_forces(hpf_respa_plan* p, const float* r, float* f_bonded, const double* box,
@@ -896,15 +1034,18 @@ int hpf_respa_forces(hpf_respa_plan* p, const float* r, float* f_bonded, const d
     sf.n = 0;
     // v is neither read nor written in this mode; r is only read
     float* rr = const_cast<float*>(r);
+    PaintFuse none;
+    memset(&none, 0, sizeof(none));
 #define HPF_RESPA_F(K)                                                                       \
     K<<<grid, kThreads, p->smem, st>>>(*p, rr, nullptr, f_bonded, sf, 1.0f, 0.0f, 0.0f, 0.0f, \
-                                       1, box, nullptr, nullptr, out, 1)
+                                       1, box, nullptr, nullptr, out, 1, none,           \
+                                       (unsigned int)grid)
     if (p->warp_mode) {
-        if (p->has_dih) HPF_RESPA_F(k_respa_warp<true>);
-        else HPF_RESPA_F(k_respa_warp<false>);
+        if (p->has_dih) HPF_RESPA_F((k_respa_warp<true, false>));
+        else HPF_RESPA_F((k_respa_warp<false, false>));
     } else {
-        if (p->has_dih) HPF_RESPA_F(k_respa_cta<true>);
-        else HPF_RESPA_F(k_respa_cta<false>);
+        if (p->has_dih) HPF_RESPA_F((k_respa_cta<true, false>));
+        else HPF_RESPA_F((k_respa_cta<false, false>));
     }
 #undef HPF_RESPA_F
     HPF_LAUNCH_CHECK();

@@ -83,15 +83,32 @@ __device__ __forceinline__ void tile_columns(ColInfo* col, const SpecGeom& g, in
 }
 
 // ------------------------------------------------------------ pass A ---
-// Plane layout (passes A and C): row r of the (y, z) plane at r * plane_ls;
-// within a row the z transform's positions p sit at p + p / N2 (one pad
-// after every N2 elements, N2 the transform's second-step length), so that
-// its strided accesses fall in distinct banks; plane_ls = 8 mod 16 (in
-// float2) puts the two rows a 16-lane access touches in complementary banks.
-// Without a second step (h <= 16) each lane owns a row: odd stride.
+// Plane layout (passes A and C): row r of the (y, z) plane at
+// r * plane_ls + r / N2y, N2y the y transform's second-step length (one
+// slot of skew per block of N2y rows, so that the y transforms' accesses
+// that run from column h of one row block into column 0 of the next land
+// in consecutive banks).  Two layouts share a row, one after the other:
+//   - between the two steps of the z transform, position p at p + p / N2
+//     (one pad after every N2 elements, N2 the z transform's second-step
+//     length), so that the stride-N2 accesses of its second step fall in
+//     distinct banks;
+//   - around the y transform, column (kz) c at c: a 16-lane access to 16
+//     consecutive columns, or to their mirror columns h - c, is then
+//     conflict-free.
+// The z transform's second step changes one into the other in place (its
+// items per row lie in one warp: a warp barrier between loads and stores).
+// plane_ls = 8 mod 16 (in float2) puts the two rows a 16-lane access of the
+// z transform touches in complementary banks.  Without a second step
+// (h <= 16) each lane owns a row: odd stride.
 __host__ __device__ constexpr int plane_n2(int h) { return h / split1(h); }
 __host__ __device__ constexpr int plane_ls(int h) {
     return plane_n2(h) > 1 ? ((h + h / plane_n2(h) + 1 + 7) / 16) * 16 + 8 : ((h + 1) | 1);
+}
+// start of row r of a plane of ny rows
+template <int NY, int HZ>
+__device__ __forceinline__ int plane_row(int r) {
+    constexpr int N2y = NY / split1(NY);
+    return r * plane_ls(HZ) + (N2y > 1 ? r / N2y : 0);
 }
 
 // One block per (grid, x) plane.  z: int64 accumulators (read and cleared)
@@ -109,8 +126,8 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     constexpr int zoff = Tw<2 * H>::off, step = Tw<2 * H>::stride;
     const int x = blockIdx.x, t = blockIdx.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    using fz = Idx<H>;
     auto zs = [](int e) { return PN > 1 ? e + e / PN : e; };
+    auto row0 = [](int r) { return plane_row<NY, HZ>(r); };
     const float s = sc.s[t] * bs->inv_dV * kFixInv;
     ulonglong2* a =
         reinterpret_cast<ulonglong2*>(acc + (int64_t)t * g.M + (int64_t)x * Ny * (2 * H));
@@ -123,12 +140,17 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             a[r * H + m] = make_ulonglong2(0ull, 0ull);
             return make_float2(fix_to_float((long long)v.x) * s, fix_to_float((long long)v.y) * s);
         };
-        auto st = [&](int r, int p, float2 v) { sm[r * Ls + zs(p)] = v; };
-        auto fin = [&](int r, int k, int p, float2 v) { sm[r * Ls + zs(p)] = v; };
+        auto st = [&](int r, int p, float2 v) { sm[row0(r) + zs(p)] = v; };
+        // (no second step: positions are frequencies, in natural order)
+        auto fin = [&](int r, int k, int p, float2 v) { sm[row0(r) + zs(p)] = v; };
         fft_step1<H, false, false>(Ny, inv_rows, ld, st, fin, tw);
         __syncthreads();
-        auto ld2 = [&](int r, int p) { return sm[r * Ls + zs(p)]; };
-        fft_step2<H, false, false>(Ny, inv_rows, ld2, fin);
+        // second step: frequency k to column k
+        static_assert(PN == 1 || ((Ny * split1(H)) % 32 == 0 && 32 % split1(H) == 0),
+                      "the z transform's second-step items of a row lie in one warp");
+        auto ld2 = [&](int r, int p) { return sm[row0(r) + zs(p)]; };
+        auto fin2 = [&](int r, int k, int p, float2 v) { sm[row0(r) + k] = v; };
+        fft_step2<H, false, false, decltype(ld2), decltype(fin2), true>(Ny, inv_rows, ld2, fin2);
     }
     __syncthreads();
     // y, step 1 with the even/odd split: X[k] = E + w^k O, X[h-k] = conj(E -
@@ -137,7 +159,6 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     // lanes 0-15 take 16 columns q, lanes 16-31 their partners h - q (h for
     // q = 0), one row offset n2 per warp task, a warp barrier between the
     // loads and the stores.  X[k] goes where Z[k] was, X[h] to slot h.
-    auto colslot = [&](int c) { return zs(c == H ? H : fz::pos(c)); };
     {
         constexpr int N1 = split1(Ny), N2 = Ny / N1;
         constexpr int pairs = H / 2 + 1, groups = (pairs + 15) / 16;
@@ -147,12 +168,12 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             const bool active = q < pairs && !(side && q == H / 2);
             const int c = !active ? 0 : (side ? (q == 0 ? H : H - q) : q);
             const int kk = c == H ? 0 : c;
-            const int pk = zs(fz::pos(kk)), pp = kk == 0 ? pk : zs(fz::pos(H - kk));
+            const int pk = kk, pp = kk == 0 ? pk : H - kk;
             const float2 w = __ldg(tw + zoff + kk * step);
             float2 v[N1];
 #pragma unroll
             for (int i = 0; i < N1; ++i) {
-                const float2* row = sm + (N2 * i + n2) * Ls;
+                const float2* row = sm + row0(N2 * i + n2);
                 const float2 zk = row[pk], zp = row[pp];
                 const float2 E = make_float2(0.5f * (zk.x + zp.x), 0.5f * (zk.y - zp.y));
                 const float2 O = make_float2(0.5f * (zk.y + zp.y), -0.5f * (zk.x - zp.x));
@@ -167,22 +188,21 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             }
             __syncwarp();
             if (active) {
-                const int sc_ = c == H ? zs(H) : pk;
 #pragma unroll
-                for (int k1 = 0; k1 < N1; ++k1) sm[(N2 * k1 + n2) * Ls + sc_] = v[k1];
+                for (int k1 = 0; k1 < N1; ++k1) sm[row0(N2 * k1 + n2) + c] = v[k1];
             }
             __syncwarp();
         }
         __syncthreads();
         if (N2 > 1) {
             // y, step 2: the spectrum plane, row ky = k1 + N1 k2
-            auto ld2 = [&](int cc, int p) { return sm[p * Ls + colslot(cc)]; };
+            auto ld2 = [&](int cc, int p) { return sm[row0(p) + cc]; };
             auto fin2 = [&](int cc, int ky, int p, float2 v2) { out[ky * Nzc + cc] = v2; };
             fft_step2<Ny, false, true>(Nzc, inv_cols, ld2, fin2);
         } else {
             // whole y transform in step 1: rows in natural order
             for (int ky = warp; ky < Ny; ky += kSpecWarps)
-                for (int cc = lane; cc < Nzc; cc += 32) out[ky * Nzc + cc] = sm[ky * Ls + colslot(cc)];
+                for (int cc = lane; cc < Nzc; cc += 32) out[ky * Nzc + cc] = sm[row0(ky) + cc];
         }
     }
 }
@@ -454,6 +474,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     using fy = Idx<Ny>;
     auto zs = [](int e) { return PN > 1 ? e + e / PN : e; };
+    auto row0 = [](int r) { return plane_row<NY, HZ>(r); };
     int src, mul;  // mul: 0 none, 1 -i g_y, 2 -i g_z
     if (pic) {
         src = gi == 1 ? 0 : 1;
@@ -482,11 +503,11 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                 a[i] = make_float2(gd * a[i].y, -gd * a[i].x);
             }
         };
-        auto st = [&](int c, int p, float2 v) { sm[p * Ls + c] = v; };
-        auto fin = [&](int c, int k, int p, float2 v) { sm[p * Ls + c] = v; };
+        auto st = [&](int c, int p, float2 v) { sm[row0(p) + c] = v; };
+        auto fin = [&](int c, int k, int p, float2 v) { sm[row0(p) + c] = v; };
         fft_step1<Ny, true, true>(Nzc, inv_cols, ld, st, fin, tw, pre);
         __syncthreads();
-        auto ld2 = [&](int c, int p) { return sm[p * Ls + c]; };
+        auto ld2 = [&](int c, int p) { return sm[row0(p) + c]; };
         fft_step2<Ny, true, true>(Nzc, inv_cols, ld2, fin);
     }
     __syncthreads();
@@ -496,7 +517,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
         for (int r0 = warp * RPW; r0 < Ny; r0 += kSpecWarps * RPW) {
             const int r = r0 + lane / N2, n2 = lane % N2;
             const bool active = lane < RPW * N2 && r < Ny;
-            float2* row = sm + (active ? r : 0) * Ls;
+            float2* row = sm + row0(active ? r : 0);
             float2 a[N1];
 #pragma unroll
             for (int i = 0; i < N1; ++i) {
@@ -526,11 +547,11 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
         __syncthreads();
         auto fin = [&](int r, int m, int p, float2 v) { out[fy::freq(r) * H + m] = v; };
         if (N2 > 1) {
-            auto ld2 = [&](int r, int p) { return sm[r * Ls + zs(p)]; };
+            auto ld2 = [&](int r, int p) { return sm[row0(r) + zs(p)]; };
             fft_step2<H, true, false>(Ny, inv_rows, ld2, fin);
         } else {
             for (int r = warp; r < Ny; r += kSpecWarps)
-                for (int m = lane; m < H; m += 32) fin(r, m, m, sm[r * Ls + m]);
+                for (int m = lane; m < H; m += 32) fin(r, m, m, sm[row0(r) + m]);
         }
     }
 }
@@ -578,7 +599,8 @@ SpecGeom spec_geom(const hpf_ctx* c) {
 }
 
 size_t plane_smem(const hpf_ctx* c) {
-    return sizeof(float2) * (size_t)c->n1 * plane_ls(c->n2 / 2);
+    // rows, then the skew of the last row block (at most split1(n1) - 1 slots)
+    return sizeof(float2) * ((size_t)c->n1 * plane_ls(c->n2 / 2) + split1(c->n1));
 }
 
 // The plane kernels are instantiated per (n1, n2 / 2): n1 and n2 in

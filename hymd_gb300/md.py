@@ -122,9 +122,9 @@ class RespaMD:
         if self.plan is not None:
             # fused inner kernel + its one-block finish (sums, barostat); the
             # second kick is fused into the readout
-            self.launches_per_step = 2 + field
+            self._launches = 2 + field
         else:
-            self.launches_per_step = 1 + self.respa * (1 + kinds) + 1 + field
+            self._launches = 1 + self.respa * (1 + kinds) + 1 + field
 
     def _make_plan(self, packed, max_block_beads):
         (b2a, b2b, b2r, b2k, b3a, b3b, b3c, b3t, b3k,
@@ -501,9 +501,9 @@ class RespaMD:
             # CSVR: sums (with the fused second kick) + scale; the barostat runs
             # in the rRESPA finish kernel and the paint (semi-isotropic: a
             # position kernel of its own)
-            self.launches_per_step += (1 if thermostat else 0) + self.baro_mode
+            self._launches += (1 if thermostat else 0) + self.baro_mode
         else:
-            self.launches_per_step += (1 if thermostat else 0) + (2 if barostat else 0)
+            self._launches += (1 if thermostat else 0) + (2 if barostat else 0)
         # (the CSVR sums ride in the readout; its scaling is one more launch)
 
     def _thermostat(self, st, kick=False):
@@ -658,14 +658,42 @@ class RespaMD:
     # charged systems: the density and charge chains of the field step run
     # on two streams (hpf_field_pic_step) rather than one after the other
     CONCURRENT_PIC = True
+    # the fused rRESPA kernel deposits every bead on the mesh where it leaves
+    # its final position (hpf_respa_step_paint), and the field step skips its
+    # paints; not with a barostat, whose rescaling of the positions comes
+    # after the inner loop
+    FUSE_PAINT = True
 
-    def _field(self, st, sums=None, pos_scale=None, kick=None):
+    @property
+    def launches_per_step(self):
+        """Kernels of this library per outer step (cuFFT's own kernels and
+        memsets not counted).  With the paint fused into the rRESPA kernel the
+        field step's paints (densities, charges) are gone and the free beads
+        run as a kernel of their own beside the groups."""
+        n = self._launches
+        if self._paint_fused:
+            n -= 1 + (1 if self.charges is not None else 0)
+            if self._free_ids is not None and self._free_ids.numel():
+                n += 1
+        return n
+
+    @property
+    def _paint_fused(self):
+        return (self.FUSE_PAINT and self.plan is not None and self.pm.spectral == "fused"
+                and self.baro_args is None
+                and (self.charges is None or self.CONCURRENT_PIC))
+
+    def _field(self, st, sums=None, pos_scale=None, kick=None, painted=False):
         scale = None if pos_scale is None else _lib.ctypes.c_void_p(pos_scale)
-        if self.charges is not None and self.CONCURRENT_PIC:
+        if (self.charges is not None and self.CONCURRENT_PIC) or painted:
+            charged = self.charges is not None
             _lib.call("hpf_field_pic_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.types),
                       self.n, self.masses, _lib.ptr(self.f_field), _lib.ptr(sums), scale,
-                      _lib.ptr(self.charges), _lib.ptr(self.charged), self.charged.numel(),
-                      float(self.elec_factor), _lib.ptr(self.f_elec), None, kick, st)
+                      _lib.ptr(self.charges) if charged else None,
+                      _lib.ptr(self.charged) if charged else None,
+                      self.charged.numel() if charged else 0,
+                      float(self.elec_factor) if charged else 0.0,
+                      _lib.ptr(self.f_elec) if charged else None, None, kick, int(painted), st)
             return
         last_kick = kick if self.charges is None else None
         _lib.call("hpf_field_step", self.pm._h, _lib.ptr(self.r), _lib.ptr(self.types), self.n,
@@ -738,6 +766,13 @@ class RespaMD:
         fs = self._slow_forces()
         arr = (_lib.P * len(fs))(*[_lib.ptr(f) for f in fs])
         baro = self.baro_args is not None
+        if self._paint_fused:
+            _lib.call("hpf_respa_step_paint", self.plan, _lib.ptr(self.r), _lib.ptr(self.v),
+                      _lib.ptr(self.f_b), arr, len(fs), self.mass, self.dt, self.respa,
+                      _lib.ptr(self.box), _lib.ptr(self.dipoles), _lib.ptr(self.transfer),
+                      _lib.ptr(self.bonded_out), self.pm._h, _lib.ptr(self.types),
+                      _lib.ptr(self.charges), _lib.ptr(self.err), st)
+            return
         _lib.call("hpf_respa_step", self.plan, _lib.ptr(self.r), _lib.ptr(self.v),
                   _lib.ptr(self.f_b), arr, len(fs), self.mass, self.dt, self.respa,
                   _lib.ptr(self.box), _lib.ptr(self.dipoles), _lib.ptr(self.transfer),
@@ -791,7 +826,7 @@ class RespaMD:
             # the bias needs the new field forces before the second kick:
             # field step without the fused kick, the bias on the host, then
             # the kick with every slow force (and the CSVR in the same pass)
-            self._field(st, self.field_sums, pos_scale=scale)
+            self._field(st, self.field_sums, pos_scale=scale, painted=self._paint_fused)
             self._bias_forces()
             st = _lib.stream_ptr()
             if thermo:
@@ -799,7 +834,8 @@ class RespaMD:
             else:
                 self._outer_kick(st)
             return
-        self._field(st, self.field_sums, pos_scale=scale, kick=self._kick_args(thermo))
+        self._field(st, self.field_sums, pos_scale=scale, kick=self._kick_args(thermo),
+                    painted=fused and self._paint_fused)
         if thermo:
             _lib.call("hpf_csvr_scale", _lib.ptr(self.v), _lib.ptr(self.group), self.n,
                       _lib.ptr(self.state), int(self.thermo_args.remove_com), st)

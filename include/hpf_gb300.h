@@ -340,15 +340,21 @@ int hpf_pic_step_list(hpf_ctx* ctx, const float* pos, const float* charges, cons
  * reference's update_field + compute_field_force and update_field_force_q
  * of one step (main.py:606-660) -- with the charge chain (paint, transforms,
  * Poisson map) run on a second stream of the context beside the density
- * chain, joined before the charge readout, which carries the kick.  On the
- * fused spectral path only; otherwise the two calls run one after the other.
- * The first call allocates the charge chain's scratch (about 3 Mc complex
- * and 4 M real values) and must not be under stream capture (HPF_ERR_ARG). */
+ * chain, joined before the charge readout, which carries the kick.  With
+ * charges NULL (count 0) only the density chain runs and its readout
+ * carries the kick, as hpf_field_step.  painted nonzero: this step's
+ * deposits (densities, and charges when given) are already in the
+ * context's accumulators, made by hpf_respa_step_paint, and the paints are
+ * skipped (not with pos_scale).  On the fused spectral path only (painted
+ * or the second stream); otherwise the two calls run one after the other.
+ * The first call with charges allocates the charge chain's scratch (about
+ * 3 Mc complex and 4 M real values) and must not be under stream capture
+ * (HPF_ERR_ARG). */
 int hpf_field_pic_step(hpf_ctx* ctx, float* pos, const int32_t* types, int64_t n,
                        const double* type_mass, float* force, double* sums,
                        const double* pos_scale, const float* charges, const int32_t* idx,
                        int64_t count, double elec_factor, float* elec_forces, double* pic_sums,
-                       const HpfKick* kick, void* stream);
+                       const HpfKick* kick, int painted, void* stream);
 
 /* ---- bonded (f2py calling form, hymd/force.py:8-23, main.py:509-550) ------
  * All three zero their force array first, as the Fortran does.  Indices are
@@ -495,6 +501,23 @@ int hpf_respa_step(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
                    double* out, hpf_ctx* baro_ctx, const HpfScrArgs* baro,
                    const double* field_sums, const double* randoms, int* counter, double* state,
                    int* d_err, void* stream);
+/* hpf_respa_step (no barostat) with the paint of the next field step
+ * fused in: every bead is deposited on field_ctx's accumulators where the
+ * kernel leaves its final position -- a free bead right after its drift,
+ * while the molecule groups still integrate; a group bead at the group's
+ * write-back -- into its type's density grid and, when charges is non-NULL,
+ * into the charge grid, the deposits of hpf_paint / hpf_pic_step
+ * (int64 fixed point, so the accumulators are bit-identical to a separate
+ * paint).  The field step then runs with painted = 1 (hpf_field_pic_step).
+ * No counterpart in the reference, where update_field paints after the
+ * inner loop (main.py:606-616).  types int32[n] and charges float[n] are
+ * device arrays of the plan's beads; d_err receives a non-finite position
+ * or a type outside [0, T). */
+int hpf_respa_step_paint(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
+                         const float* const* slow_forces, int n_slow, double mass, double dt,
+                         int respa_inner, const double* box, float* dipoles, float* transfer,
+                         double* out, hpf_ctx* field_ctx, const int32_t* types,
+                         const float* charges, int* d_err, void* stream);
 
 /* Bonded forces (bonds, angles, dihedrals with CBT) of the plan's topology at
  * positions r, without any integration: f_bonded of every bead in a bonded

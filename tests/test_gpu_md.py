@@ -268,7 +268,8 @@ def test_md_with_charges_compact_pic_matches_full_pic():
     b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
     from hymd_gb300 import _lib
 
-    def full_field(st, sums=None, pos_scale=None, kick=None):
+    def full_field(st, sums=None, pos_scale=None, kick=None, painted=False):
+        assert not painted
         _lib.call("hpf_field_step", b.pm._h, _lib.ptr(b.r), _lib.ptr(b.types), b.n, b.masses,
                   _lib.ptr(b.f_field), _lib.ptr(sums),
                   None if pos_scale is None else _lib.ctypes.c_void_p(pos_scale), None, st)
@@ -276,6 +277,7 @@ def test_md_with_charges_compact_pic_matches_full_pic():
                   float(b.elec_factor), _lib.ptr(b.f_elec), None, None, None, None, None, kick,
                   st)
     b._field = full_field
+    b.FUSE_PAINT = False  # the full PIC step paints every bead itself
     for m in (a, b):
         m.couple(thermostat=True, seed=3, n_steps=20)
         m.prime()
@@ -396,5 +398,47 @@ def test_concurrent_charge_chain_matches_sequential(barostat):
     for name in ("r", "v", "f_field", "f_elec"):
         assert torch.equal(getattr(a, name), getattr(b, name)), name
     assert torch.equal(a.box, b.box)
+    a.check_errors()
+    b.check_errors()
+
+
+@pytest.mark.parametrize("kind", ["peptide_cta", "peptide_warp", "melt"])
+def test_paint_fused_into_respa_matches_separate_paint(kind):
+    """hpf_respa_step_paint (each bead deposited on the mesh by the rRESPA
+    kernel where it leaves its final position) followed by the field step
+    with painted = 1, against the separate paint: the int64 fixed-point
+    accumulators are order-independent, so after captured NVT (CSVR) steps
+    positions, velocities and field forces are bit-identical -- for chains in
+    CTA groups and in warp groups, with and without the charge grid."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    if kind == "melt":
+        s = systems.homopolymer_melt(seed=12, n_chains=300, length=10, box=6.0, mesh=24)
+        kw = dict(topology=s["topology"])
+    else:
+        n_res = 40 if kind == "peptide_cta" else 10
+        s = systems.charged_peptides(seed=13, n_chains=12, n_res=n_res, n_total=5000, box=7.5,
+                                     mesh=32)
+        kw = dict(topology=s["topology"], charges=s["charges"])
+    cfg = s["config"]
+    ham = get_hamiltonian(cfg)
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    b.FUSE_PAINT = False
+    assert a.plan is not None and a.pm.spectral == "fused"
+    for m in (a, b):
+        m.couple(thermostat=True, seed=10, n_steps=20)
+        m.prime()
+    assert a._paint_fused and not b._paint_fused
+    a.step()
+    b.step()
+    for m in (a, b):
+        m.capture()
+        m.run(4)
+    torch.cuda.synchronize()
+    names = ["r", "v", "f_field"] + (["f_elec"] if kind != "melt" else [])
+    for name in names:
+        assert torch.equal(getattr(a, name), getattr(b, name)), name
     a.check_errors()
     b.check_errors()
