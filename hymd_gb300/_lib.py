@@ -118,6 +118,7 @@ _SIGNATURES.update({
     "hpf_scr_scale_positions": [P, I64, P, I, P],
     "hpf_respa_forces": [P, P, P, P, P, P, P],
     "hpf_field_force_vjp": [P, P, P, I64, ctypes.POINTER(D), P, P, P, P],
+    "hpf_dihedral_hvp": [P, P, P, I64, P, P, P, P, P, P, P, P, I64, P, P],
     "hpf_bonded_hvp": [P, P, P, I64, P, P, P, P, P, I64, P, P, P, P, P, I64, P, P],
     "hpf_gpe_step": [P, P, P, P, I64, P, ctypes.POINTER(D), ctypes.POINTER(D), D, D, D, I, I,
                      P, P, P, P, P, P, P, P, P, ctypes.POINTER(I), P],

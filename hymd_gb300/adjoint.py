@@ -24,8 +24,12 @@ is symmetric with G_ij = G_ji = S_ij / (2 rho0) and a zero diagonal: moving
 one pair's chi by d (both entries) changes W by S_ij d / rho0.
 
 dW/dx is the exact derivative of the discrete energy; the MD force (the
-spectral readout of -grad V) equals -dW/dx up to the O(h^2) difference
-between the two gradients.
+spectral readout of -grad V) equals -dW/dx only up to the difference
+between the two discretisations of the gradient, which vanishes as the mesh
+is refined (gradient_gap measures it).  field_energy(...,
+reference_gradient=True) returns minus the MD force as the positions'
+gradient instead, so that a loss differentiated through W follows the
+reference's own forces.
 """
 import numpy as np
 import torch
@@ -72,7 +76,7 @@ def _energy(pm, pos, typ, masses, Q, b, c):
 
 class _FieldEnergy(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, positions, chi, kappa, sigma, pm, types, masses, kind, rho0, a):
+    def forward(ctx, positions, chi, kappa, sigma, pm, types, masses, kind, rho0, a, ref_grad):
         k, s = float(kappa), float(sigma)
         Q, b, c = functional_coefficients(kind, chi.detach().cpu().numpy(), k, rho0, a)
         _set(pm, Q, b, c, s)
@@ -80,6 +84,7 @@ class _FieldEnergy(torch.autograd.Function):
         ctx.pm, ctx.types, ctx.masses, ctx.kind = pm, types, masses, kind
         ctx.rho0, ctx.a, ctx.kappa, ctx.sigma = rho0, a, k, s
         ctx.Q, ctx.b, ctx.c = Q, b, c
+        ctx.ref_grad = bool(ref_grad)
         ctx.chi_meta = (chi.dtype, chi.device)
         ctx.save_for_backward(positions)
         return torch.tensor(W, dtype=torch.float64, device=positions.device)
@@ -95,11 +100,19 @@ class _FieldEnergy(torch.autograd.Function):
         P = T * (T + 1) // 2
         sums = torch.zeros(P + 1 + T, dtype=torch.float64, device=positions.device) if need_p \
             else None
-        _lib.call("hpf_field_adjoint", pm._h, _lib.ptr(positions), _lib.ptr(ctx.types),
-                  positions.shape[0], _lib.dvec(ctx.masses), _lib.ptr(grad_x), _lib.ptr(sums),
-                  _lib.stream_ptr())
-        g = float(gW.item())
-        out = [None] * 10
+        if need_x and ctx.ref_grad:
+            # minus the MD force (the readout of the spectral gradient)
+            _lib.call("hpf_field_step", pm._h, _lib.ptr(positions), _lib.ptr(ctx.types),
+                      positions.shape[0], _lib.dvec(ctx.masses), _lib.ptr(grad_x), None, None,
+                      None, _lib.stream_ptr())
+            grad_x.neg_()
+        if (need_x and not ctx.ref_grad) or need_p:
+            _lib.call("hpf_field_adjoint", pm._h, _lib.ptr(positions), _lib.ptr(ctx.types),
+                      positions.shape[0], _lib.dvec(ctx.masses),
+                      _lib.ptr(grad_x) if (need_x and not ctx.ref_grad) else None,
+                      _lib.ptr(sums), _lib.stream_ptr())
+        g = float(gW.detach().item())
+        out = [None] * 11
         if need_x:
             out[0] = grad_x * g
         if need_p:
@@ -132,11 +145,13 @@ class _FieldEnergy(torch.autograd.Function):
 
 
 def field_energy(positions, types, pm, masses, chi, kappa, sigma, rho0, a,
-                 kind="DefaultWithChi"):
+                 kind="DefaultWithChi", reference_gradient=False):
     """W (FP64 torch scalar) of the current positions with the quadratic
     functional `kind` at (chi, kappa, sigma); differentiable with respect to
     positions (float32 CUDA (N,3)), chi ((T,T) tensor), kappa and sigma
-    (0-d float64 tensors or floats)."""
+    (0-d float64 tensors or floats).  reference_gradient: the positions'
+    gradient is minus the MD force (hymd/field.py:152-200) instead of the
+    exact dW/dx."""
     pos = _lib.require_cuda(positions, "positions", torch.float32)
     typ = types if types.dtype == torch.int32 else types.to(torch.int32)
     _lib.require_cuda(typ, "types", torch.int32, (pos.shape[0],))
@@ -150,4 +165,24 @@ def field_energy(positions, types, pm, masses, chi, kappa, sigma, rho0, a,
     if not isinstance(sigma, torch.Tensor):
         sigma = torch.tensor(float(sigma), dtype=torch.float64)
     m = [float(x) for x in masses] if masses is not None else [1.0] * T
-    return _FieldEnergy.apply(pos, chi, kappa, sigma, pm, typ, m, kind, float(rho0), float(a))
+    return _FieldEnergy.apply(pos, chi, kappa, sigma, pm, typ, m, kind, float(rho0), float(a),
+                              bool(reference_gradient))
+
+
+def gradient_gap(positions, types, pm, masses, chi, kappa, sigma, rho0, a,
+                 kind="DefaultWithChi"):
+    """Relative RMS difference between the MD field force F (hymd/field.py:
+    152-200: the CIC readout of the spectral gradient of v_ext) and minus the
+    exact derivative dW/dx of the discrete field energy, ||F + dW/dx|| /
+    ||F||, at the given positions."""
+    pos = _lib.require_cuda(positions, "positions", torch.float32).detach().clone()
+    pos.requires_grad_(True)
+    W = field_energy(pos, types, pm, masses, chi, kappa, sigma, rho0, a, kind)
+    (g,) = torch.autograd.grad(W, pos)
+    typ = types if types.dtype == torch.int32 else types.to(torch.int32)
+    F = torch.empty_like(pos)
+    m = [float(x) for x in masses] if masses is not None else [1.0] * pm.n_types
+    _lib.call("hpf_field_step", pm._h, _lib.ptr(pos.detach()), _lib.ptr(typ), pos.shape[0],
+              _lib.dvec(m), _lib.ptr(F), None, None, None, _lib.stream_ptr())
+    d = (F.double() + g.double())
+    return float(torch.sqrt((d ** 2).mean()) / torch.sqrt((F.double() ** 2).mean()))

@@ -212,9 +212,51 @@ __global__ void k_angles_hvp(float* __restrict__ out, const float* __restrict__ 
     }
 }
 
+__global__ void k_dihedrals_hvp(float* __restrict__ out, const float* __restrict__ r,
+                                const float* __restrict__ lam, int64_t n,
+                                const double* __restrict__ box, const int32_t* __restrict__ a,
+                                const int32_t* __restrict__ b, const int32_t* __restrict__ c,
+                                const int32_t* __restrict__ d, const float* __restrict__ coeff,
+                                const int32_t* __restrict__ dtype,
+                                const int32_t* __restrict__ last, int64_t nd, int* err) {
+    const Box bx = load_box(box);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nd;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int idx[4] = {a[t], b[t], c[t], d[t]};
+        if (!in_range(idx[0], n) || !in_range(idx[1], n) || !in_range(idx[2], n) ||
+            !in_range(idx[3], n)) {
+            hpf_flag(err, HPF_ERR_INDEX);
+            continue;
+        }
+        float trig[30];
+        dih_phase_trig(coeff + 30 * t, trig);
+        V3 dF[4];
+        dihedral_force_tangent(load3(r, idx[0]), load3(r, idx[1]), load3(r, idx[2]),
+                               load3(r, idx[3]), load3(lam, idx[0]), load3(lam, idx[1]),
+                               load3(lam, idx[2]), load3(lam, idx[3]), coeff + 30 * t, trig,
+                               dtype[t], last[t], bx, dF);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) add3(out, idx[q], dF[q]);
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int hpf_dihedral_hvp(float* out, const float* r, const float* lam, int64_t n, const double* box,
+                     const int32_t* a, const int32_t* b, const int32_t* c, const int32_t* d,
+                     const float* coeff, const int32_t* dtype, const int32_t* last, int64_t nd,
+                     int* d_err, void* stream) {
+    if (!out || !r || !lam || !box || n < 0 || nd < 0 ||
+        (nd > 0 && (!a || !b || !c || !d || !coeff || !dtype || !last)))
+        return HPF_ERR_ARG;
+    if (nd == 0) return HPF_OK;
+    k_dihedrals_hvp<<<grid_for(nd), kThreads, 0, as_stream(stream)>>>(
+        out, r, lam, n, box, a, b, c, d, coeff, dtype, last, nd, d_err);
+    HPF_LAUNCH_CHECK();
+    return HPF_OK;
+}
 
 int hpf_bonds(float* f, const float* r, int64_t n, const double* box, const int32_t* a,
               const int32_t* b, const float* r0, const float* k, int64_t nb, double* out,

@@ -9,10 +9,20 @@ kernels in libhpf_gb300.so:
     k-space -> c2r -> readout), backward hpf_field_force_vjp: the
     vector-Jacobian product with respect to the positions and the
     functional's matrix Q (hence chi);
-  * bonded force F_b(x) (bonds and angles, hymd/compute_bond_forces.f90,
-    compute_angle_forces.f90) -- forward the fused plan's deterministic
-    gather (hpf_respa_forces), backward hpf_bonded_hvp (minus the Hessian of
-    the bonded energy times the cotangent, by forward-mode dual arithmetic).
+  * bonded force F_b(x) (bonds, angles and four-body terms,
+    hymd/compute_bond_forces.f90, compute_angle_forces.f90,
+    compute_dihedral_forces.f90 with the CBT bending of
+    dipole_reconstruction.f90) -- forward the fused plan's deterministic
+    gather (hpf_respa_forces), backward hpf_bonded_hvp + hpf_dihedral_hvp
+    (minus the Hessian of the bonded energy times the cotangent, by
+    forward-mode dual arithmetic: the forces are minus the gradient of the
+    energy, so the Jacobian is symmetric).  The one exception is the CBT
+    bending force where the reference clamps sin(gamma) at 0.1
+    (dipole_reconstruction.f90): there its force is not the gradient of its
+    energy, and the product is that of the energy's Hessian;
+  * the CSVR thermostat (hymd/thermostat.py:111-219) at the end of the outer
+    step, when the RespaMD is coupled, with the random numbers of its table
+    (row = step index), as torch operations.
 
 A K-step loss is differentiated by torch autograd with the trajectory cut
 into segments of ~sqrt(K) steps under torch.utils.checkpoint, so that only
@@ -21,8 +31,8 @@ backward pass.  The loss provided is the mean squared deviation of the
 time-averaged per-type density profile along z (linear binning, so that it
 is differentiable in the positions) from a target profile.
 
-Scope: NVE (no thermostat or barostat in the differentiated step), bonds and
-angles (dihedral Hessian-vector products are not implemented).
+Scope: NVE or NVT (CSVR); no barostat in the differentiated step; no
+electrostatics (the PIC charge force is not differentiated).
 """
 import math
 
@@ -44,8 +54,10 @@ class ForceModel:
             raise ValueError("the bonded forward needs the fused plan (RespaMD(fused=True))")
         if md.perm is not None:
             raise ValueError("reverse mode works in the caller's bead order (no sort_particles)")
-        if md.topo is not None and md.topo.n_dihedrals:
-            raise NotImplementedError("no Hessian-vector product for dihedrals")
+        if md.charges is not None:
+            raise NotImplementedError("electrostatics (PIC) are not differentiated")
+        if md.baro_args is not None:
+            raise NotImplementedError("no barostat in the differentiated step")
         cfg = md.config
         self.md = md
         self.pm = md.pm
@@ -58,6 +70,12 @@ class ForceModel:
         self.box = md.box
         self.box_f = md.box.float()
         self._key = None
+        # CSVR of a coupled RespaMD: its arguments and random table (host)
+        self.thermo = md.thermo_args
+        self.randoms = md.randoms.cpu().numpy() if self.thermo is not None else None
+        self.group_masks = None
+        if self.thermo is not None and md.group is not None:
+            self.group_masks = [md.group == g for g in range(self.thermo.n_groups)]
 
     def set_chi(self, chi):
         Q, b, c = functional_coefficients(self.kind, chi.detach().cpu().numpy(), self.kappa,
@@ -126,11 +144,18 @@ class _BondedForce(torch.autograd.Function):
         md = ctx.model.md
         t = md.topo
         out = torch.empty_like(x)
-        _lib.call("hpf_bonded_hvp", _lib.ptr(out), _lib.ptr(x), _lib.ptr(lam.contiguous()), md.n,
+        lam = lam.contiguous()
+        _lib.call("hpf_bonded_hvp", _lib.ptr(out), _lib.ptr(x), _lib.ptr(lam), md.n,
                   _lib.ptr(ctx.model.box), _lib.ptr(t.bond_a), _lib.ptr(t.bond_b),
                   _lib.ptr(t.bond_r0), _lib.ptr(t.bond_k), t.n_bonds, _lib.ptr(t.ang_a),
                   _lib.ptr(t.ang_b), _lib.ptr(t.ang_c), _lib.ptr(t.ang_t0), _lib.ptr(t.ang_k),
                   t.n_angles, _lib.ptr(md.err), _lib.stream_ptr())
+        if t.n_dihedrals:
+            _lib.call("hpf_dihedral_hvp", _lib.ptr(out), _lib.ptr(x), _lib.ptr(lam), md.n,
+                      _lib.ptr(ctx.model.box), _lib.ptr(t.dih_a), _lib.ptr(t.dih_b),
+                      _lib.ptr(t.dih_c), _lib.ptr(t.dih_d), _lib.ptr(t.dih_coeff),
+                      _lib.ptr(t.dih_type), _lib.ptr(t.dih_last), t.n_dihedrals,
+                      _lib.ptr(md.err), _lib.stream_ptr())
         return out, None
 
 
@@ -144,10 +169,45 @@ def bonded_force(x, model):
     return _BondedForce.apply(x, model)
 
 
-def respa_step(x, v, f_field, f_bond, chi, model):
-    """One outer rRESPA step (hymd/main.py:802-887, 1143-1169), NVE, in torch
+def csvr(v, model, step):
+    """The CSVR thermostat of outer step `step` (hymd/thermostat.py:167-219)
+    as torch operations: per coupling group, in order, the kinetic energy
+    (about the group's COM velocity with COM removal), the reference's
+    alpha^2 from the group's (R, chi^2) draws of table row `step`, and the
+    rescaling (of the group about its COM, or of every bead)."""
+    a = model.thermo
+    if (step + 1) % a.every:
+        return v
+    row = model.randoms[step * a.stride:(step + 1) * a.stride]
+    m, c = model.md.mass, a.c
+    for g in range(a.n_groups):
+        sel = None if model.group_masks is None else model.group_masks[g]
+        n_g = int(a.count[g])
+        use_com = bool(a.remove_com) and n_g > 1
+        if use_com:
+            vg = v if sel is None else v[sel]
+            com = vg.sum(0) / n_g
+            K = 0.5 * m * ((vg - com) ** 2).sum()
+        else:
+            K = 0.5 * m * (v ** 2).sum()
+        k_target = 1.5 * a.gas_constant * n_g * a.target_temperature
+        nf = 3 * n_g
+        R, S = float(row[a.offset + 2 * g]), float(row[a.offset + 2 * g + 1])
+        q = k_target / (nf * K)
+        alpha = torch.sqrt(c + (1.0 - c) * (S + R * R) * q + 2.0 * R * torch.sqrt(c * (1.0 - c) * q))
+        if use_com:
+            scaled = (v - com) * alpha + com
+            v = scaled if sel is None else torch.where(sel[:, None], scaled, v)
+        else:
+            v = v * alpha
+    return v
+
+
+def respa_step(x, v, f_field, f_bond, chi, model, step=None):
+    """One outer rRESPA step (hymd/main.py:802-887, 1143-1169) in torch
     operations: outer half kick, respa_inner x (half kick, drift, wrap,
-    bonded forces, half kick), field forces, outer half kick."""
+    bonded forces, half kick), field forces, outer half kick, and the CSVR
+    thermostat of outer step `step` when the RespaMD is coupled."""
     md = model.md
     m, dt, n_in = md.mass, md.dt, md.respa
     dto = n_in * dt
@@ -159,6 +219,8 @@ def respa_step(x, v, f_field, f_bond, chi, model):
         v = v + (0.5 * dt / m) * f_bond
     f_field = field_force(x, chi, model)
     v = v + (0.5 * dto / m) * f_field
+    if model.thermo is not None and step is not None:
+        v = csvr(v, model, step)
     return x, v, f_field, f_bond
 
 
@@ -179,10 +241,11 @@ def z_profile(x, types, n_types, n_bins, box):
     return flat.reshape(n_types, n_bins) / vol
 
 
-def profile_loss(x0, v0, chi, model, n_steps, target, n_bins=100, segment=None):
+def profile_loss(x0, v0, chi, model, n_steps, target, n_bins=100, segment=None, step0=0):
     """MSE between the z-density profile averaged over n_steps outer steps
     and `target` (n_types, n_bins), differentiable in x0, v0 and chi; the
-    trajectory is checkpointed every `segment` steps (default ceil(sqrt(K)))."""
+    trajectory is checkpointed every `segment` steps (default ceil(sqrt(K))).
+    step0: outer step index of the first step (the thermostat's table row)."""
     md = model.md
     seg = segment or max(1, int(math.ceil(math.sqrt(n_steps))))
     box = [float(b) for b in model.box.cpu()]
@@ -191,10 +254,10 @@ def profile_loss(x0, v0, chi, model, n_steps, target, n_bins=100, segment=None):
     f_field = field_force(x, chi, model)
     f_bond = bonded_force(x, model)
 
-    def run(k, x, v, f_field, f_bond, chi):
+    def run(k, s0, x, v, f_field, f_bond, chi):
         acc = torch.zeros((model.T, n_bins), dtype=x.dtype, device=x.device)
-        for _ in range(k):
-            x, v, f_field, f_bond = respa_step(x, v, f_field, f_bond, chi, model)
+        for i in range(k):
+            x, v, f_field, f_bond = respa_step(x, v, f_field, f_bond, chi, model, s0 + i)
             acc = acc + z_profile(x, types, model.T, n_bins, box)
         return x, v, f_field, f_bond, acc
 
@@ -202,8 +265,8 @@ def profile_loss(x0, v0, chi, model, n_steps, target, n_bins=100, segment=None):
     done = 0
     while done < n_steps:
         k = min(seg, n_steps - done)
-        x, v, f_field, f_bond, acc = checkpoint(run, k, x, v, f_field, f_bond, chi,
-                                                use_reentrant=False)
+        x, v, f_field, f_bond, acc = checkpoint(run, k, step0 + done, x, v, f_field, f_bond,
+                                                chi, use_reentrant=False)
         total = total + acc
         done += k
     prof = total / n_steps

@@ -230,6 +230,19 @@ int hpf_bonded_hvp(float* out, const float* r, const float* lam, int64_t n, cons
                    const int32_t* ba, const int32_t* bb, const float* br0, const float* bk,
                    int64_t nb, const int32_t* aa, const int32_t* ab, const int32_t* ac,
                    const float* at0, const float* ak, int64_t na, int* d_err, void* stream);
+/* Directional derivative of the four-body forces (compute_dihedral_forces.f90:
+ * 61-134 with the CBT bending of dipole_reconstruction.f90:50-106; no
+ * dipoles) along lam, ADDED to out (float[n][3]): minus the Hessian of the
+ * dihedral energy times lam, the four-body part of the vector-Jacobian
+ * product of reverse mode (hpf_bonded_hvp gives the bonds and angles and
+ * zeroes out first).  Forward-mode dual arithmetic over the same expressions
+ * as the force kernel; coeff float[nd][6][5], dtype / last int32[nd] as for
+ * hpf_dihedrals.  No counterpart in the reference, which has no
+ * derivatives of the forces. */
+int hpf_dihedral_hvp(float* out, const float* r, const float* lam, int64_t n, const double* box,
+                     const int32_t* a, const int32_t* b, const int32_t* c, const int32_t* d,
+                     const float* coeff, const int32_t* dtype, const int32_t* last, int64_t nd,
+                     int* d_err, void* stream);
 
 /* ---- PIC_Spectral_GPE electrostatics ------------------------------------
  * update_field_force_q_GPE (hymd/field.py:764-1112) and the energy of

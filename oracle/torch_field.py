@@ -8,6 +8,9 @@ on the full |k|^2):
   field force   hymd/field.py:152-200, 428-616 (update_field, compute_field_force)
   bond force    hymd/compute_bond_forces.f90:45-61
   angle force   hymd/compute_angle_forces.f90:58-92
+  four-body     hymd/compute_dihedral_forces.f90:61-134 (cosine series of
+                rows 0/1 and 2/3, type 2 improper) with the CBT bending
+                energy of hymd/dipole_reconstruction.f90:50-106
 The forces are minus the autograd gradient of the energies for the bonded
 terms, and the explicit spectral-gradient readout for the field.
 """
@@ -89,9 +92,53 @@ def _min_image(r, box):
     return r - L * torch.round(r / L)
 
 
-def bonded_energy(x, box, bonds=None, angles=None):
-    """E of harmonic bonds (a, b, r0, k) and angles (a, b, c, t0, k)."""
+def _series(c_row, d_row, phi):
+    """sum_n c_n (1 + cos(n phi - d_n)), n = 0..4 (dipole_reconstruction.f90:37-48)."""
+    n = torch.arange(5, dtype=phi.dtype, device=phi.device)
+    return (c_row * (1.0 + torch.cos(n * phi[:, None] - d_row))).sum(1)
+
+
+def dihedral_energy(x, box, dihedrals):
+    """E of the four-body terms (a, b, c, d, coeff (D, 6, 5), type, last):
+    type 0 the cosine series of rows 0/1 (+ rows 2/3 where both are
+    non-zero), type 1 that plus the CBT bending 1/2 K(phi) (gamma -
+    gamma_0(phi))^2 of the angle at b (and at c for the chain's last term),
+    K the series of rows 4/5 and gamma_0 = 1.85 - 0.227 cos(phi - 0.785),
+    type 2 the improper 1/2 k (phi - phi_0)^2 (row 0: phi_0, k)."""
+    a, b, c, d, coeff, dtype, last = dihedrals
+    f = _min_image(x[a] - x[b], box)
+    g = _min_image(x[b] - x[c], box)
+    h = _min_image(x[d] - x[c], box)
+    v = torch.cross(f, g, dim=1)
+    w = torch.cross(h, g, dim=1)
+    gn = torch.linalg.norm(g, dim=1)
+    phi = torch.atan2((w * f).sum(1) * gn, (v * w).sum(1))
+    cf = coeff.to(x.dtype)
+    e = _series(cf[:, 0], cf[:, 1], phi)
+    second = (cf[:, 2] != 0).any(1) & (cf[:, 3] != 0).any(1)
+    e = e + torch.where(second, _series(cf[:, 2], cf[:, 3], phi), torch.zeros_like(phi))
+    E = (e * ((dtype == 0) | (dtype == 1)).to(x.dtype)).sum()
+    K = _series(cf[:, 4], cf[:, 5], phi)
+    # 0.785 as the single-precision literal of the Fortran
+    gamma_0 = 1.85 - 0.227 * torch.cos(phi - float(np.float32(0.785)))
+
+    def bend(rab, rcb):
+        cg = (rab * rcb).sum(1) / (torch.linalg.norm(rab, dim=1) * torch.linalg.norm(rcb, dim=1))
+        return 0.5 * K * (torch.acos(cg) - gamma_0) ** 2
+
+    cbt = (dtype == 1).to(x.dtype)
+    E = E + (bend(f, -g) * cbt).sum() + (bend(g, h) * cbt * (last == 1).to(x.dtype)).sum()
+    imp = (dtype == 2).to(x.dtype)
+    E = E + (0.5 * cf[:, 0, 1] * (phi - cf[:, 0, 0]) ** 2 * imp).sum()
+    return E
+
+
+def bonded_energy(x, box, bonds=None, angles=None, dihedrals=None):
+    """E of harmonic bonds (a, b, r0, k), angles (a, b, c, t0, k) and the
+    four-body terms (dihedral_energy)."""
     E = x.new_zeros(())
+    if dihedrals is not None and len(dihedrals[0]):
+        E = E + dihedral_energy(x, box, dihedrals)
     if bonds is not None and len(bonds[0]):
         a, b, r0, k = bonds
         r = _min_image(x[b] - x[a], box)
@@ -108,9 +155,9 @@ def bonded_energy(x, box, bonds=None, angles=None):
     return E
 
 
-def bonded_force(x, box, bonds=None, angles=None, create_graph=True):
+def bonded_force(x, box, bonds=None, angles=None, create_graph=True, dihedrals=None):
     if not x.requires_grad:
         x = x.detach().requires_grad_(True)
-    E = bonded_energy(x, box, bonds, angles)
+    E = bonded_energy(x, box, bonds, angles, dihedrals)
     (g,) = torch.autograd.grad(E, x, create_graph=create_graph)
     return -g
