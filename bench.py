@@ -682,6 +682,12 @@ def run_gpu(args):
     na = topo.n_angles if topo else 0
     nd = topo.n_dihedrals if topo else 0
     respa_bytes = cfg.respa_inner * (72 * n + 16 * nb + 20 * na + 144 * nd)
+    nq = int(md.charged.numel()) if md.charged is not None else 0
+    fused_paint = md._paint_fused
+    if fused_paint:
+        # the launch also paints every bead (and the charged ones): the
+        # paint's contract bytes, 16 N + 4 T M (+ 16 N_q + 4 M)
+        respa_bytes += 16 * n + 4 * T * M + ((16 * nq + 4 * M) if nq else 0)
     respa_gbs = respa_bytes / (respa_ms * 1e-3) / 1e9
     traffic = _traffic(args.workload)
     # the other kernels of the step, timed stage by stage (graphs + events,
@@ -695,7 +701,6 @@ def run_gpu(args):
     # grids; the k-space work reads T spectra and writes 3T; the readout
     # reads r + type and 3T grids once and writes F; the charge path of the
     # charged beads N_q is 44 N_q + 16 M + 32 Mc
-    nq = int(md.charged.numel()) if md.charged is not None else 0
     stage_bytes = {"paint": 16 * n + 4 * T * M, "kspace": 32 * T * Mc,
                    "spectral_fused": 32 * T * Mc,
                    "readout_kick": 28 * n + 12 * T * M,
@@ -707,6 +712,9 @@ def run_gpu(args):
         gbs = b_ / (bd[k] * 1e-6) / 1e9
         kernels[k] = {"algorithmic_bytes": b_, "us": bd[k], "achieved": gbs, "frac": gbs / peak,
                       "traffic": traffic.get(k)}
+    if fused_paint and "paint" in kernels:
+        kernels["paint"]["note"] = ("timed standalone (k_paint); in the step the deposits are "
+                                    "made by the rRESPA launch")
 
     ns_day = sps * cfg.respa_inner * cfg.time_step * 86400 / 1000.0
     # CPU baseline (rank 0, N=1 only): bounded oracle sample
@@ -730,6 +738,11 @@ def run_gpu(args):
                 "ns_per_day": ns_day * ws,
                 "config": _config_block(cfg, n, args.workload),
                 "gpu_setup": {"bead_order": "sorted by mesh cell at setup",
+                              "paint": ("fused into the rRESPA launch (free beads in a "
+                                        "kernel of their own beside the molecule groups)"
+                                        if fused_paint else "separate launch"),
+                              "charge_chain": ("second stream beside the density chain"
+                                               if md.charges is not None else None),
                               "respa_groups": md.plan_info(),
                               "respa_group_tuning_us": md.block_timings,
                               "kspace_tile": md.pm.spectral_tile,
@@ -748,7 +761,9 @@ def run_gpu(args):
                              "peak_kind": peak_kind, "ms_per_launch": respa_ms,
                              "algorithmic_bytes": respa_bytes,
                              "bytes_basis": "respa_inner x (72 N + 16 B + 20 A + 144 D), "
-                                            "the unfused inner step's reads and writes",
+                                            "the unfused inner step's reads and writes"
+                                            + (", + the fused paint's 16 N + 4 T M (+ 16 N_q "
+                                               "+ 4 M for the charges)" if fused_paint else ""),
                              "note": "latency-bound in practice: the loop runs on chip and "
                                      "touches DRAM once per bead per launch (traffic)"},
                 "roofline_kernels": kernels,
