@@ -300,9 +300,9 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                 const int64_t c30 = 30 * (int64_t)(d0 + t);
                 dihedral_term(p0, p1, p2, p3, p.dih_coeff + c30, p.dih_trig + c30, tl.x, tl.y,
                               (last_it && dipoles) ? 1 : 0, bx, F, e, dip, tmx);
-                const int sl = nbd + 2 * na + 4 * t;
+                const int sl = nbd + 2 * na + t;
 #pragma unroll
-                for (int j = 0; j < 4; ++j) put3(s.slot, sl + j, F[j]);
+                for (int j = 0; j < 4; ++j) put3(s.slot, sl + j * nd, F[j]);
                 if (last_it) acc[8] += e;
             } else if (task < cd + ca) {
                 const int t = ((task - cd) << 5) + l32;
@@ -320,8 +320,8 @@ __device__ __forceinline__ void run_group(const hpf_respa_plan& p, int grp, int 
                     e = 0.0f;
                     vir = ga;
                 }
-                put3(s.slot, nbd + 2 * t, ga);
-                put3(s.slot, nbd + 2 * t + 1, gc);
+                put3(s.slot, nbd + t, ga);
+                put3(s.slot, nbd + na + t, gc);
                 if (last_it) {
                     acc[4] += e;
                     acc[5] += vir.x;
@@ -764,7 +764,10 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
         dih_gid[k] = (int)t;
     }
     // incidence lists: per bead the (slot, sign) entries of the terms that
-    // touch it; slots per group: bonds, then 2 per angle, then 4 per dihedral
+    // touch it; slots per group: bonds, then the angles' first and second
+    // gradients, then the dihedrals' four corners, each corner-major (slot j
+    // of term k at j * count + k), so that a warp's 32 terms write 32
+    // consecutive slots; the entries per bead keep the terms' order
     std::vector<std::vector<int>> inc(grp_bead[G]);
     int mx_slots = 0, mx_bonds = 0, mx_angles = 0, mx_beads = 0, mx_inc = 0;
     for (int g = 0; g < G; ++g) {
@@ -777,17 +780,17 @@ int hpf_respa_plan_create(hpf_respa_plan** out, int64_t n, int64_t nb, const int
         }
         for (int k = 0; k < na_g; ++k) {
             const int2 q = ang_ijk[sa[g] + k];
-            const int s0 = nbd_g + 2 * k;
+            const int s0 = nbd_g + k, s1 = nbd_g + na_g + k;
             inc[base + (q.x & 0xffff)].push_back((s0 << 1) | 1);
             inc[base + (q.x >> 16)].push_back(s0 << 1);
-            inc[base + (q.x >> 16)].push_back((s0 + 1) << 1);
-            inc[base + q.y].push_back(((s0 + 1) << 1) | 1);
+            inc[base + (q.x >> 16)].push_back(s1 << 1);
+            inc[base + q.y].push_back((s1 << 1) | 1);
         }
         for (int k = 0; k < nd_g; ++k) {
             const short4 q = dih_ijkl[sd[g] + k];
-            const int s0 = nbd_g + 2 * na_g + 4 * k;
+            const int s0 = nbd_g + 2 * na_g + k;
             const int li[4] = {q.x, q.y, q.z, q.w};
-            for (int j = 0; j < 4; ++j) inc[base + li[j]].push_back((s0 + j) << 1);
+            for (int j = 0; j < 4; ++j) inc[base + li[j]].push_back((s0 + j * nd_g) << 1);
         }
         int ng = 0;
         for (int i = grp_bead[g]; i < grp_bead[g + 1]; ++i) ng += (int)inc[i].size();
