@@ -21,6 +21,7 @@ box).  N > 1 (torchrun): independent replicas, one per GPU; value = sum over
 ranks.
 """
 import argparse
+import copy
 import json
 import os
 import statistics
@@ -382,7 +383,9 @@ def accuracy(md, sys_, ham, torch):
     from oracle import field as of
     from oracle import hamiltonian as oh
     of.FFT_WORKERS = os.cpu_count() or 1
-    cfg = sys_["config"]
+    # the state's own box (a barostat has moved it away from the config's)
+    cfg = copy.copy(sys_["config"])
+    cfg.box_size = md.box.cpu().numpy().astype(np.float64)
     T = cfg.n_types
     R, V, Ty = md.r, md.v, md.types
     pm, fl, ecl, cl = gf.initialize_pm(None, cfg)
