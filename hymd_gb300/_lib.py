@@ -74,7 +74,7 @@ _SIGNATURES = {
     "hpf_respa_step": [P, P, P, P, ctypes.POINTER(P), I, D, D, I, P, P, P, P, P, P, P, P, P,
                        P, P, P],
     "hpf_respa_step_paint": [P, P, P, P, ctypes.POINTER(P), I, D, D, I, P, P, P, P, P, P, P,
-                             P, P],
+                             P, P, P, P, P, P, P],
     "hpf_sum_dot": [P, P, I64, P, P],
     "hpf_sum_v2": [P, I64, P, P],
 }

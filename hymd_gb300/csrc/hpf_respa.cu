@@ -1012,7 +1012,12 @@ int hpf_respa_step_paint(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
                          const float* const* slow_forces, int n_slow, double mass, double dt,
                          int respa_inner, const double* box, float* dipoles, float* transfer,
                          double* out, hpf_ctx* field_ctx, const int32_t* types,
-                         const float* charges, int* d_err, void* stream) {
+                         const float* charges, const HpfScrArgs* baro, const double* field_sums,
+                         const double* randoms, int* counter, double* state, int* d_err,
+                         void* stream) {
+    // a semi-isotropic barostat moves the box under unscaled positions: its
+    // grid coordinates change after the deposits, so it is refused
+    if (baro && baro->mode != 0) return HPF_ERR_ARG;
     if (!field_ctx || !types || (p && field_ctx->M <= 0)) return HPF_ERR_ARG;
     PaintFuse pf;
     pf.acc = field_ctx->d_acc;
@@ -1023,8 +1028,8 @@ int hpf_respa_step_paint(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
     pf.T = field_ctx->T;
     pf.err = d_err ? d_err : field_ctx->d_err;
     return respa_run(p, r, v, f_bonded, slow_forces, n_slow, mass, dt, respa_inner, box, dipoles,
-                     transfer, out, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, d_err,
-                     stream, &pf);
+                     transfer, out, baro ? field_ctx : nullptr, baro, field_sums, randoms, counter,
+                     state, d_err, stream, &pf);
 }
 
 int hpf_respa_forces(hpf_respa_plan* p, const float* r, float* f_bonded, const double* box,

@@ -660,8 +660,11 @@ class RespaMD:
     CONCURRENT_PIC = True
     # the fused rRESPA kernel deposits every bead on the mesh where it leaves
     # its final position (hpf_respa_step_paint), and the field step skips its
-    # paints; not with a barostat, whose rescaling of the positions comes
-    # after the inner loop
+    # paints; with the isotropic barostat the deposits of the unscaled
+    # positions in the old box are those of the scaled ones in the new box
+    # (up to rounding), and the positions are scaled after the inner loop;
+    # not with the semi-isotropic one, whose position update leaves most
+    # beads unscaled while the box changes
     FUSE_PAINT = True
 
     @property
@@ -675,12 +678,14 @@ class RespaMD:
             n -= 1 + (1 if self.charges is not None else 0)
             if self._free_ids is not None and self._free_ids.numel():
                 n += 1
+            if self.baro_args is not None:
+                n += 1  # the isotropic position scaling after the fused paint
         return n
 
     @property
     def _paint_fused(self):
         return (self.FUSE_PAINT and self.plan is not None and self.pm.spectral == "fused"
-                and self.baro_args is None
+                and (self.baro_args is None or self.baro_mode == 0)
                 and (self.charges is None or self.CONCURRENT_PIC))
 
     def _field(self, st, sums=None, pos_scale=None, kick=None, painted=False):
@@ -771,7 +776,12 @@ class RespaMD:
                       _lib.ptr(self.f_b), arr, len(fs), self.mass, self.dt, self.respa,
                       _lib.ptr(self.box), _lib.ptr(self.dipoles), _lib.ptr(self.transfer),
                       _lib.ptr(self.bonded_out), self.pm._h, _lib.ptr(self.types),
-                      _lib.ptr(self.charges), _lib.ptr(self.err), st)
+                      _lib.ptr(self.charges),
+                      _lib.ctypes.byref(self.baro_args) if baro else None,
+                      _lib.ptr(self.field_sums) if baro else None,
+                      _lib.ptr(self.randoms) if baro else None,
+                      _lib.ptr(self.counter) if baro else None,
+                      _lib.ptr(self.state) if baro else None, _lib.ptr(self.err), st)
             return
         _lib.call("hpf_respa_step", self.plan, _lib.ptr(self.r), _lib.ptr(self.v),
                   _lib.ptr(self.f_b), arr, len(fs), self.mass, self.dt, self.respa,
@@ -815,18 +825,20 @@ class RespaMD:
         the second outer half kick (and the CSVR sums) fused into the last
         readout, then the thermostat's scaling."""
         scale = None
+        painted = fused and self._paint_fused
         if fused and self.baro_args is not None:
-            if self.baro_mode == 0:
+            if self.baro_mode == 0 and not painted:
                 scale = self.state.data_ptr() + 12 * 8  # alpha, applied in the paint
             else:
+                # semi-isotropic (mode 1), or isotropic after a fused paint
                 _lib.call("hpf_scr_scale_positions", _lib.ptr(self.r), self.n,
-                          _lib.ptr(self.state), 1, st)
+                          _lib.ptr(self.state), self.baro_mode, st)
         thermo = self.thermo_args is not None
         if self.bias is not None:
             # the bias needs the new field forces before the second kick:
             # field step without the fused kick, the bias on the host, then
             # the kick with every slow force (and the CSVR in the same pass)
-            self._field(st, self.field_sums, pos_scale=scale, painted=self._paint_fused)
+            self._field(st, self.field_sums, pos_scale=scale, painted=painted)
             self._bias_forces()
             st = _lib.stream_ptr()
             if thermo:
@@ -835,7 +847,7 @@ class RespaMD:
                 self._outer_kick(st)
             return
         self._field(st, self.field_sums, pos_scale=scale, kick=self._kick_args(thermo),
-                    painted=fused and self._paint_fused)
+                    painted=painted)
         if thermo:
             _lib.call("hpf_csvr_scale", _lib.ptr(self.v), _lib.ptr(self.group), self.n,
                       _lib.ptr(self.state), int(self.thermo_args.remove_com), st)

@@ -514,23 +514,32 @@ int hpf_respa_step(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
                    double* out, hpf_ctx* baro_ctx, const HpfScrArgs* baro,
                    const double* field_sums, const double* randoms, int* counter, double* state,
                    int* d_err, void* stream);
-/* hpf_respa_step (no barostat) with the paint of the next field step
- * fused in: every bead is deposited on field_ctx's accumulators where the
- * kernel leaves its final position -- a free bead right after its drift,
- * while the molecule groups still integrate; a group bead at the group's
- * write-back -- into its type's density grid and, when charges is non-NULL,
- * into the charge grid, the deposits of hpf_paint / hpf_pic_step
- * (int64 fixed point, so the accumulators are bit-identical to a separate
+/* hpf_respa_step with the paint of the next field step fused in: every
+ * bead is deposited on field_ctx's accumulators where the kernel leaves its
+ * final position -- a free bead right after its drift, while the molecule
+ * groups still integrate; a group bead at the group's write-back -- into
+ * its type's density grid and, when charges is non-NULL, into the charge
+ * grid, the deposits of hpf_paint / hpf_pic_step (int64 fixed point, so
+ * without a barostat the accumulators are bit-identical to a separate
  * paint).  The field step then runs with painted = 1 (hpf_field_pic_step).
- * No counterpart in the reference, where update_field paints after the
- * inner loop (main.py:606-616).  types int32[n] and charges float[n] are
- * device arrays of the plan's beads; d_err receives a non-finite position
- * or a type outside [0, T). */
+ * baro (NULL: none) must be isotropic (mode 0; HPF_ERR_ARG otherwise): the
+ * beads are deposited unscaled into the old box, which gives the grid
+ * coordinates of the scaled positions in the new box (r n / L is unchanged
+ * by r -> alpha r, L -> alpha L; equal up to FP32 rounding), and the caller
+ * scales the positions afterwards (hpf_scr_scale_positions mode 0) and
+ * runs the field step without pos_scale.  field_sums, randoms, counter and
+ * state as for hpf_respa_step's barostat.  No counterpart in the
+ * reference, where update_field paints after the inner loop and the
+ * barostat (main.py:606-616, 889-963).  types int32[n] and charges float[n]
+ * are device arrays of the plan's beads; d_err receives a non-finite
+ * position or a type outside [0, T). */
 int hpf_respa_step_paint(hpf_respa_plan* plan, float* r, float* v, float* f_bonded,
                          const float* const* slow_forces, int n_slow, double mass, double dt,
                          int respa_inner, const double* box, float* dipoles, float* transfer,
                          double* out, hpf_ctx* field_ctx, const int32_t* types,
-                         const float* charges, int* d_err, void* stream);
+                         const float* charges, const HpfScrArgs* baro, const double* field_sums,
+                         const double* randoms, int* counter, double* state, int* d_err,
+                         void* stream);
 
 /* Bonded forces (bonds, angles, dihedrals with CBT) of the plan's topology at
  * positions r, without any integration: f_bonded of every bead in a bonded

@@ -388,6 +388,9 @@ def test_concurrent_charge_chain_matches_sequential(barostat):
     a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
     b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
     b.CONCURRENT_PIC = False
+    # the paint stays separate on both (with the barostat a fused paint
+    # agrees with it to rounding only; tested below)
+    a.FUSE_PAINT = b.FUSE_PAINT = False
     assert a.pm.spectral == "fused"
     for m in (a, b):
         m.couple(thermostat=True, barostat=barostat, seed=9, n_steps=20)
@@ -442,3 +445,58 @@ def test_paint_fused_into_respa_matches_separate_paint(kind):
         assert torch.equal(getattr(a, name), getattr(b, name)), name
     a.check_errors()
     b.check_errors()
+
+
+def test_paint_fused_with_isotropic_barostat_matches_separate_paint():
+    """With the isotropic SCR barostat the fused paint deposits the unscaled
+    positions into the old box (grid coordinates r n / L unchanged by
+    r -> alpha r, L -> alpha L) and the positions are scaled afterwards;
+    against the separate paint of the scaled positions the deposits differ
+    only by FP32 rounding of the coordinates, so after captured NPT (CSVR +
+    SCR) steps positions, velocities, forces and box agree to that level."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.lipid_membrane(seed=9, n_lipids=60, n_water=900, box=5.6, mesh=24)
+    cfg = s["config"]
+    cfg.tau_p, cfg.n_b = 1.0, 1
+    ham = get_hamiltonian(cfg)
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    b.FUSE_PAINT = False
+    for m in (a, b):
+        m.couple(thermostat=True, barostat="isotropic", seed=12, n_steps=20)
+        m.prime()
+    assert a._paint_fused and not b._paint_fused
+    for m in (a, b):
+        m.capture()
+        m.run(5)
+    torch.cuda.synchronize()
+    assert rel_rms(a.r.cpu().numpy(), b.r.cpu().numpy()) < 1e-6
+    assert rel_rms(a.v.cpu().numpy(), b.v.cpu().numpy()) < 1e-5
+    assert rel_rms(a.f_field.cpu().numpy(), b.f_field.cpu().numpy()) < 1e-5
+    assert np.allclose(a.box_now(), b.box_now(), rtol=1e-7)
+    assert not np.allclose(a.box_now(), np.asarray(cfg.box()), rtol=1e-9)  # the box moved
+    a.check_errors()
+    b.check_errors()
+
+
+def test_fused_paint_refuses_semiisotropic_barostat():
+    """The semi-isotropic position update leaves most beads unscaled while
+    the box changes, so the paint is not fused (the MD loop keeps the
+    separate paint) and the C entry point refuses the combination."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.lipid_membrane(seed=9, n_lipids=60, n_water=900, box=5.6, mesh=24)
+    cfg = s["config"]
+    cfg.tau_p, cfg.n_b = 1.0, 1
+    md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, get_hamiltonian(cfg),
+                 topology=s["topology"])
+    md.couple(thermostat=True, barostat="semiisotropic", seed=3, n_steps=5,
+              target_pressure=(1.0, 1.0))
+    assert not md._paint_fused
+    md.prime()
+    md.step()
+    torch.cuda.synchronize()
+    md.check_errors()
