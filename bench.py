@@ -678,6 +678,27 @@ def run_gpu(args):
     # accuracy of the state the timed region left (before any diagnostic runs)
     acc = accuracy(md, s, ham, torch) if rank == 0 and not args.no_accuracy else None
 
+    # ---- the same K steps after 1000 more: the bead order of the setup sort
+    # decays as the beads move (no re-sort, RespaMD.resort_every = 0)
+    aged = None
+    if not args.no_aging:
+        md.run(1000)
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            a0, b0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(st)
+            md.replay()
+            b0.record(st)
+            b0.synchronize()
+            tot += a0.elapsed_time(b0)
+        md.check_errors()
+        aged = {"steps_before": args.warmup + args.steps + 1000,
+                "value": 1000.0 * args.steps / tot * ws, "unit": "steps/s",
+                "ms_per_step": tot / args.steps,
+                "note": "the timed protocol of `value` after 1000 further steps, no re-sort"}
+
     # ---- end to end, host wall clock --------------------------------------
     e2e_sps, e2e_h2d, e2e_d2h = e2e_wall(md, flush, torch, args.steps)
     dropin = None
@@ -773,6 +794,7 @@ def run_gpu(args):
                         "transfer": "RespaMD.run_host (r, v in; r out; page-locked host "
                                     "memory), host wall clock around the call + synchronize"},
                 "e2e_dropin": dropin,
+                "after_1000_steps": aged,
                 "accuracy": acc,
                 "gpu_launches": md.launches_per_step * args.steps,
                 "roofline": {"kernel": f"{respa_kernel} (fused rRESPA inner loop, "
@@ -1172,6 +1194,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64-oracle accuracy check of the timed state")
+    ap.add_argument("--no-aging", action="store_true",
+                    help="skip the second timing after 1000 further steps")
     ap.add_argument("--no-dropin", action="store_true",
                     help="skip the drop-in-API end-to-end measurement")
     ap.add_argument("--breakdown", action="store_true",
