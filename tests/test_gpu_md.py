@@ -500,3 +500,81 @@ def test_fused_paint_refuses_semiisotropic_barostat():
     md.step()
     torch.cuda.synchronize()
     md.check_errors()
+
+
+def test_charge_chain_with_no_charged_beads():
+    """Charges given but all zero: the charge chain runs on an empty list of
+    charged beads (no deposits, a zero field), and the step equals the one
+    without charges."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.charged_peptides(seed=14, n_chains=8, n_res=10, n_total=3000, box=6.0, mesh=24)
+    cfg = s["config"]
+    ham = get_hamiltonian(cfg)
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"],
+                charges=np.zeros(len(s["types"]), np.float32))
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    assert a.charged.numel() == 0
+    for m in (a, b):
+        m.couple(thermostat=True, seed=2, n_steps=10)
+        m.prime()
+        m.capture()
+        m.run(3)
+    torch.cuda.synchronize()
+    assert torch.count_nonzero(a.f_elec) == 0
+    assert torch.equal(a.r, b.r) and torch.equal(a.v, b.v)
+    a.check_errors()
+
+
+def test_fused_paint_without_free_beads():
+    """A melt where every bead is bonded: no free-bead kernel to fork, the
+    deposits all come from the molecule groups; same trajectory as the
+    separate paint."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.homopolymer_melt(seed=15, n_chains=200, length=10, box=5.5, mesh=24)
+    cfg = s["config"]
+    ham = get_hamiltonian(cfg)
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    b.FUSE_PAINT = False
+    assert a._free_ids.numel() == 0 and a._paint_fused
+    for m in (a, b):
+        m.prime()
+        m.capture()
+        m.run(4)
+    torch.cuda.synchronize()
+    assert torch.equal(a.r, b.r) and torch.equal(a.v, b.v)
+    assert torch.equal(a.f_field, b.f_field)
+    a.check_errors()
+
+
+def test_resort_with_fused_paint_and_barostat():
+    """Re-sorting a captured NPT system whose paint is fused into the rRESPA
+    launch: the trajectory in the caller's order follows the run without
+    re-sorts to rounding (the barostat's sums run in another order)."""
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    s = systems.lipid_membrane(seed=10, n_lipids=60, n_water=900, box=5.6, mesh=24)
+    cfg = s["config"]
+    cfg.tau_p, cfg.n_b = 1.0, 1
+    ham = get_hamiltonian(cfg)
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    b = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"])
+    for m in (a, b):
+        m.couple(thermostat=True, barostat="isotropic", seed=6, n_steps=20)
+        m.prime()
+        m.capture()
+    assert a._paint_fused
+    a.resort_every = 2
+    a.run(6)
+    b.run(6)
+    torch.cuda.synchronize()
+    assert a.resorts == 3
+    assert rel_rms(a.in_input_order(a.r).cpu().numpy(), b.r.cpu().numpy()) < 1e-6
+    assert rel_rms(a.in_input_order(a.v).cpu().numpy(), b.v.cpu().numpy()) < 1e-4
+    assert np.allclose(a.box_now(), b.box_now(), rtol=1e-6)
+    a.check_errors()
