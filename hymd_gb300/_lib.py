@@ -117,6 +117,7 @@ _SIGNATURES.update({
     "hpf_field_adjoint": [P, P, P, I64, ctypes.POINTER(D), P, P, P],
     "hpf_scr_scale_positions": [P, I64, P, I, P],
     "hpf_respa_forces": [P, P, P, P, P, P, P],
+    "hpf_pic_force_vjp": [P, P, P, I64, D, P, P, P],
     "hpf_field_force_vjp": [P, P, P, I64, ctypes.POINTER(D), P, P, P, P],
     "hpf_dihedral_hvp": [P, P, P, I64, P, P, P, P, P, P, P, P, I64, P, P],
     "hpf_bonded_hvp": [P, P, P, I64, P, P, P, P, P, I64, P, P, P, P, P, I64, P, P],

@@ -547,7 +547,7 @@ __global__ void k_readout_grad(const float* __restrict__ vg, const float* __rest
                                const int32_t* __restrict__ types, int64_t n, int T, int64_t M,
                                const BoxState* __restrict__ bs, TypeScale sc,
                                float* __restrict__ grad, int* err, int accumulate = 0,
-                               int per_volume = 0) {
+                               int per_volume = 0, const float* __restrict__ charges = nullptr) {
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
@@ -555,7 +555,7 @@ __global__ void k_readout_grad(const float* __restrict__ vg, const float* __rest
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-        const int t = types[i];
+        const int t = types ? types[i] : 0;
         float gr[3] = {0.0f, 0.0f, 0.0f};
         const bool ok = isfinite(x) && isfinite(y) && isfinite(z) && t >= 0 && t < T;
         if (!ok) hpf_flag(err, (t >= 0 && t < T) ? HPF_ERR_NONFINITE : HPF_ERR_INDEX);
@@ -584,7 +584,9 @@ __global__ void k_readout_grad(const float* __restrict__ vg, const float* __rest
                         gr[2] = fmaf(wx[a] * wy[b] * dz[c], v, gr[2]);
                     }
                 }
-            const float m = per_volume ? sc.s[t] * bs->inv_dV : sc.s[t];
+            // charges: the bead's charge in place of its type's scale
+            const float w0 = charges ? charges[i] : sc.s[t];
+            const float m = per_volume ? w0 * bs->inv_dV : w0;
             gr[0] *= m;
             gr[1] *= m;
             gr[2] *= m;
@@ -1936,7 +1938,8 @@ namespace {
 __global__ void k_vjp_local(const float* __restrict__ E, const float* __restrict__ pos,
                             const int32_t* __restrict__ types, const float* __restrict__ lam,
                             int64_t n, int T, int64_t M, const BoxState* __restrict__ bs,
-                            float* __restrict__ grad, int* err) {
+                            float* __restrict__ grad, int* err,
+                            const float* __restrict__ charges = nullptr) {
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
@@ -1944,7 +1947,7 @@ __global__ void k_vjp_local(const float* __restrict__ E, const float* __restrict
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-        const int t = types[i];
+        const int t = types ? types[i] : 0;
         float gr[3] = {0.0f, 0.0f, 0.0f};
         const bool ok = isfinite(x) && isfinite(y) && isfinite(z) && t >= 0 && t < T;
         if (!ok) hpf_flag(err, (t >= 0 && t < T) ? HPF_ERR_NONFINITE : HPF_ERR_INDEX);
@@ -1977,23 +1980,26 @@ __global__ void k_vjp_local(const float* __restrict__ E, const float* __restrict
                     }
                 }
         }
-        grad[3 * i] = gr[0];
-        grad[3 * i + 1] = gr[1];
-        grad[3 * i + 2] = gr[2];
+        // charges: F_i = q_i sum W E, so the local term carries q_i
+        const float qq = charges ? charges[i] : 1.0f;
+        grad[3 * i] = qq * gr[0];
+        grad[3 * i + 1] = qq * gr[1];
+        grad[3 * i + 2] = qq * gr[2];
     }
 }
 
 // rho[d][t][g] += lambda_{i,d} W(g - x_i) (float atomics)
 __global__ void k_paint_lambda(const float* __restrict__ pos, const int32_t* __restrict__ types,
                                const float* __restrict__ lam, int64_t n, int T, int64_t M,
-                               const BoxState* __restrict__ bs, float* __restrict__ rho) {
+                               const BoxState* __restrict__ bs, float* __restrict__ rho,
+                               const float* __restrict__ charges = nullptr) {
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
     const float l0 = bs->ih_lo[0], l1 = bs->ih_lo[1], l2 = bs->ih_lo[2];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-        const int t = types[i];
+        const int t = types ? types[i] : 0;
         if (!(isfinite(x) && isfinite(y) && isfinite(z)) || t < 0 || t >= T) continue;
         int ix, iy, iz;
         float fx, fy, fz;
@@ -2004,7 +2010,10 @@ __global__ void k_paint_lambda(const float* __restrict__ pos, const int32_t* __r
         const int ys[2] = {iy, iy + 1 == n1 ? 0 : iy + 1};
         const int zs[2] = {iz, iz + 1 == n2 ? 0 : iz + 1};
         const float wx[2] = {1.0f - fx, fx}, wy[2] = {1.0f - fy, fy}, wz[2] = {1.0f - fz, fz};
-        const float l[3] = {lam[3 * i], lam[3 * i + 1], lam[3 * i + 2]};
+        // charges: the cotangent weighted by the bead's charge
+        const float qq = charges ? charges[i] : 1.0f;
+        if (qq == 0.0f) continue;
+        const float l[3] = {qq * lam[3 * i], qq * lam[3 * i + 1], qq * lam[3 * i + 2]};
 #pragma unroll
         for (int a = 0; a < 2; ++a)
 #pragma unroll
@@ -2076,7 +2085,79 @@ __global__ void k_vjp_kspace(const float2* __restrict__ rho_k, float2* phi_k, in
     if (dQ) grid_reduce_store_f<K, kThreads>(acc, partials, ticket, dQ);
 }
 
+// Adjoint of the PIC map (hymd/field.py:356-403): E_d(k) = -i k'_d psi(k),
+// psi = c M rho(k) / M with c(k) = 4 pi f H(k) / (M k^2) (k = 0: k^2 = 1, where
+// k'_d = 0), so U(k) = c(k) sum_d i k'_d P_d(k) for the charge-weighted
+// cotangent paint P_d (written over u_k).
+__global__ void k_vjp_kspace_pic(const float2* __restrict__ p_k, float2* __restrict__ u_k,
+                                 int64_t Mc, KGeom g, const BoxState* __restrict__ bs,
+                                 const Functional* __restrict__ fun, float four_pi_fac) {
+    const float s2h = fun->sigma2_half;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < Mc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        float kx, ky, kz, gx, gy, gz, wk;
+        mode_k(idx, g, bs, kx, ky, kz, gx, gy, gz, wk);
+        float k2 = kx * kx + ky * ky + kz * kz;
+        const float H = expf(-s2h * k2);
+        if (idx == 0) k2 = 1.0f;
+        const float cc = four_pi_fac * H / k2 * g.invM;
+        const float gk[3] = {gx, gy, gz};
+        float sx = 0.0f, sy = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float2 r = p_k[(int64_t)d * Mc + idx];
+            sx = fmaf(-gk[d], r.y, sx);
+            sy = fmaf(gk[d], r.x, sy);
+        }
+        u_k[idx] = make_float2(cc * sx, cc * sy);
+    }
+}
+
 }  // namespace
+
+extern "C" int hpf_pic_force_vjp(hpf_ctx* c, const float* pos, const float* charges, int64_t n,
+                                 double elec_factor, const float* lam, float* grad_pos,
+                                 void* stream) {
+    if (!c || n < 0 || (n > 0 && (!pos || !charges || !lam || !grad_pos))) return HPF_ERR_ARG;
+    if (n == 0) return HPF_OK;
+    cudaStream_t st = as_stream(stream);
+    const int64_t M = c->M, Mc = c->Mc;
+    const float four_pi_fac = (float)(4.0 * 3.14159265358979323846 * elec_factor);
+    TypeScale sq;
+    sq.s[0] = 1.0f;
+    int r;
+    // forward charge density, psi and E spectra, E grids
+    if ((r = do_paint(c, pos, nullptr, charges, n, 1, sq, c->d_grid, st)) != HPF_OK) return r;
+    if ((r = exec_r2c(c, c->d_grid, c->d_spec_phi, 1, st)) != HPF_OK) return r;
+    const KGeom g = kgeom(c);
+    k_kspace_pic<<<grid_for(Mc, kThreads), kThreads, 0, st>>>(
+        c->d_spec_phi, c->d_spec, Mc, g, c->d_box, c->d_fun, four_pi_fac, nullptr, nullptr,
+        nullptr);
+    HPF_LAUNCH_CHECK();
+    if ((r = exec_c2r(c, c->d_spec + Mc, c->d_grid, 3, st)) != HPF_OK) return r;
+    k_vjp_local<<<grid_for(n, kThreads), kThreads, 0, st>>>(c->d_grid, pos, nullptr, lam, n, 1,
+                                                            M, c->d_box, grad_pos, c->d_err,
+                                                            charges);
+    HPF_LAUNCH_CHECK();
+    // charge-weighted cotangent paint [d][M], its spectra, U, and the readout
+    HPF_CUDA_TRY(cudaMemsetAsync(c->d_grid, 0, sizeof(float) * 3 * M, st));
+    k_paint_lambda<<<grid_for(n, kThreads), kThreads, 0, st>>>(pos, nullptr, lam, n, 1, M,
+                                                               c->d_box, c->d_grid, charges);
+    HPF_LAUNCH_CHECK();
+    for (int d = 0; d < 3; ++d)
+        if ((r = exec_r2c(c, c->d_grid + (int64_t)d * M, c->d_spec + (int64_t)d * Mc, 1, st)) !=
+            HPF_OK)
+            return r;
+    k_vjp_kspace_pic<<<grid_for(Mc, kThreads), kThreads, 0, st>>>(
+        c->d_spec, c->d_spec_phi, Mc, g, c->d_box, c->d_fun, four_pi_fac);
+    HPF_LAUNCH_CHECK();
+    if ((r = exec_c2r(c, c->d_spec_phi, c->d_grid, 1, st)) != HPF_OK) return r;
+    k_readout_grad<<<grid_for(n, kThreads), kThreads, 0, st>>>(c->d_grid, pos, nullptr, n, 1, M,
+                                                               c->d_box, sq, grad_pos, c->d_err,
+                                                               1, 1, charges);
+    HPF_LAUNCH_CHECK();
+    return HPF_OK;
+}
 
 extern "C" int hpf_field_force_vjp(hpf_ctx* c, const float* pos, const int32_t* types, int64_t n,
                                    const double* type_mass, const float* lam, float* grad_pos,

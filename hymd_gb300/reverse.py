@@ -9,6 +9,9 @@ kernels in libhpf_gb300.so:
     k-space -> c2r -> readout), backward hpf_field_force_vjp: the
     vector-Jacobian product with respect to the positions and the
     functional's matrix Q (hence chi);
+  * electrostatic force of a charged system (PIC_Spectral,
+    hymd/field.py:241-403) -- forward hpf_pic_step, backward
+    hpf_pic_force_vjp (positions; the charges are constants);
   * bonded force F_b(x) (bonds, angles and four-body terms,
     hymd/compute_bond_forces.f90, compute_angle_forces.f90,
     compute_dihedral_forces.f90 with the CBT bending of
@@ -31,8 +34,8 @@ backward pass.  The loss provided is the mean squared deviation of the
 time-averaged per-type density profile along z (linear binning, so that it
 is differentiable in the positions) from a target profile.
 
-Scope: NVE or NVT (CSVR); no barostat in the differentiated step; no
-electrostatics (the PIC charge force is not differentiated).
+Scope: NVE or NVT (CSVR); no barostat in the differentiated step;
+PIC_Spectral electrostatics (not the GPE variant).
 """
 import math
 
@@ -54,8 +57,6 @@ class ForceModel:
             raise ValueError("the bonded forward needs the fused plan (RespaMD(fused=True))")
         if md.perm is not None:
             raise ValueError("reverse mode works in the caller's bead order (no sort_particles)")
-        if md.charges is not None:
-            raise NotImplementedError("electrostatics (PIC) are not differentiated")
         if md.baro_args is not None:
             raise NotImplementedError("no barostat in the differentiated step")
         cfg = md.config
@@ -70,6 +71,9 @@ class ForceModel:
         self.box = md.box
         self.box_f = md.box.float()
         self._key = None
+        # PIC_Spectral electrostatics of a charged RespaMD
+        self.charges = md.charges
+        self.elec_factor = float(md.elec_factor) if md.charges is not None else 0.0
         # CSVR of a coupled RespaMD: its arguments and random table (host)
         self.thermo = md.thermo_args
         self.randoms = md.randoms.cpu().numpy() if self.thermo is not None else None
@@ -159,8 +163,36 @@ class _BondedForce(torch.autograd.Function):
         return out, None
 
 
+class _PicForce(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, model):
+        md = model.md
+        F = torch.empty_like(x)
+        _lib.call("hpf_pic_step", model.pm._h, _lib.ptr(x), _lib.ptr(model.charges), md.n,
+                  model.elec_factor, _lib.ptr(F), None, None, None, None, None, None,
+                  _lib.stream_ptr())
+        ctx.model = model
+        ctx.save_for_backward(x)
+        return F
+
+    @staticmethod
+    def backward(ctx, lam):
+        (x,) = ctx.saved_tensors
+        model = ctx.model
+        g = torch.empty_like(x)
+        _lib.call("hpf_pic_force_vjp", model.pm._h, _lib.ptr(x), _lib.ptr(model.charges),
+                  model.md.n, model.elec_factor, _lib.ptr(lam.contiguous()), _lib.ptr(g),
+                  _lib.stream_ptr())
+        return g, None
+
+
 def field_force(x, chi, model):
-    return _FieldForce.apply(x, chi, model)
+    """The slow force of the outer kicks: the field force, plus the
+    PIC_Spectral electrostatic force of a charged system."""
+    F = _FieldForce.apply(x, chi, model)
+    if model.charges is not None:
+        F = F + _PicForce.apply(x, model)
+    return F
 
 
 def bonded_force(x, model):

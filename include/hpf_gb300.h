@@ -221,6 +221,17 @@ int hpf_energy_fp64(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_
 int hpf_field_force_vjp(hpf_ctx* ctx, const float* pos, const int32_t* types, int64_t n,
                         const double* type_mass, const float* lam, float* grad_pos, double* dQ,
                         void* stream);
+/* Vector-Jacobian product of the PIC_Spectral electrostatic force
+ * (hymd/field.py:241-403: F_i = q_i E(x_i), E = -grad psi, psi = 4 pi f H
+ * rho / k^2, f = elec_factor) with a cotangent lam (float[n][3]):
+ * grad_pos (float[n][3]) = d(lam . F)/dx, the local term (q_i times the
+ * CIC-gradient readout of lam_i . E) plus the global one (the
+ * charge-weighted cotangent paint through the adjoint Poisson map, read out
+ * with CIC-gradient weights times q_j / dV).  Charges are not differentiated.
+ * Runs on cuFFT (plans created on first use, outside capture).  No
+ * counterpart in the reference, which has no derivatives of the forces. */
+int hpf_pic_force_vjp(hpf_ctx* ctx, const float* pos, const float* charges, int64_t n,
+                      double elec_factor, const float* lam, float* grad_pos, void* stream);
 /* out (device float[n][3]) = d/de F_b(r + e lam) at e = 0 for the bond and
  * angle forces of cbf / caf (the terms of hpf_bonds / hpf_angles): minus the
  * Hessian of the bonded energy times lam, which is also the vector-Jacobian

@@ -8,6 +8,7 @@ on the full |k|^2):
   field force   hymd/field.py:152-200, 428-616 (update_field, compute_field_force)
   bond force    hymd/compute_bond_forces.f90:45-61
   angle force   hymd/compute_angle_forces.f90:58-92
+  PIC force     hymd/field.py:356-403 (update_field_force_q, PIC_Spectral)
   four-body     hymd/compute_dihedral_forces.f90:61-134 (cosine series of
                 rows 0/1 and 2/3, type 2 improper) with the CBT bending
                 energy of hymd/dipole_reconstruction.f90:50-106
@@ -84,6 +85,30 @@ def field_force(x, types, n_types, masses, mesh, box, Q, sigma):
     for d in range(3):
         Ed = E[d][t[None, :].expand(8, -1), idx]
         F.append((w * Ed).sum(0))
+    return torch.stack(F, 1)
+
+
+def pic_force(x, charges, mesh, box, sigma, elec_factor):
+    """PIC_Spectral electrostatic force (hymd/field.py:356-403) in FP64:
+    rho = CIC paint of q / dV, psi(k) = 4 pi f H rho(k) / k^2 (k = 0: k^2 =
+    1), E_d = irfft(-i k'_d psi), F_i = q_i sum W E; x may require grad."""
+    n = tuple(int(v) for v in mesh)
+    M = n[0] * n[1] * n[2]
+    dV = float(np.prod(box)) / M
+    idx, w = _cic(x, n, box)
+    q = torch.as_tensor(charges, dtype=torch.float64, device=x.device)
+    flat = torch.zeros(M, dtype=torch.float64, device=x.device)
+    flat = flat.index_add(0, idx.reshape(-1), (w * (q / dV)[None, :]).reshape(-1))
+    R = torch.fft.rfftn(flat.reshape(n))
+    k2, g = _kgrids(n, box, x.device)
+    H = torch.exp(-0.5 * sigma * sigma * k2)
+    k2z = k2.clone()
+    k2z[0, 0, 0] = 1.0
+    psi = 4.0 * math.pi * elec_factor * H * R / k2z
+    F = []
+    for d in range(3):
+        Ed = torch.fft.irfftn(-1j * g[d] * psi, s=n).reshape(M)
+        F.append(q * (w * Ed[idx]).sum(0))
     return torch.stack(F, 1)
 
 

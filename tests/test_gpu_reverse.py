@@ -98,7 +98,7 @@ def test_bonded_hvp_matches_torch_double_backward():
 
 
 def _torch_loss(x0, v0, chi, md, cfg, model, K, target, n_bins, bonds, angles, dihedrals=None,
-                thermo=None):
+                thermo=None, charges=None):
     """The same rRESPA trajectory and profile loss with the FP64 torch forces
     (four-body terms when given) and, with thermo = (args, random table),
     the CSVR of each outer step in FP64."""
@@ -110,7 +110,10 @@ def _torch_loss(x0, v0, chi, md, cfg, model, K, target, n_bins, bonds, angles, d
     dto = n_in * dt
 
     def ff(x):
-        return tf.field_force(x, md.types, md.T, list(cfg.m), cfg.mesh(), box, Q, model.sigma)
+        F = tf.field_force(x, md.types, md.T, list(cfg.m), cfg.mesh(), box, Q, model.sigma)
+        if charges is not None:
+            F = F + tf.pic_force(x, charges, cfg.mesh(), box, model.sigma, model.elec_factor)
+        return F
 
     def fb(x):
         return tf.bonded_force(x, box, bonds, angles, create_graph=True, dihedrals=dihedrals)
@@ -190,10 +193,11 @@ def test_profile_loss_gradient_matches_fp64_autograd_and_finite_differences():
     md.check_errors()
 
 
-def _peptides():
-    """Uncharged peptide chains with CBT four-body terms; no CBT angle near
-    the reference's sin(gamma) = 0.1 clamp (where its force is not the
-    gradient of its energy)."""
+def _peptides(charged=False):
+    """Peptide chains with CBT four-body terms (with charges: the side-chain
+    and counter-ion charges of the recipe); no CBT angle near the
+    reference's sin(gamma) = 0.1 clamp (where its force is not the gradient
+    of its energy)."""
     from hymd_gb300 import systems
     from hymd_gb300.hamiltonian import get_hamiltonian
     from hymd_gb300.md import RespaMD
@@ -201,7 +205,8 @@ def _peptides():
     cfg = s["config"]
     cfg.respa_inner = 3
     md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, get_hamiltonian(cfg),
-                 topology=s["topology"], max_block_beads=36)
+                 topology=s["topology"], max_block_beads=36,
+                 charges=s["charges"] if charged else None)
     names = cfg.unique_names
     T = cfg.n_types
     chi = np.zeros((T, T))
@@ -351,3 +356,78 @@ def test_force_gradient_gap_shrinks_with_the_mesh():
     _lib.call("hpf_field_step", pm._h, _lib.ptr(pos), _lib.ptr(typ), pos.shape[0],
               _lib.dvec(cfg.m), _lib.ptr(F), None, None, None, _lib.stream_ptr())
     assert torch.equal(g, -F)
+
+
+def test_pic_force_vjp_matches_torch_autograd():
+    """hpf_pic_force_vjp against the FP64 torch PIC force differentiated by
+    autograd (the forward against hpf_pic_step first)."""
+    from hymd_gb300 import _lib
+    from hymd_gb300.reverse import ForceModel
+    s, cfg, md, chi = _peptides(charged=True)
+    model = ForceModel(md)
+    q = s["charges"].astype(np.float64)
+    assert np.count_nonzero(q) > 0
+    F32 = torch.empty_like(md.r)
+    _lib.call("hpf_pic_step", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.charges), md.n,
+              model.elec_factor, _lib.ptr(F32), None, None, None, None, None, None,
+              _lib.stream_ptr())
+    x = md.r.double().clone().requires_grad_(True)
+    F = tf.pic_force(x, q, cfg.mesh(), list(cfg.box()), model.sigma, model.elec_factor)
+    assert rel_rms(F32.cpu().numpy(), F.detach().cpu().numpy()) < 1e-5
+    rng = np.random.default_rng(6)
+    lam = torch.tensor(rng.normal(size=(md.n, 3)), dtype=torch.float32, device="cuda")
+    g = torch.empty_like(md.r)
+    _lib.call("hpf_pic_force_vjp", md.pm._h, _lib.ptr(md.r), _lib.ptr(md.charges), md.n,
+              model.elec_factor, _lib.ptr(lam), _lib.ptr(g), _lib.stream_ptr())
+    (lam.double() * F).sum().backward()
+    assert rel_rms(g.cpu().numpy(), x.grad.cpu().numpy()) < 1e-4
+    md.check_errors()
+
+
+def test_profile_loss_gradient_with_charges_dihedrals_and_csvr():
+    """The K-step chi gradient through a charged peptide trajectory (field +
+    PIC_Spectral forces, CBT four-body terms, CSVR every outer step) against
+    the FP64 torch trajectory, and that against a central finite difference."""
+    from hymd_gb300.reverse import ForceModel, profile_loss
+    s, cfg, md, chi = _peptides(charged=True)
+    md.couple(thermostat=True, seed=8, n_steps=50)
+    model = ForceModel(md)
+    K, n_bins = 4, 20
+    rng = np.random.default_rng(7)
+    target = torch.tensor(rng.uniform(0.0, 3.0, size=(md.T, n_bins)), dtype=torch.float32,
+                          device="cuda")
+    chi_t = torch.tensor(chi, dtype=torch.float32, device="cuda", requires_grad=True)
+    loss, _ = profile_loss(md.r.clone(), md.v.clone(), chi_t, model, K, target, n_bins=n_bins,
+                           segment=2)
+    loss.backward()
+    g = chi_t.grad.double().cpu().numpy()
+    t = md.topo
+    bonds = (t.bond_a.long(), t.bond_b.long(), t.bond_r0.double(), t.bond_k.double())
+    angles = (t.ang_a.long(), t.ang_b.long(), t.ang_c.long(), t.ang_t0.double(),
+              t.ang_k.double())
+    dih = _dihedral_tuple(t)
+    thermo = (md.thermo_args, md.randoms.cpu().numpy())
+    q = s["charges"].astype(np.float64)
+    chi64 = torch.tensor(chi, dtype=torch.float64, device="cuda", requires_grad=True)
+    args = (md, cfg, model, K, target.double(), n_bins, bonds, angles, dih, thermo, q)
+    x0, v0 = md.r.double(), md.v.double()
+    L64 = _torch_loss(x0, v0, chi64, *args)
+    L64.backward()
+    g64 = chi64.grad.cpu().numpy()
+    assert float(loss.detach()) == pytest.approx(float(L64.detach()), rel=1e-4)
+    pairs = [(i, j) for i in range(md.T) for j in range(i + 1, md.T) if chi[i, j] != 0]
+    got = np.array([g[i, j] + g[j, i] for i, j in pairs])
+    want = np.array([g64[i, j] + g64[j, i] for i, j in pairs])
+    assert rel_rms(got, want) < 2e-3
+    i, j = pairs[0]
+    h = 1e-3
+    with torch.no_grad():
+        cp, cm = chi64.detach().clone(), chi64.detach().clone()
+        cp[i, j] += h
+        cp[j, i] += h
+        cm[i, j] -= h
+        cm[j, i] -= h
+    fd = (float(_torch_loss(x0, v0, cp, *args).detach())
+          - float(_torch_loss(x0, v0, cm, *args).detach())) / (2 * h)
+    assert want[0] == pytest.approx(fd, rel=1e-5)
+    md.check_errors()
