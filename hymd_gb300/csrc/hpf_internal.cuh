@@ -75,6 +75,7 @@ struct hpf_ctx {
     float2* d_tw;
     double* d_spec_ws;
     int spec_W, spec_tiles, spec_max_tiles;
+    int spec_W_pic, spec_tiles_pic;  // the charge k-space pass's own tile width
     int spec_ok;     // the mesh qualifies and the scratch exists
     int spec_fused;  // use them (default when spec_ok)
     // the charge chain's own scratch, so that it can run beside the density

@@ -583,14 +583,14 @@ int ilog2_host(int n) {
 
 int tile_pad(int W) { return W < 16 ? W : 0; }
 
-SpecGeom spec_geom(const hpf_ctx* c) {
+SpecGeom spec_geom(const hpf_ctx* c, int W) {
     SpecGeom g;
     g.n0 = c->n0;
     g.n1 = c->n1;
     g.n2 = c->n2;
     g.h = c->n2 / 2;
     g.nzc = g.h + 1;
-    g.W = c->spec_W;
+    g.W = W;
     g.ws = ilog2_host(g.W > 0 ? g.W : 1);
     g.ts = c->n0 * g.W + tile_pad(g.W);
     g.M = c->M;
@@ -622,11 +622,23 @@ int with_planes(int n1, int h, F f) {
 #undef HPF_PLANE
     return HPF_ERR_ARG;
 }
-// a k-space tile: T density blocks in + 2T out, or 1 charge block in + 2
-// out (PIC)
-size_t tile_smem(const hpf_ctx* c, int W) {
-    const int blocks = 3 * c->T;
+// a k-space tile: T density blocks in + 2T out, or (pic) 1 charge block in
+// + 2 out
+size_t tile_smem(const hpf_ctx* c, int W, bool pic = false) {
+    const int blocks = pic ? 3 : 3 * c->T;
     return sizeof(float2) * (size_t)blocks * (c->n0 * W + tile_pad(W));
+}
+
+// The widest tile of W in {16, 8, 4} columns that divides n1, fits the
+// shared-memory budget and leaves a tile for every SM (4 when none does).
+// The charge pass takes it for itself: with one grid in, narrower tiles
+// leave most of a block's threads without an item in the x transforms.
+int widest_tile(const hpf_ctx* c, bool pic) {
+    const int64_t cols = (int64_t)c->n1 * (c->n2 / 2 + 1);
+    int W = 16;
+    while (W > 4 && (c->n1 % W != 0 || tile_smem(c, W, pic) > kSpecTileSmem || cols / W < 152))
+        W >>= 1;
+    return W;
 }
 
 }  // namespace
@@ -661,12 +673,13 @@ int spectral_set_tile(hpf_ctx* c, int W) {
 int spectral_setup(hpf_ctx* c) {
     if (!spectral_eligible(c)) return HPF_OK;
     // default: the widest tile that leaves a block for every SM
-    int W = 16;
+    const int W = widest_tile(c, false);
     const int64_t cols = (int64_t)c->n1 * (c->n2 / 2 + 1);
-    while (W > 4 && (!spectral_tile_ok(c, W) || cols / W < 152)) W >>= 1;
     if (!spectral_tile_ok(c, W)) return HPF_OK;
     c->spec_W = W;
     c->spec_tiles = (int)(cols / W);
+    c->spec_W_pic = widest_tile(c, true);
+    c->spec_tiles_pic = (int)(cols / c->spec_W_pic);
     float2 h_tw[kTableTotal];
     for (int m = 0; m < kTable2; ++m) {
         const double a = -2.0 * 3.14159265358979323846 * (double)m / (double)kTable2;
@@ -715,7 +728,7 @@ size_t spectral_ws_words(const hpf_ctx* c) { return 4 * (size_t)c->spec_max_tile
 // accumulators (T grids, painted) -> force mesh c->d_grid [3T][M]; sums as
 // k_kspace_force's (out[0..3]) when non-null.
 int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cudaStream_t st) {
-    const SpecGeom g = spec_geom(c);
+    const SpecGeom g = spec_geom(c, c->spec_W);
     SpecScale sc;
     for (int t = 0; t < c->T; ++t) sc.s[t] = type_scale[t];
     const int ps = (int)plane_smem(c), ts = (int)tile_smem(c, g.W);
@@ -747,10 +760,10 @@ int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cuda
 // E_d (grids 1..3) in b.grid; sums[0] as k_kspace_pic's when non-null.
 int spectral_pic(hpf_ctx* c, const SpecBufs& b, float four_pi_fac, bool want_psi, double* sums,
                  cudaStream_t st) {
-    const SpecGeom g = spec_geom(c);
+    const SpecGeom g = spec_geom(c, c->spec_W_pic);
     SpecScale sc;
     sc.s[0] = 1.0f;
-    const int ps = (int)plane_smem(c), ts = (int)tile_smem(c, g.W);
+    const int ps = (int)plane_smem(c), ts = (int)tile_smem(c, g.W, true);
     with_planes(c->n1, c->n2 / 2, [&](auto kf, auto) {
         kf<<<dim3(c->n0, 1), kSpecThreads, ps, st>>>(c->d_acc + (int64_t)c->T * c->M,
                                                      b.spec_phi, g, sc, c->d_box, c->d_tw);
@@ -760,7 +773,7 @@ int spectral_pic(hpf_ctx* c, const SpecBufs& b, float four_pi_fac, bool want_psi
     double* part = b.ws;
     unsigned int* tick = reinterpret_cast<unsigned int*>(b.ws + 4 * (size_t)c->spec_max_tiles);
     int r = with_kspace(c->n0, [&](auto, auto kp) {
-        kp<<<c->spec_tiles, kSpecThreads, ts, st>>>(b.spec_phi, b.spec, g, c->d_box, c->d_fun,
+        kp<<<c->spec_tiles_pic, kSpecThreads, ts, st>>>(b.spec_phi, b.spec, g, c->d_box, c->d_fun,
                                                     four_pi_fac, c->d_tw, sums, part, tick);
         return HPF_OK;
     });
