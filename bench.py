@@ -932,6 +932,101 @@ def run_topology(args):
     return 0
 
 
+def run_gpe(args):
+    """PIC_Spectral_GPE electrostatics (hymd/field.py:764-1112) through the
+    drop-in update_field_force_q_GPE on the charged-peptide recipe (500k
+    beads, box 40 nm, mesh 128^3; dielectric 2 / 10 / 80 for BB / SC / W,
+    max_diff convergence to 1e-6, mixing 0.6): wall time per solve with the
+    filtered densities already on the device, the iteration count, and the
+    FP64 oracle's solve of the same system on one host core beside it, with
+    the forces, energy and iterations compared."""
+    import time
+    import torch
+    from hymd_gb300 import field as gf, systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from oracle import field as of
+    from oracle import hamiltonian as oh
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(0)
+    s = systems.charged_peptides(seed=2)
+    cfg = s["config"]
+    cfg.coulombtype = "PIC_Spectral_GPE"
+    cfg.dielectric_type = [2.0, 10.0, 80.0]
+    cfg.conv_crit, cfg.pol_mixing, cfg.convergence_type = 1e-6, 0.6, "max_diff"
+    T = cfg.n_types
+    ham = get_hamiltonian(cfg)
+    pm, fl, ecl, cl = gf.initialize_pm(None, cfg)
+    phi, phi_fourier, force_on_grid, v_ext_fourier, v_ext, phi_transfer, phi_lap = fl
+    phi_q, phi_q_fourier, psi, elec_field = ecl
+    (phi_eps, phi_eps_fourier, phi_eta, phi_eta_fourier, phi_pol, phi_pol_prev, elec_dot,
+     elec_field_contrib, Vbar_elec, Vbar_elec_fourier, force_mesh_elec,
+     force_mesh_elec_fourier) = cl
+    R = torch.as_tensor(s["positions"], device="cuda")
+    Ty = torch.as_tensor(s["types"], device="cuda")
+    Q = torch.as_tensor(s["charges"], device="cuda")
+    gf.update_field(phi, phi_lap, phi_transfer, None, force_on_grid, ham, pm, R, Ty, cfg, v_ext,
+                    phi_fourier, v_ext_fourier, cfg.m)
+    F = torch.zeros_like(R)
+
+    def solve():
+        out = gf.update_field_force_q_GPE(
+            None, phi, Ty, Q, phi_q, phi_q_fourier, phi_eps, phi_eps_fourier, phi_eta,
+            phi_eta_fourier, phi_pol_prev, phi_pol, elec_field, F, elec_field_contrib, psi,
+            Vbar_elec, Vbar_elec_fourier, force_mesh_elec, force_mesh_elec_fourier, ham, None,
+            None, pm, R, cfg)
+        torch.cuda.synchronize()
+        return out
+
+    for _ in range(max(args.warmup, 1)):
+        solve()
+    times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, eps_g, dot = solve()
+        times.append(time.perf_counter() - t0)
+    dev_ms = 1000.0 * float(np.median(times))
+    iters = int(pm.gpe_iterations)
+    W = gf.compute_field_energy_q_GPE(cfg, eps_g, None, dot)
+    # the FP64 oracle on the same inputs: filtered densities, then the solve
+    names = cfg.unique_names
+    chim = np.zeros((T, T))
+    for c in cfg.chi:
+        i, j = names.index(c.atom_1), names.index(c.atom_2)
+        chim[i, j] = chim[j, i] = c.interaction_energy
+    fun = oh.quadratic_from_params("DefaultWithChi", T, cfg.kappa, cfg.rho0, cfg.a, chim)
+    r64 = s["positions"].astype(np.float64)
+    ref_field = of.update_field(r64, s["types"], T, cfg.mesh(), cfg.box(), cfg.m, fun, cfg.sigma)
+    nshape = tuple(cfg.mesh())
+    state = dict(phi_eps=np.zeros(nshape), pol_prev=np.zeros(nshape), contrib=np.zeros(nshape))
+    t0 = time.perf_counter()
+    ref = of.gpe_step(ref_field["phi"], s["charges"], s["positions"], s["types"], T, cfg.mesh(),
+                      cfg.box(), cfg.sigma, cfg.dielectric_type, cfg.type_charges or [0.0] * T,
+                      state, conv_crit=cfg.conv_crit, mixing=cfg.pol_mixing, conv_kind="max_diff")
+    cpu_s = time.perf_counter() - t0
+    f_ref = ref["forces"]
+    f_rel = float(np.sqrt(np.mean((F.cpu().numpy() - f_ref) ** 2)) / np.sqrt(np.mean(f_ref ** 2)))
+    line = {"metric": "PIC_Spectral_GPE solve time (update_field_force_q_GPE)",
+            "value": dev_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 1), "higher_is_better": False, "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "iterations": iters,
+            "ms_per_iteration": dev_ms / max(iters, 1),
+            "accuracy": {"reference": "FP64 oracle (oracle/field.py:gpe_step) on the same "
+                                      "inputs", "force_rel_rms": f_rel,
+                         "energy_rel_err": abs(W - ref["energy"]) / abs(ref["energy"]),
+                         "oracle_iterations": int(ref["iterations"])},
+            "cpu_baseline": {"value": 1000.0 * cpu_s, "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": "the whole solve, FP64 numpy oracle"},
+            "config": {"workload": "charged peptides 500k beads, box 40 nm, mesh 128^3, "
+                                   "3 types, dielectric 2/10/80",
+                       "timed": "wall time of one solve (densities resident), host "
+                                "synchronisations included"}}
+    print(json.dumps(line))
+    return 0
+
+
 def run_reverse(args):
     """Reverse mode on the membrane recipe scaled to 1.3M beads (54 nm box,
     mesh 128^3): the gradient with respect to chi of the MSE between the
@@ -1211,6 +1306,8 @@ def main():
     ap.add_argument("--reverse-steps", type=int, default=200)
     ap.add_argument("--locality", action="store_true",
                     help="diagnostic: step time against the age of the bead order")
+    ap.add_argument("--gpe", action="store_true",
+                    help="PIC_Spectral_GPE solve time on the 500k peptides (one JSON line)")
     ap.add_argument("--topology", action="store_true",
                     help="bonded-term discovery (prepare_bonds) on the device, 1.3M-bead membrane")
     args = ap.parse_args()
@@ -1222,6 +1319,8 @@ def main():
         return run_reverse(args)
     if args.topology:
         return run_topology(args)
+    if args.gpe:
+        return run_gpe(args)
     if args.locality:
         return run_locality(args)
     if args.impl == "reference":

@@ -926,6 +926,9 @@ int hpf_ctx_destroy(hpf_ctx* c) {
     cudaFree(c->gpe_spec);
     cudaFree(c->gpe_ws);
     cudaFreeHost(c->gpe_host);
+    if (c->gpe_exec) cudaGraphExecDestroy(c->gpe_exec);
+    if (c->gpe_graph) cudaGraphDestroy(c->gpe_graph);
+    if (c->gpe_cap) cudaStreamDestroy(c->gpe_cap);
     cudaFree(c->d_tw);
     cudaFree(c->d_spec_ws);
     cudaFree(c->pic_spec_phi);
@@ -1788,6 +1791,42 @@ __global__ void k_gpe_force_spec(const float2* __restrict__ vk, float2* __restri
     }
 }
 
+// The polarisation loop's device state: the iteration counter and the max
+// measure's bits in the tail of gpe_ws.
+unsigned int* gpe_max_bits(hpf_ctx* c) {
+    return reinterpret_cast<unsigned int*>(c->gpe_ws + 8 + 8 * HPF_REDUCE_BLOCKS + 2);
+}
+int* gpe_iter(hpf_ctx* c) {
+    return reinterpret_cast<int*>(c->gpe_ws + 8 + 8 * HPF_REDUCE_BLOCKS + 3);
+}
+
+// before the loop: counter and max measure cleared; the loop runs when the
+// reference's `while it < max_iter and delta > conv_crit` holds for it = 0,
+// delta = 1
+__global__ void k_gpe_loop_init(int* it, unsigned int* max_bits, cudaGraphConditionalHandle h,
+                                int run) {
+    *it = 0;
+    *max_bits = 0u;
+    cudaGraphSetConditional(h, run ? 1u : 0u);
+}
+
+// after each update: the measure (KIND 0 max from its bits, else the grid
+// sum), one more iteration counted, and the loop test for the next
+template <int KIND>
+__global__ void k_gpe_loop_test(int* it, unsigned int* max_bits, const double* ws,
+                                cudaGraphConditionalHandle h, int max_iter, double crit) {
+    double delta;
+    if (KIND == 0) {
+        delta = (double)__uint_as_float(*max_bits);
+        *max_bits = 0u;
+    } else {
+        delta = ws[0];
+    }
+    const int n = *it + 1;
+    *it = n;
+    cudaGraphSetConditional(h, (n < max_iter && delta > crit) ? 1u : 0u);
+}
+
 int gpe_scratch(hpf_ctx* c) {
     if (c->gpe_grid) return HPF_OK;
     HPF_CUDA_TRY(cudaMalloc(&c->gpe_grid, sizeof(float) * (size_t)kGpeGrids * c->M));
@@ -1795,6 +1834,95 @@ int gpe_scratch(hpf_ctx* c) {
     HPF_CUDA_TRY(cudaMalloc(&c->gpe_ws, sizeof(double) * HPF_OUT_DOUBLES));
     HPF_CUDA_TRY(cudaMemset(c->gpe_ws, 0, sizeof(double) * HPF_OUT_DOUBLES));
     HPF_CUDA_TRY(cudaMallocHost(&c->gpe_host, sizeof(double) * 2));
+    return HPF_OK;
+}
+
+// One polarisation update on `st`: X -> spectrum -> E (3 grids), then pol
+// and X updated and the measure taken.
+int gpe_update(hpf_ctx* c, float* pol, int kind, float w, cudaStream_t st) {
+    const int64_t M = c->M, Mc = c->Mc;
+    float* G = c->gpe_grid;
+    float2* S = c->gpe_spec;
+    const KGeom g = kgeom(c);
+    const int gk = grid_for(Mc, kThreads), rg = reduce_grid(M, kThreads);
+    int r;
+    if ((r = exec_r2c(c, G + kGpeX * M, S, 1, st)) != HPF_OK) return r;
+    k_gpe_field_spec<<<gk, kThreads, 0, st>>>(S, S + Mc, nullptr, Mc, g, c->d_box, 1.0f);
+    HPF_LAUNCH_CHECK();
+    for (int d = 0; d < 3; ++d)
+        if ((r = exec_c2r(c, S + (1 + d) * Mc, G + (kGpeE + d) * M, 1, st)) != HPF_OK) return r;
+    unsigned int* mb = gpe_max_bits(c);
+    if (kind == 0)
+        k_gpe_pol<0><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M, G + kGpeQ * M, pol,
+                                              G + kGpeX * M, M, w, mb, c->gpe_ws);
+    else if (kind == 1)
+        k_gpe_pol<1><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M, G + kGpeQ * M, pol,
+                                              G + kGpeX * M, M, w, mb, c->gpe_ws);
+    else
+        k_gpe_pol<2><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M, G + kGpeQ * M, pol,
+                                              G + kGpeX * M, M, w, mb, c->gpe_ws);
+    HPF_LAUNCH_CHECK();
+    return HPF_OK;
+}
+
+// The loop graph: init kernel -> while node { update, test }, captured on the
+// context's own stream (cuFFT included) and instantiated once per parameter
+// set.  The handle's launch default is 0, so a graph whose init kernel did
+// not run executes no iteration.
+int gpe_loop_graph(hpf_ctx* c, float* pol, int kind, double mixing, double crit, int max_iter) {
+    if (c->gpe_exec && c->gpe_key_pol == pol && c->gpe_key_kind == kind &&
+        c->gpe_key_mix == mixing && c->gpe_key_crit == crit && c->gpe_key_max == max_iter)
+        return HPF_OK;
+    if (c->gpe_exec) cudaGraphExecDestroy(c->gpe_exec);
+    if (c->gpe_graph) cudaGraphDestroy(c->gpe_graph);
+    c->gpe_exec = nullptr;
+    c->gpe_graph = nullptr;
+    if (!c->gpe_cap) HPF_CUDA_TRY(cudaStreamCreateWithFlags(&c->gpe_cap, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    HPF_CUDA_TRY(cudaGraphCreate(&g, 0));
+    c->gpe_graph = g;
+    cudaGraphConditionalHandle h;
+    HPF_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+    cudaStream_t cs = c->gpe_cap;
+    int* it = gpe_iter(c);
+    unsigned int* mb = gpe_max_bits(c);
+    HPF_CUDA_TRY(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+    k_gpe_loop_init<<<1, 1, 0, cs>>>(it, mb, h, max_iter > 0 && 1.0 > crit);
+    cudaGraph_t g2 = nullptr;
+    const cudaError_t e1 = cudaGetLastError();
+    HPF_CUDA_TRY(cudaStreamEndCapture(cs, &g2));
+    if (e1 != cudaSuccess) return HPF_ERR_CUDA;
+    cudaGraphNode_t init = nullptr;
+    size_t count = 1;
+    HPF_CUDA_TRY(cudaGraphGetNodes(g, &init, &count));
+    if (count != 1) return HPF_ERR_CUDA;
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t loop = nullptr;
+    HPF_CUDA_TRY(cudaGraphAddNode(&loop, g, &init, nullptr, 1, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    HPF_CUDA_TRY(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+    int r = gpe_update(c, pol, kind, (float)mixing, cs);
+    if (r == HPF_OK) {
+        if (kind == 0)
+            k_gpe_loop_test<0><<<1, 1, 0, cs>>>(it, mb, c->gpe_ws, h, max_iter, crit);
+        else
+            k_gpe_loop_test<1><<<1, 1, 0, cs>>>(it, mb, c->gpe_ws, h, max_iter, crit);
+        if (cudaGetLastError() != cudaSuccess) r = HPF_ERR_CUDA;
+    }
+    cudaGraph_t b2 = nullptr;
+    HPF_CUDA_TRY(cudaStreamEndCapture(cs, &b2));
+    if (r != HPF_OK) return r;
+    HPF_CUDA_TRY(cudaGraphInstantiate(&c->gpe_exec, g, 0));
+    c->gpe_key_pol = pol;
+    c->gpe_key_kind = kind;
+    c->gpe_key_mix = mixing;
+    c->gpe_key_crit = crit;
+    c->gpe_key_max = max_iter;
     return HPF_OK;
 }
 
@@ -1812,9 +1940,12 @@ extern "C" int hpf_gpe_step(hpf_ctx* c, const float* pos, const int32_t* types,
         !eps_type || !type_charges || !phi_eps || !pol_prev || !contrib || conv_kind < 0 ||
         conv_kind > 2 || max_iter < 0 || !(coulomb_constant > 0))
         return HPF_ERR_ARG;
+    cudaStream_t st = as_stream(stream);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return HPF_ERR_ARG;
     int r = gpe_scratch(c);
     if (r != HPF_OK) return r;
-    cudaStream_t st = as_stream(stream);
     const int T = c->T;
     const int64_t M = c->M, Mc = c->Mc;
     float* G = c->gpe_grid;
@@ -1845,52 +1976,13 @@ extern "C" int hpf_gpe_step(hpf_ctx* c, const float* pos, const int32_t* types,
         if ((r = exec_c2r(c, S + (1 + d) * Mc, G + (kGpeEta + d) * M, 1, st)) != HPF_OK) return r;
     k_gpe_eta_div<<<gm, kThreads, 0, st>>>(G + kGpeEta * M, phi_eps, M);
     HPF_LAUNCH_CHECK();
-    // polarisation iteration (host-driven: the reference tests convergence
-    // after every update, so each iteration ends with a 4-byte read-back)
-    unsigned int* max_bits = reinterpret_cast<unsigned int*>(c->gpe_ws + 8 + 8 * HPF_REDUCE_BLOCKS + 2);
-    int it = 0;
-    double delta = 1.0;
+    // polarisation iteration: the reference tests convergence after every
+    // update; here the test runs on the device and drives the while node of
+    // the loop graph, so the loop needs no host round trip
+    if ((r = gpe_loop_graph(c, pol_prev, conv_kind, mixing, conv_crit, max_iter)) != HPF_OK)
+        return r;
+    HPF_CUDA_TRY(cudaGraphLaunch(c->gpe_exec, st));
     const int rg = reduce_grid(M, kThreads);
-    while (it < max_iter && delta > conv_crit) {
-        if ((r = exec_r2c(c, G + kGpeX * M, S, 1, st)) != HPF_OK) return r;
-        k_gpe_field_spec<<<gk, kThreads, 0, st>>>(S, S + Mc, nullptr, Mc, g, c->d_box, 1.0f);
-        HPF_LAUNCH_CHECK();
-        for (int d = 0; d < 3; ++d)
-            if ((r = exec_c2r(c, S + (1 + d) * Mc, G + (kGpeE + d) * M, 1, st)) != HPF_OK) return r;
-        if (conv_kind == 0) {
-            HPF_CUDA_TRY(cudaMemsetAsync(max_bits, 0, sizeof(unsigned int), st));
-            k_gpe_pol<0><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M, G + kGpeQ * M,
-                                                  pol_prev, G + kGpeX * M, M, (float)mixing,
-                                                  max_bits, c->gpe_ws);
-            HPF_LAUNCH_CHECK();
-            HPF_CUDA_TRY(cudaMemcpyAsync(c->gpe_host, max_bits, sizeof(unsigned int),
-                                         cudaMemcpyDeviceToHost, st));
-        } else {
-            if (conv_kind == 1)
-                k_gpe_pol<1><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M,
-                                                      G + kGpeQ * M, pol_prev, G + kGpeX * M, M,
-                                                      (float)mixing, max_bits, c->gpe_ws);
-            else
-                k_gpe_pol<2><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M,
-                                                      G + kGpeQ * M, pol_prev, G + kGpeX * M, M,
-                                                      (float)mixing, max_bits, c->gpe_ws);
-            HPF_LAUNCH_CHECK();
-            HPF_CUDA_TRY(cudaMemcpyAsync(c->gpe_host, c->gpe_ws, sizeof(double),
-                                         cudaMemcpyDeviceToHost, st));
-        }
-        HPF_CUDA_TRY(cudaStreamSynchronize(st));
-        if (conv_kind == 0) {
-            unsigned int b;
-            memcpy(&b, c->gpe_host, sizeof(b));
-            float f;
-            memcpy(&f, &b, sizeof(f));
-            delta = (double)f;
-        } else {
-            delta = c->gpe_host[0];
-        }
-        ++it;
-    }
-    if (iterations) *iterations = it;
     // psi = c2r(eps0^-1 r2c(q + pol) / k^2), E = c2r(-i k psi_k)
     const double e0inv = coulomb_constant * 4.0 * 3.14159265358979323846;
     if ((r = exec_r2c(c, G + kGpeX * M, S, 1, st)) != HPF_OK) return r;
@@ -1920,7 +2012,17 @@ extern "C" int hpf_gpe_step(hpf_ctx* c, const float* pos, const int32_t* types,
                                               c->d_fun);
     HPF_LAUNCH_CHECK();
     if ((r = exec_c2r(c, c->d_spec, c->d_grid, 3 * T, st)) != HPF_OK) return r;
-    if (n > 0) return launch_readout(c, c->d_grid, pos, types, nullptr, n, T, elec_forces, nullptr, st);
+    if (n > 0 &&
+        (r = launch_readout(c, c->d_grid, pos, types, nullptr, n, T, elec_forces, nullptr, st)) !=
+            HPF_OK)
+        return r;
+    if (iterations) {
+        // the count of the loop just run (the one read-back of the call)
+        HPF_CUDA_TRY(cudaMemcpyAsync(c->gpe_host, gpe_iter(c), sizeof(int),
+                                     cudaMemcpyDeviceToHost, st));
+        HPF_CUDA_TRY(cudaStreamSynchronize(st));
+        memcpy(iterations, c->gpe_host, sizeof(int));
+    }
     return HPF_OK;
 }
 

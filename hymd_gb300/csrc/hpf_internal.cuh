@@ -70,6 +70,16 @@ struct hpf_ctx {
     float2* gpe_spec;
     double* gpe_ws;
     double* gpe_host;
+    // the polarisation iteration as a CUDA graph: a while node whose body
+    // (r2c, field map, 3 c2r, update, convergence test) sets its own
+    // condition on the device; built on first use on gpe_cap, rebuilt when
+    // the iterated grid, mixing, tolerance, measure or iteration cap change
+    cudaGraph_t gpe_graph;
+    cudaGraphExec_t gpe_exec;
+    cudaStream_t gpe_cap;
+    const float* gpe_key_pol;
+    double gpe_key_mix, gpe_key_crit;
+    int gpe_key_kind, gpe_key_max;
     // fused spectral passes: twiddle tables exp(-2 pi i m / 512) and
     // exp(-2 pi i m / 768), k-space tile width, partial sums + ticket
     float2* d_tw;

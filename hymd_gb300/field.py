@@ -443,8 +443,9 @@ def update_field_force_q_GPE(conv_fun, phi, types, charges, phi_q, phi_q_fourier
     iteration starts from phi_pol_prev on every call and neither phi_pol_prev
     nor phi_pol is written: the reference rebinds both names locally
     (field.py:1010-1024), so its caller's grids keep their initial zeros and
-    every solve starts cold.  Synchronises once per iteration (the
-    convergence test)."""
+    every solve starts cold.  The polarisation iteration runs as a CUDA
+    graph whose loop test is evaluated on the device; the call synchronises
+    once, at its end, to return the iteration count (pm.gpe_iterations)."""
     T = pm.n_types
     pos = _lib.require_cuda(positions, "positions", torch.float32)
     n = pos.shape[0]

@@ -273,9 +273,13 @@ int hpf_dihedral_hvp(float* out, const float* r, const float* lam, int64_t n, co
  * starts every solve from its caller's unchanged grid (field.py:1010-1024),
  * so the drop-in passes a copy.  Optional outputs (NULL to skip): psi,
  * elec_field (float[3][M]), elec_dot (|E|^2, float[M]), vbar (float[T][M]),
- * energy (device double: dV eps0/2 sum eps |E|^2).  The convergence test
- * after each update reads 4-8 bytes back, so this call synchronises the
- * stream once per iteration; *iterations receives their number. */
+ * energy (device double: dV eps0/2 sum eps |E|^2).  The polarisation
+ * iteration runs as a CUDA graph whose while node repeats the update while
+ * the convergence test, evaluated on the device after each update, holds;
+ * the graph is built on the first call and again when pol_prev, mixing,
+ * conv_crit, conv_kind or max_iter change.  With iterations != NULL the call
+ * synchronises the stream once, at its end, and *iterations receives their
+ * number.  Not capturable: a stream under capture returns HPF_ERR_ARG. */
 int hpf_gpe_step(hpf_ctx* ctx, const float* pos, const int32_t* types, const float* charges,
                  int64_t n, const float* phi_tilde, const double* eps_type,
                  const double* type_charges, double coulomb_constant, double conv_crit,

@@ -101,3 +101,66 @@ def test_gpe_matches_oracle(conv):
         assert rel_rms(Vb[0].cpu().numpy(), ref["Vbar"][0]) < 1e-4
     assert not torch.any(phi_pol_prev) and not torch.any(phi_pol)  # caller's grids untouched
     pm.check_errors()
+
+
+def test_gpe_loop_graph_follows_parameters():
+    """The polarisation loop runs as a cached CUDA graph with a device-side
+    loop test: calls on one mesh context with another tolerance, or with
+    max_iter = 0 (no iteration), rebuild it, and each call's iteration count
+    and forces follow the FP64 oracle with that tolerance."""
+    from hymd_gb300 import _lib, field as gf
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    cfg, r, types, q = _system("max_diff", seed=23)
+    T = cfg.n_types
+    ham = get_hamiltonian(cfg)
+    pm, fl, ecl, cl = gf.initialize_pm(None, cfg)
+    phi, phi_fourier, force_on_grid, v_ext_fourier, v_ext, phi_transfer, phi_lap = fl
+    phi_q, phi_q_fourier, psi, elec_field = ecl
+    (phi_eps, phi_eps_fourier, phi_eta, phi_eta_fourier, phi_pol, phi_pol_prev, elec_dot,
+     elec_field_contrib, Vbar_elec, Vbar_elec_fourier, force_mesh_elec,
+     force_mesh_elec_fourier) = cl
+    R = torch.as_tensor(r, device="cuda")
+    Ty = torch.as_tensor(types, device="cuda")
+    Q = torch.as_tensor(q, device="cuda")
+    gf.update_field(phi, phi_lap, phi_transfer, None, force_on_grid, ham, pm, R, Ty, cfg, v_ext,
+                    phi_fourier, v_ext_fourier, cfg.m)
+    names = cfg.unique_names
+    chim = np.zeros((T, T))
+    for c in cfg.chi:
+        i, j = names.index(c.atom_1), names.index(c.atom_2)
+        chim[i, j] = chim[j, i] = c.interaction_energy
+    fun = oh.quadratic_from_params("DefaultWithChi", T, cfg.kappa, cfg.rho0, cfg.a, chim)
+    ref_field = of.update_field(r.astype(np.float64), types, T, cfg.mesh(), cfg.box(), cfg.m,
+                                fun, cfg.sigma)
+    nshape = tuple(cfg.mesh())
+    state = dict(phi_eps=np.zeros(nshape), pol_prev=np.zeros(nshape), contrib=np.zeros(nshape))
+    F = torch.zeros_like(R)
+    counts = []
+    for crit in (1e-3, 1e-7, 1e-3):
+        cfg.conv_crit = crit
+        gf.update_field_force_q_GPE(
+            None, phi, Ty, Q, phi_q, phi_q_fourier, phi_eps, phi_eps_fourier, phi_eta,
+            phi_eta_fourier, phi_pol_prev, phi_pol, elec_field, F, elec_field_contrib, psi,
+            Vbar_elec, Vbar_elec_fourier, force_mesh_elec, force_mesh_elec_fourier, ham, None,
+            None, pm, R, cfg)
+        ref = of.gpe_step(ref_field["phi"], q, r, types, T, cfg.mesh(), cfg.box(), cfg.sigma,
+                          cfg.dielectric_type, cfg.type_charges, state, conv_crit=crit,
+                          mixing=cfg.pol_mixing, conv_kind="max_diff")
+        torch.cuda.synchronize()
+        assert abs(pm.gpe_iterations - ref["iterations"]) <= 2, (crit, pm.gpe_iterations,
+                                                                ref["iterations"])
+        assert rel_rms(F.cpu().numpy(), ref["forces"]) < 1e-4, crit
+        counts.append(pm.gpe_iterations)
+    assert counts[0] < counts[1] and counts[0] == counts[2]
+    # max_iter = 0 through the C entry: the loop body never runs
+    eps = _lib.dvec(cfg.dielectric_type)
+    qt = _lib.dvec(cfg.type_charges)
+    phi_all = torch.stack([p for p in phi]) if isinstance(phi, (list, tuple)) else phi
+    pol = torch.zeros(nshape, dtype=torch.float32, device="cuda")
+    it = _lib.ctypes.c_int(-1)
+    _lib.call("hpf_gpe_step", pm._h, _lib.ptr(R), _lib.ptr(Ty), _lib.ptr(Q), R.shape[0],
+              _lib.ptr(phi_all.contiguous()), eps, qt, float(cfg.coulomb_constant), 1e-7, 0.6, 0,
+              0, _lib.ptr(phi_eps), _lib.ptr(pol), _lib.ptr(elec_field_contrib), _lib.ptr(F),
+              None, None, None, None, None, _lib.ctypes.byref(it), _lib.stream_ptr())
+    assert it.value == 0 and not torch.any(pol)
+    pm.check_errors()
