@@ -285,12 +285,16 @@ struct KickDev {
     double* ws;
 };
 
-template <int MODE>
+// SCALE: the positions are first multiplied by the isotropic barostat's
+// alpha ((float)scale[0], as hpf_scr_scale_positions does) and written back
+// through pos_w, which then also serves the reads (pos is not used).
+template <int MODE, bool SCALE = false>
 __global__ void k_readout(const float* __restrict__ fm, const float* __restrict__ pos,
                           const int32_t* __restrict__ types, const float* __restrict__ charges,
                           int64_t n, int T, int64_t M, const BoxState* __restrict__ bs,
                           float* __restrict__ force, int* err, KickDev kd,
-                          const int32_t* __restrict__ idx = nullptr, int64_t n_total = 0) {
+                          const int32_t* __restrict__ idx = nullptr, int64_t n_total = 0,
+                          float* pos_w = nullptr, const double* __restrict__ scale = nullptr) {
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
@@ -303,7 +307,20 @@ __global__ void k_readout(const float* __restrict__ fm, const float* __restrict_
             hpf_flag(err, HPF_ERR_INDEX);
             continue;
         }
-        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        float x, y, z;
+        if (SCALE) {
+            const float al = (float)scale[0];
+            x = pos_w[3 * i] * al;
+            y = pos_w[3 * i + 1] * al;
+            z = pos_w[3 * i + 2] * al;
+            pos_w[3 * i] = x;
+            pos_w[3 * i + 1] = y;
+            pos_w[3 * i + 2] = z;
+        } else {
+            x = pos[3 * i];
+            y = pos[3 * i + 1];
+            z = pos[3 * i + 2];
+        }
         float out[3] = {0.0f, 0.0f, 0.0f};
         int t = types ? types[i] : 0;
         const float q = charges ? charges[i] : 1.0f;
@@ -790,9 +807,11 @@ int do_paint(hpf_ctx* c, const float* pos, const int32_t* types, const float* ch
     return HPF_OK;
 }
 
+// pos_w / scale (both or neither): positions scaled by the barostat's alpha
+// and written back in the same pass (k_readout's SCALE).
 int launch_readout(hpf_ctx* c, const float* fm, const float* pos, const int32_t* types,
                    const float* charges, int64_t n, int T, float* force, const HpfKick* kick,
-                   cudaStream_t st) {
+                   cudaStream_t st, float* pos_w = nullptr, const double* scale = nullptr) {
     KickDev kd;
     memset(&kd, 0, sizeof(kd));
     int mode = 0;
@@ -822,7 +841,12 @@ int launch_readout(hpf_ctx* c, const float* fm, const float* pos, const int32_t*
             mode = 2;
         }
     }
-    if (mode == 0)
+    if ((pos_w != nullptr) != (scale != nullptr) || (pos_w && mode == 1)) return HPF_ERR_ARG;
+    if (mode == 0 && pos_w)
+        k_readout<0, true><<<grid_for(n, kThreads), kThreads, 0, st>>>(
+            fm, pos, types, charges, n, T, c->M, c->d_box, force, c->d_err, kd, nullptr, 0,
+            pos_w, scale);
+    else if (mode == 0)
         k_readout<0><<<grid_for(n, kThreads), kThreads, 0, st>>>(fm, pos, types, charges, n, T,
                                                                  c->M, c->d_box, force, c->d_err,
                                                                  kd);
@@ -830,6 +854,10 @@ int launch_readout(hpf_ctx* c, const float* fm, const float* pos, const int32_t*
         k_readout<1><<<grid_for(n, kThreads), kThreads, 0, st>>>(fm, pos, types, charges, n, T,
                                                                  c->M, c->d_box, force, c->d_err,
                                                                  kd);
+    else if (pos_w)
+        k_readout<2, true><<<readout_grid(n), kThreads, 0, st>>>(
+            fm, pos, types, charges, n, T, c->M, c->d_box, force,
+            kick->d_err ? kick->d_err : c->d_err, kd, nullptr, 0, pos_w, scale);
     else
         k_readout<2><<<readout_grid(n), kThreads, 0, st>>>(
             fm, pos, types, charges, n, T, c->M, c->d_box, force,
@@ -1388,8 +1416,13 @@ int hpf_field_pic_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
                        const HpfKick* kick, int painted, void* stream) {
     if (!c || !type_mass || n < 0 || count < 0 || count > n ||
         (n > 0 && (!pos || !types || !force)) ||
-        (count > 0 && (!charges || !idx || !elec_forces)) || (painted && pos_scale))
+        (count > 0 && (!charges || !idx || !elec_forces)))
         return HPF_ERR_ARG;
+    // painted with pos_scale: deposits made at the unscaled positions in the
+    // old box (those of the scaled ones in the new box); the density readout
+    // scales the positions as it reads them
+    float* pos_w = painted && pos_scale ? pos : nullptr;
+    const double* rscale = painted ? pos_scale : nullptr;
     cudaStream_t st = as_stream(stream);
     int r;
     if (!c->spec_fused) {
@@ -1412,15 +1445,18 @@ int hpf_field_pic_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
                                       pos_scale, false)) != HPF_OK)
             return r;
         if ((r = spectral_field_force(c, sc.s, sums, st)) != HPF_OK) return r;
-        if (n > 0) return launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, kick, st);
+        if (n > 0)
+            return launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, kick, st,
+                                  pos_w, rscale);
         return HPF_OK;
     }
     if ((r = pic_chain_setup(c, st)) != HPF_OK) return r;
     const float four_pi_fac = (float)(4.0 * 3.14159265358979323846 * elec_factor);
     // a barostat's rescaling of the positions happens in the density paint:
     // the charge chain starts after it
-    if (pos_scale && (r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale,
-                                   false)) != HPF_OK)
+    if (pos_scale && !painted &&
+        (r = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, pos_scale, false)) !=
+            HPF_OK)
         return r;
     HPF_CUDA_TRY(cudaEventRecord(c->pic_fork, st));
     HPF_CUDA_TRY(cudaStreamWaitEvent(c->pic_stream, c->pic_fork, 0));
@@ -1438,7 +1474,8 @@ int hpf_field_pic_step(hpf_ctx* c, float* pos, const int32_t* types, int64_t n,
         rd = do_paint(c, pos, types, nullptr, n, c->T, sc, c->d_grid, st, nullptr, false);
     if (rd == HPF_OK) rd = spectral_field_force(c, sc.s, sums, st);
     if (rd == HPF_OK && n > 0)
-        rd = launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, nullptr, st);
+        rd = launch_readout(c, c->d_grid, pos, types, nullptr, n, c->T, force, nullptr, st, pos_w,
+                            rscale);
     if (je != cudaSuccess) return HPF_ERR_CUDA;
     HPF_CUDA_TRY(cudaStreamWaitEvent(st, c->pic_join, 0));
     if (r != HPF_OK) return r;

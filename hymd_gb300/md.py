@@ -662,8 +662,8 @@ class RespaMD:
     # its final position (hpf_respa_step_paint), and the field step skips its
     # paints; with the isotropic barostat the deposits of the unscaled
     # positions in the old box are those of the scaled ones in the new box
-    # (up to rounding), and the positions are scaled after the inner loop;
-    # not with the semi-isotropic one, whose position update leaves most
+    # (up to rounding), and the density readout scales the positions as it
+    # reads them; not with the semi-isotropic one, whose position update leaves most
     # beads unscaled while the box changes
     FUSE_PAINT = True
 
@@ -678,8 +678,6 @@ class RespaMD:
             n -= 1 + (1 if self.charges is not None else 0)
             if self._free_ids is not None and self._free_ids.numel():
                 n += 1
-            if self.baro_args is not None:
-                n += 1  # the isotropic position scaling after the fused paint
         return n
 
     @property
@@ -827,10 +825,12 @@ class RespaMD:
         scale = None
         painted = fused and self._paint_fused
         if fused and self.baro_args is not None:
-            if self.baro_mode == 0 and not painted:
-                scale = self.state.data_ptr() + 12 * 8  # alpha, applied in the paint
+            if self.baro_mode == 0:
+                # alpha, applied in the paint, or after a fused paint by the
+                # density readout as it reads the positions
+                scale = self.state.data_ptr() + 12 * 8
             else:
-                # semi-isotropic (mode 1), or isotropic after a fused paint
+                # semi-isotropic (mode 1): a position kernel of its own
                 _lib.call("hpf_scr_scale_positions", _lib.ptr(self.r), self.n,
                           _lib.ptr(self.state), self.baro_mode, st)
         thermo = self.thermo_args is not None

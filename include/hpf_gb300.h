@@ -373,8 +373,13 @@ int hpf_pic_step_list(hpf_ctx* ctx, const float* pos, const float* charges, cons
  * carries the kick, as hpf_field_step.  painted nonzero: this step's
  * deposits (densities, and charges when given) are already in the
  * context's accumulators, made by hpf_respa_step_paint, and the paints are
- * skipped (not with pos_scale).  On the fused spectral path only (painted
- * or the second stream); otherwise the two calls run one after the other.
+ * skipped; with pos_scale as well, those deposits were made at the positions
+ * before the isotropic barostat's r -> alpha r (in the box before its
+ * update, which gives the same grid coordinates), and the density readout
+ * scales the positions by (float)pos_scale[0] as it reads them and writes
+ * them back (as hpf_scr_scale_positions would, without its launch).  On the
+ * fused spectral path only (painted or the second stream); otherwise the
+ * two calls run one after the other.
  * The first call with charges allocates the charge chain's scratch (about
  * 3 Mc complex and 4 M real values) and must not be under stream capture
  * (HPF_ERR_ARG). */

@@ -578,3 +578,56 @@ def test_resort_with_fused_paint_and_barostat():
     assert rel_rms(a.in_input_order(a.v).cpu().numpy(), b.v.cpu().numpy()) < 1e-4
     assert np.allclose(a.box_now(), b.box_now(), rtol=1e-6)
     a.check_errors()
+
+
+@pytest.mark.parametrize("kind", ["membrane", "charged"])
+def test_barostat_scaling_in_readout_matches_scaling_kernel(kind):
+    """With the fused paint under the isotropic barostat the density readout
+    scales the positions by alpha as it reads them (hpf_field_pic_step with
+    painted and pos_scale); against hpf_scr_scale_positions followed by the
+    field step on the scaled positions, the same float products in another
+    launch, positions, velocities, forces and box are bit-identical over
+    eager and captured NPT (CSVR + SCR) steps."""
+    from hymd_gb300 import _lib, systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+
+    class ScaleKernel(RespaMD):
+        def _outer_rest(self, st, fused=True):
+            if not (fused and self._paint_fused and self.baro_args is not None):
+                return super()._outer_rest(st, fused)
+            _lib.call("hpf_scr_scale_positions", _lib.ptr(self.r), self.n,
+                      _lib.ptr(self.state), 0, st)
+            thermo = self.thermo_args is not None
+            self._field(st, self.field_sums, kick=self._kick_args(thermo), painted=True)
+            if thermo:
+                _lib.call("hpf_csvr_scale", _lib.ptr(self.v), _lib.ptr(self.group), self.n,
+                          _lib.ptr(self.state), int(self.thermo_args.remove_com), st)
+
+    if kind == "membrane":
+        s = systems.lipid_membrane(seed=9, n_lipids=60, n_water=900, box=5.6, mesh=24)
+        kw = dict(topology=s["topology"])
+    else:
+        s = systems.charged_peptides(seed=8, n_chains=10, n_res=25, n_total=5000, box=7.5,
+                                     mesh=32)
+        kw = dict(topology=s["topology"], charges=s["charges"])
+    cfg = s["config"]
+    cfg.tau_p, cfg.n_b = 1.0, 1
+    ham = get_hamiltonian(cfg)
+    a = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    b = ScaleKernel(s["positions"], s["velocities"], s["types"], cfg, ham, **kw)
+    for m in (a, b):
+        m.couple(thermostat=True, barostat="isotropic", seed=12, n_steps=20)
+        m.prime()
+        m.run(2)
+    assert a._paint_fused and b._paint_fused
+    for m in (a, b):
+        m.capture()
+        m.run(4)
+    torch.cuda.synchronize()
+    names = ["r", "v", "f_field", "box"] + (["f_elec"] if kind == "charged" else [])
+    for name in names:
+        assert torch.equal(getattr(a, name), getattr(b, name)), name
+    assert not np.allclose(a.box_now(), np.asarray(cfg.box()), rtol=1e-9)  # the box moved
+    a.check_errors()
+    b.check_errors()
