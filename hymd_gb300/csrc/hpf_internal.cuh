@@ -706,8 +706,12 @@ __device__ __forceinline__ bool grid_reduce_store_f(float (&vf)[K], double* part
                                                     unsigned int* ticket, double* out) {
     __shared__ bool is_last;
     block_partials_f<K, NT>(vf, partials, gridDim.x);
+    // the partials may come from several warps (the transposed form): each
+    // writer fences, and the barrier puts every write before the ticket, so
+    // that the last block never reads a slot its owner has not yet written
+    __threadfence();
+    __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
         unsigned int t = atomicAdd(ticket, 1u);
         is_last = (t == gridDim.x - 1);
     }
