@@ -1874,20 +1874,47 @@ int gpe_scratch(hpf_ctx* c) {
     return HPF_OK;
 }
 
-// One polarisation update on `st`: X -> spectrum -> E (3 grids), then pol
-// and X updated and the measure taken.
-int gpe_update(hpf_ctx* c, float* pol, int kind, float w, cudaStream_t st) {
+// psi = scale c2r(r2c(X) / (M k^2)) into *psi_grid (when psi_grid is given)
+// and E_d = c2r(-i k'_d ...) into the E grids: the fused spectral passes of
+// the PIC chain on the real grid X without the filter (psi then lands in
+// X's slot, after pass A has read X), or cuFFT with k_gpe_field_spec.
+int gpe_field(hpf_ctx* c, float scale, float** psi_grid, cudaStream_t st) {
     const int64_t M = c->M, Mc = c->Mc;
     float* G = c->gpe_grid;
     float2* S = c->gpe_spec;
-    const KGeom g = kgeom(c);
-    const int gk = grid_for(Mc, kThreads), rg = reduce_grid(M, kThreads);
     int r;
+    if (c->spec_fused) {
+        const SpecBufs b{S, S + Mc, G + (kGpeE - 1) * M, c->d_spec_ws};
+        static_assert(kGpeE - 1 == kGpeX, "psi takes X's slot");
+        if ((r = spectral_pic(c, b, scale, psi_grid != nullptr, nullptr, st, G + kGpeX * M,
+                              false)) != HPF_OK)
+            return r;
+        if (psi_grid) *psi_grid = G + kGpeX * M;
+        return HPF_OK;
+    }
+    const KGeom g = kgeom(c);
+    const int gk = grid_for(Mc, kThreads);
     if ((r = exec_r2c(c, G + kGpeX * M, S, 1, st)) != HPF_OK) return r;
-    k_gpe_field_spec<<<gk, kThreads, 0, st>>>(S, S + Mc, nullptr, Mc, g, c->d_box, 1.0f);
+    k_gpe_field_spec<<<gk, kThreads, 0, st>>>(S, S + Mc, psi_grid ? S : nullptr, Mc, g, c->d_box,
+                                              scale);
     HPF_LAUNCH_CHECK();
     for (int d = 0; d < 3; ++d)
         if ((r = exec_c2r(c, S + (1 + d) * Mc, G + (kGpeE + d) * M, 1, st)) != HPF_OK) return r;
+    if (psi_grid) {
+        if ((r = exec_c2r(c, S, G + kGpePsi * M, 1, st)) != HPF_OK) return r;
+        *psi_grid = G + kGpePsi * M;
+    }
+    return HPF_OK;
+}
+
+// One polarisation update on `st`: X -> E (3 grids), then pol and X updated
+// and the measure taken.
+int gpe_update(hpf_ctx* c, float* pol, int kind, float w, cudaStream_t st) {
+    const int64_t M = c->M;
+    float* G = c->gpe_grid;
+    const int rg = reduce_grid(M, kThreads);
+    int r;
+    if ((r = gpe_field(c, 1.0f, nullptr, st)) != HPF_OK) return r;
     unsigned int* mb = gpe_max_bits(c);
     if (kind == 0)
         k_gpe_pol<0><<<rg, kThreads, 0, st>>>(G + kGpeEta * M, G + kGpeE * M, G + kGpeQ * M, pol,
@@ -2022,20 +2049,16 @@ extern "C" int hpf_gpe_step(hpf_ctx* c, const float* pos, const int32_t* types,
     const int rg = reduce_grid(M, kThreads);
     // psi = c2r(eps0^-1 r2c(q + pol) / k^2), E = c2r(-i k psi_k)
     const double e0inv = coulomb_constant * 4.0 * 3.14159265358979323846;
-    if ((r = exec_r2c(c, G + kGpeX * M, S, 1, st)) != HPF_OK) return r;
-    k_gpe_field_spec<<<gk, kThreads, 0, st>>>(S, S + Mc, S, Mc, g, c->d_box, (float)e0inv);
-    HPF_LAUNCH_CHECK();
-    for (int d = 0; d < 3; ++d)
-        if ((r = exec_c2r(c, S + (1 + d) * Mc, G + (kGpeE + d) * M, 1, st)) != HPF_OK) return r;
-    if ((r = exec_c2r(c, S, G + kGpePsi * M, 1, st)) != HPF_OK) return r;
+    float* psi_grid = nullptr;
+    if ((r = gpe_field(c, (float)e0inv, &psi_grid, st)) != HPF_OK) return r;
     // |E|^2, contributions, V_t (into the context's real scratch), energy
-    k_gpe_vbar<<<rg, kThreads, 0, st>>>(G + kGpeE * M, G + kGpePsi * M, G + kGpeTot * M, phi_eps,
+    k_gpe_vbar<<<rg, kThreads, 0, st>>>(G + kGpeE * M, psi_grid, G + kGpeTot * M, phi_eps,
                                         contrib, T, M, eps_t, q_t, (float)(0.5 / e0inv), c->d_grid,
                                         elec_dot_out, c->gpe_ws, energy_out, c->d_box,
                                         0.5 / e0inv);
     HPF_LAUNCH_CHECK();
     if (psi_out)
-        HPF_CUDA_TRY(cudaMemcpyAsync(psi_out, G + kGpePsi * M, sizeof(float) * M,
+        HPF_CUDA_TRY(cudaMemcpyAsync(psi_out, psi_grid, sizeof(float) * M,
                                      cudaMemcpyDeviceToDevice, st));
     if (elec_field_out)
         HPF_CUDA_TRY(cudaMemcpyAsync(elec_field_out, G + kGpeE * M, sizeof(float) * 3 * M,

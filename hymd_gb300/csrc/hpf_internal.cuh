@@ -131,8 +131,11 @@ int spectral_setup(hpf_ctx* c);
 bool spectral_tile_ok(const hpf_ctx* c, int W);
 int spectral_set_tile(hpf_ctx* c, int W);
 int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cudaStream_t st);
+// real_in non-NULL: the input is that real grid (float[M]) instead of the
+// charge accumulator; filter = false drops H(k) from the Poisson map (the GPE
+// solve's psi = scale (q + pol) / k^2).
 int spectral_pic(hpf_ctx* c, const SpecBufs& b, float four_pi_fac, bool want_psi, double* sums,
-                 cudaStream_t st);
+                 cudaStream_t st, const float* real_in = nullptr, bool filter = true);
 // words of a pass-B partial-sum buffer (partials of the narrowest tile + ticket)
 size_t spectral_ws_words(const hpf_ctx* c);
 

@@ -116,10 +116,13 @@ __device__ __forceinline__ int plane_row(int r) {
 // the half spectrum X[0..h] fused into the first step of the y transform;
 // the y transform's second step writes the spectrum plane.
 // blockIdx.y: the grid (type) of acc and spec; sc.s[that grid] scales it.
-template <int NY, int HZ>
+// FIX = false: the input is a real grid (fin, float[grids][M]) scaled by
+// sc.s[grid] alone, read and left as it is (the accumulators are not used).
+template <int NY, int HZ, bool FIX = true>
 __global__ void __launch_bounds__(kSpecThreads, 2)
     k_spec_fwd(unsigned long long* __restrict__ acc, float2* __restrict__ spec, SpecGeom g,
-               SpecScale sc, const BoxState* __restrict__ bs, const float2* __restrict__ tw) {
+               SpecScale sc, const BoxState* __restrict__ bs, const float2* __restrict__ tw,
+               const float* __restrict__ fin = nullptr) {
     extern __shared__ __align__(16) float2 sm[];
     constexpr int Ny = NY, H = HZ, Nzc = H + 1, Ls = plane_ls(H), PN = plane_n2(H);
     // twiddles exp(-2 pi i k / n2) of the even/odd split
@@ -128,17 +131,27 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     auto zs = [](int e) { return PN > 1 ? e + e / PN : e; };
     auto row0 = [](int r) { return plane_row<NY, HZ>(r); };
-    const float s = sc.s[t] * bs->inv_dV * kFixInv;
+    const float s = FIX ? sc.s[t] * bs->inv_dV * kFixInv : sc.s[t];
     ulonglong2* a =
-        reinterpret_cast<ulonglong2*>(acc + (int64_t)t * g.M + (int64_t)x * Ny * (2 * H));
+        FIX ? reinterpret_cast<ulonglong2*>(acc + (int64_t)t * g.M + (int64_t)x * Ny * (2 * H))
+            : nullptr;
+    const float2* af =
+        FIX ? nullptr
+            : reinterpret_cast<const float2*>(fin + (int64_t)t * g.M + (int64_t)x * Ny * (2 * H));
     float2* out = spec + (int64_t)t * g.Mc + (int64_t)x * Ny * Nzc;
     constexpr float inv_rows = 1.0f / (float)Ny, inv_cols = 1.0f / (float)Nzc;
     {
         // z (rows r = y)
         auto ld = [&](int r, int m) {
-            const ulonglong2 v = __ldcg(a + r * H + m);
-            a[r * H + m] = make_ulonglong2(0ull, 0ull);
-            return make_float2(fix_to_float((long long)v.x) * s, fix_to_float((long long)v.y) * s);
+            if constexpr (FIX) {
+                const ulonglong2 v = __ldcg(a + r * H + m);
+                a[r * H + m] = make_ulonglong2(0ull, 0ull);
+                return make_float2(fix_to_float((long long)v.x) * s,
+                                   fix_to_float((long long)v.y) * s);
+            } else {
+                const float2 v = __ldg(af + r * H + m);
+                return make_float2(v.x * s, v.y * s);
+            }
         };
         auto st = [&](int r, int p, float2 v) { sm[row0(r) + zs(p)] = v; };
         // (no second step: positions are frequencies, in natural order)
@@ -367,7 +380,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     k_spec_kspace_pic(const float2* __restrict__ rho, float2* __restrict__ out_spec, SpecGeom g,
                       const BoxState* __restrict__ bs, const Functional* __restrict__ fun,
                       float four_pi_fac, const float2* __restrict__ tw,
-                      double* sums, double* partials, unsigned int* ticket) {
+                      double* sums, double* partials, unsigned int* ticket, int filter) {
     extern __shared__ __align__(16) float2 sm[];
     __shared__ ColInfo col[16];
     const int W = g.W, ws = g.ws, TS = g.ts;
@@ -408,7 +421,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                 const int ix = N2 * i + n2;
                 const float kx = (ix <= N / 2 ? ix : ix - N) * kf0;
                 float k2 = kx * kx + ci.ky * ci.ky + ci.kz * ci.kz;
-                const float Hk = expf(-s2h * k2);
+                const float Hk = filter ? expf(-s2h * k2) : 1.0f;
                 if (ix == 0 && ci.origin) k2 = 1.0f;  // k.normp(p=2, zeromode=1)
                 const float2 r = in[fx::pos(ix) * W + w];
                 const float2 rq = make_float2(r.x * invM, r.y * invM);
@@ -608,8 +621,9 @@ size_t plane_smem(const hpf_ctx* c) {
 // for this mesh.
 template <class F>
 int with_planes(int n1, int h, F f) {
-#define HPF_PLANE(NY, HZ) \
-    if (n1 == NY && h == HZ) return f(k_spec_fwd<NY, HZ>, k_spec_inv<NY, HZ>);
+#define HPF_PLANE(NY, HZ)   \
+    if (n1 == NY && h == HZ) \
+        return f(k_spec_fwd<NY, HZ>, k_spec_inv<NY, HZ>, k_spec_fwd<NY, HZ, false>);
 #define HPF_PLANES(NY) HPF_PLANE(NY, 8) HPF_PLANE(NY, 16) HPF_PLANE(NY, 32) HPF_PLANE(NY, 64)
     HPF_PLANES(16)
     HPF_PLANES(32)
@@ -648,7 +662,7 @@ bool spectral_eligible(const hpf_ctx* c) {
     if (c->T > kSpecMaxT) return false;
     if (with_kspace(c->n0, [](auto, auto) { return HPF_OK; }) != HPF_OK) return false;
     if (plane_smem(c) > kSpecMaxSmem) return false;
-    if (with_planes(c->n1, c->n2 / 2, [](auto, auto) { return HPF_OK; }) != HPF_OK) return false;
+    if (with_planes(c->n1, c->n2 / 2, [](auto, auto, auto) { return HPF_OK; }) != HPF_OK) return false;
     return tile_smem(c, 4) <= kSpecTileSmem;
 }
 
@@ -701,10 +715,12 @@ int spectral_setup(hpf_ctx* c) {
     // the kernels' shared-memory ceilings are process-wide attributes: set
     // them to the largest size any context may launch with
     const int ps = (int)kSpecMaxSmem, ts = (int)kSpecTileSmem;
-    if (with_planes(c->n1, c->n2 / 2, [&](auto kf, auto ki) {
+    if (with_planes(c->n1, c->n2 / 2, [&](auto kf, auto ki, auto kr) {
             return (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, ps) !=
                         cudaSuccess ||
                     cudaFuncSetAttribute(ki, cudaFuncAttributeMaxDynamicSharedMemorySize, ps) !=
+                        cudaSuccess ||
+                    cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, ps) !=
                         cudaSuccess)
                        ? HPF_ERR_CUDA
                        : HPF_OK;
@@ -732,9 +748,9 @@ int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cuda
     SpecScale sc;
     for (int t = 0; t < c->T; ++t) sc.s[t] = type_scale[t];
     const int ps = (int)plane_smem(c), ts = (int)tile_smem(c, g.W);
-    with_planes(c->n1, c->n2 / 2, [&](auto kf, auto) {
+    with_planes(c->n1, c->n2 / 2, [&](auto kf, auto, auto) {
         kf<<<dim3(c->n0, c->T), kSpecThreads, ps, st>>>(c->d_acc, c->d_spec_phi, g, sc, c->d_box,
-                                                        c->d_tw);
+                                                        c->d_tw, nullptr);
         return HPF_OK;
     });
     HPF_LAUNCH_CHECK();
@@ -747,7 +763,7 @@ int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cuda
     });
     if (r != HPF_OK) return r;
     HPF_LAUNCH_CHECK();
-    with_planes(c->n1, c->n2 / 2, [&](auto, auto ki) {
+    with_planes(c->n1, c->n2 / 2, [&](auto, auto ki, auto) {
         ki<<<dim3(c->n0, 3 * c->T), kSpecThreads, ps, st>>>(c->d_spec, c->d_grid, g, c->d_box,
                                                              c->d_tw, 0, 0);
         return HPF_OK;
@@ -756,17 +772,23 @@ int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cuda
     return HPF_OK;
 }
 
-// charge accumulator (slot T, painted) -> psi (grid 0, when want_psi) and
-// E_d (grids 1..3) in b.grid; sums[0] as k_kspace_pic's when non-null.
+// charge accumulator (slot T, painted), or the real grid real_in -> psi
+// (grid 0, when want_psi) and E_d (grids 1..3) in b.grid; sums[0] as
+// k_kspace_pic's when non-null.
 int spectral_pic(hpf_ctx* c, const SpecBufs& b, float four_pi_fac, bool want_psi, double* sums,
-                 cudaStream_t st) {
+                 cudaStream_t st, const float* real_in, bool filter) {
     const SpecGeom g = spec_geom(c, c->spec_W_pic);
     SpecScale sc;
     sc.s[0] = 1.0f;
     const int ps = (int)plane_smem(c), ts = (int)tile_smem(c, g.W, true);
-    with_planes(c->n1, c->n2 / 2, [&](auto kf, auto) {
-        kf<<<dim3(c->n0, 1), kSpecThreads, ps, st>>>(c->d_acc + (int64_t)c->T * c->M,
-                                                     b.spec_phi, g, sc, c->d_box, c->d_tw);
+    with_planes(c->n1, c->n2 / 2, [&](auto kf, auto, auto kr) {
+        if (real_in)
+            kr<<<dim3(c->n0, 1), kSpecThreads, ps, st>>>(nullptr, b.spec_phi, g, sc, c->d_box,
+                                                         c->d_tw, real_in);
+        else
+            kf<<<dim3(c->n0, 1), kSpecThreads, ps, st>>>(c->d_acc + (int64_t)c->T * c->M,
+                                                         b.spec_phi, g, sc, c->d_box, c->d_tw,
+                                                         nullptr);
         return HPF_OK;
     });
     HPF_LAUNCH_CHECK();
@@ -774,13 +796,14 @@ int spectral_pic(hpf_ctx* c, const SpecBufs& b, float four_pi_fac, bool want_psi
     unsigned int* tick = reinterpret_cast<unsigned int*>(b.ws + 4 * (size_t)c->spec_max_tiles);
     int r = with_kspace(c->n0, [&](auto, auto kp) {
         kp<<<c->spec_tiles_pic, kSpecThreads, ts, st>>>(b.spec_phi, b.spec, g, c->d_box, c->d_fun,
-                                                    four_pi_fac, c->d_tw, sums, part, tick);
+                                                    four_pi_fac, c->d_tw, sums, part, tick,
+                                                    filter ? 1 : 0);
         return HPF_OK;
     });
     if (r != HPF_OK) return r;
     HPF_LAUNCH_CHECK();
     const int first = want_psi ? 0 : 1;
-    with_planes(c->n1, c->n2 / 2, [&](auto, auto ki) {
+    with_planes(c->n1, c->n2 / 2, [&](auto, auto ki, auto) {
         ki<<<dim3(c->n0, 4 - first), kSpecThreads, ps, st>>>(b.spec, b.grid, g, c->d_box,
                                                              c->d_tw, first, 1);
         return HPF_OK;

@@ -26,7 +26,7 @@ def rel_rms(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
 
 
-def _system(conv, seed=21):
+def _system(conv, seed=21, mesh=(24, 24, 26)):
     from hymd_gb300.config import Config
     from hymd_gb300.force import Chi
     rng = np.random.default_rng(seed)
@@ -41,7 +41,7 @@ def _system(conv, seed=21):
     q[k] = rng.choice([-1.0, 1.0], len(k)).astype(np.float32)
     names = ["A", "B", "C"]
     chi = [Chi("A", "B", 12.0), Chi("A", "C", 4.0), Chi("B", "C", 20.0)]
-    cfg = Config(n_steps=1, time_step=0.03, mesh_size=[24, 24, 26], sigma=0.5,
+    cfg = Config(n_steps=1, time_step=0.03, mesh_size=list(mesh), sigma=0.5,
                  kappa=0.05, box_size=box, n_particles=n, n_types=T, mass=72.0,
                  hamiltonian="DefaultWithChi", unique_names=names,
                  type_to_name_map=dict(enumerate(names)), chi=chi, m=[1.0, 1.0, 1.0],
@@ -52,11 +52,15 @@ def _system(conv, seed=21):
     return cfg, r, types, q
 
 
-@pytest.mark.parametrize("conv", ["max_diff", "csum"])
-def test_gpe_matches_oracle(conv):
+@pytest.mark.parametrize("conv,mesh", [("max_diff", (24, 24, 26)), ("csum", (24, 24, 26)),
+                                       ("max_diff", (24, 24, 24)), ("csum", (32, 32, 32))])
+def test_gpe_matches_oracle(conv, mesh):
+    """24 x 24 x 26 takes the cuFFT transforms; the cubic meshes the fused
+    spectral passes (the polarisation loop and the final psi, E on the PIC
+    chain's passes without the filter)."""
     from hymd_gb300 import field as gf
     from hymd_gb300.hamiltonian import get_hamiltonian
-    cfg, r, types, q = _system(conv)
+    cfg, r, types, q = _system(conv, mesh=mesh)
     T = cfg.n_types
     ham = get_hamiltonian(cfg)
     pm, fl, ecl, cl = gf.initialize_pm(None, cfg)
@@ -68,6 +72,7 @@ def test_gpe_matches_oracle(conv):
     R = torch.as_tensor(r, device="cuda")
     Ty = torch.as_tensor(types, device="cuda")
     Q = torch.as_tensor(q, device="cuda")
+    assert pm.spectral == ("cufft" if mesh[2] == 26 else "fused")
     gf.update_field(phi, phi_lap, phi_transfer, None, force_on_grid, ham, pm, R, Ty, cfg, v_ext,
                     phi_fourier, v_ext_fourier, cfg.m)
     names = cfg.unique_names
@@ -110,7 +115,7 @@ def test_gpe_loop_graph_follows_parameters():
     and forces follow the FP64 oracle with that tolerance."""
     from hymd_gb300 import _lib, field as gf
     from hymd_gb300.hamiltonian import get_hamiltonian
-    cfg, r, types, q = _system("max_diff", seed=23)
+    cfg, r, types, q = _system("max_diff", seed=23, mesh=(24, 24, 24))
     T = cfg.n_types
     ham = get_hamiltonian(cfg)
     pm, fl, ecl, cl = gf.initialize_pm(None, cfg)
