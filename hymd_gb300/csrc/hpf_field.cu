@@ -295,6 +295,7 @@ __global__ void k_readout(const float* __restrict__ fm, const float* __restrict_
                           float* __restrict__ force, int* err, KickDev kd,
                           const int32_t* __restrict__ idx = nullptr, int64_t n_total = 0,
                           float* pos_w = nullptr, const double* __restrict__ scale = nullptr) {
+    pdl_wait();
     float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const int n0 = bs->n[0], n1 = bs->n[1], n2 = bs->n[2];
     const float h0 = bs->ih_hi[0], h1 = bs->ih_hi[1], h2 = bs->ih_hi[2];
@@ -382,6 +383,7 @@ __global__ void k_readout(const float* __restrict__ fm, const float* __restrict_
             }
         }
     }
+    pdl_trigger();
     if (MODE == 2) {
         if (grid_reduce_store_f<8, kThreads>(acc, ws_partials(kd.ws), ws_ticket(kd.ws), kd.ws))
             csvr_update(kd.a, kd.ws, kd.randoms, kd.counter, kd.state, err);
@@ -842,28 +844,27 @@ int launch_readout(hpf_ctx* c, const float* fm, const float* pos, const int32_t*
         }
     }
     if ((pos_w != nullptr) != (scale != nullptr) || (pos_w && mode == 1)) return HPF_ERR_ARG;
+    int* err = mode == 2 && kick->d_err ? kick->d_err : c->d_err;
+    const int grid = mode == 2 ? readout_grid(n) : grid_for(n, kThreads);
+    const int32_t* no_idx = nullptr;
+    const int64_t n_total = 0;
+    cudaError_t e;
     if (mode == 0 && pos_w)
-        k_readout<0, true><<<grid_for(n, kThreads), kThreads, 0, st>>>(
-            fm, pos, types, charges, n, T, c->M, c->d_box, force, c->d_err, kd, nullptr, 0,
-            pos_w, scale);
+        e = launch_pdl(k_readout<0, true>, grid, kThreads, 0, st, fm, pos, types, charges, n, T,
+                       c->M, c->d_box, force, err, kd, no_idx, n_total, pos_w, scale);
     else if (mode == 0)
-        k_readout<0><<<grid_for(n, kThreads), kThreads, 0, st>>>(fm, pos, types, charges, n, T,
-                                                                 c->M, c->d_box, force, c->d_err,
-                                                                 kd);
+        e = launch_pdl(k_readout<0>, grid, kThreads, 0, st, fm, pos, types, charges, n, T, c->M,
+                       c->d_box, force, err, kd, no_idx, n_total, pos_w, scale);
     else if (mode == 1)
-        k_readout<1><<<grid_for(n, kThreads), kThreads, 0, st>>>(fm, pos, types, charges, n, T,
-                                                                 c->M, c->d_box, force, c->d_err,
-                                                                 kd);
+        e = launch_pdl(k_readout<1>, grid, kThreads, 0, st, fm, pos, types, charges, n, T, c->M,
+                       c->d_box, force, err, kd, no_idx, n_total, pos_w, scale);
     else if (pos_w)
-        k_readout<2, true><<<readout_grid(n), kThreads, 0, st>>>(
-            fm, pos, types, charges, n, T, c->M, c->d_box, force,
-            kick->d_err ? kick->d_err : c->d_err, kd, nullptr, 0, pos_w, scale);
+        e = launch_pdl(k_readout<2, true>, grid, kThreads, 0, st, fm, pos, types, charges, n, T,
+                       c->M, c->d_box, force, err, kd, no_idx, n_total, pos_w, scale);
     else
-        k_readout<2><<<readout_grid(n), kThreads, 0, st>>>(
-            fm, pos, types, charges, n, T, c->M, c->d_box, force,
-            kick->d_err ? kick->d_err : c->d_err, kd);
-    HPF_LAUNCH_CHECK();
-    return HPF_OK;
+        e = launch_pdl(k_readout<2>, grid, kThreads, 0, st, fm, pos, types, charges, n, T, c->M,
+                       c->d_box, force, err, kd, no_idx, n_total, pos_w, scale);
+    return e == cudaSuccess ? HPF_OK : HPF_ERR_CUDA;
 }
 
 SpecBufs main_bufs(hpf_ctx* c) { return SpecBufs{c->d_spec_phi, c->d_spec, c->d_grid, c->d_spec_ws}; }

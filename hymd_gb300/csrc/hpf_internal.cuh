@@ -386,6 +386,34 @@ __device__ __forceinline__ void scr_update(const HpfScrArgs& a, double sum_v2,
 
 static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Programmatic dependent launch (sm_90 and later).  A kernel started with
+// launch_pdl may be scheduled before its predecessor on the stream has
+// finished: it calls pdl_wait() before anything else, which returns once the
+// predecessor grid has completed and its memory operations are visible.  A
+// kernel calls pdl_trigger() when its main work is done, so that its
+// successor's blocks are scheduled while it drains (a block that exits
+// without it counts as triggered).  Both are no-ops in a kernel launched the
+// ordinary way.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 
 // Grid coordinate s = x * n/L split into a node index and a fraction in
 // [0,1), using only FP32 arithmetic.  n/L is held as hi+lo floats and the

@@ -151,6 +151,7 @@ __global__ void k_csvr_scale(float* __restrict__ v, const int32_t* __restrict__ 
 // j is j mod 3.  Bit-equal to k_csvr_scale.
 __global__ void k_csvr_scale_flat(float* __restrict__ v, int64_t n3,
                                   const double* __restrict__ state) {
+    pdl_wait();
     const float al = (float)state[0];
     const float b0 = (float)state[1], b1 = (float)state[2], b2 = (float)state[3];
     const int64_t n4 = n3 >> 2;
@@ -178,7 +179,8 @@ void launch_csvr_scale(float* v, const int32_t* group, int64_t n, const double* 
                        int remove_com, cudaStream_t st) {
     if (!group && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
         const int64_t n4 = (3 * n + 3) / 4;
-        k_csvr_scale_flat<<<grid_for(n4), kThreads, 0, st>>>(v, 3 * n, state);
+        // a failed launch is left in the runtime's last error for the caller's check
+        (void)launch_pdl(k_csvr_scale_flat, grid_for(n4), kThreads, 0, st, v, 3 * n, state);
     } else {
         k_csvr_scale<<<grid_for(n), kThreads, 0, st>>>(v, group, n, state, remove_com);
     }

@@ -514,6 +514,8 @@ __device__ __forceinline__ void prefetch_l1(const void* p) {
 __global__ void __launch_bounds__(kFinishThreads)
 k_respa_finish(const double* __restrict__ partials, unsigned int G, double* out, BaroFuse baro,
                int* err) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double res[kOut];
     __shared__ float2 red[kOut * 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -986,10 +988,10 @@ int respa_run(hpf_respa_plan* p, float* r, float* v, float* f_bonded,
     }
     if (split) HPF_CUDA_TRY(cudaStreamWaitEvent(st, p->free_join, 0));
     if (rc != HPF_OK) return rc;
-    if (out) {
-        k_respa_finish<<<1, kFinishThreads, 0, st>>>(p->partials, G, out, bf, d_err);
-        HPF_LAUNCH_CHECK();
-    }
+    if (out && launch_pdl(k_respa_finish, 1, kFinishThreads, 0, st,
+                          static_cast<const double*>(p->partials), G, out, bf, d_err) !=
+                   cudaSuccess)
+        return HPF_ERR_CUDA;
     return HPF_OK;
 }
 

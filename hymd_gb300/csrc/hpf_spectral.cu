@@ -123,6 +123,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     k_spec_fwd(unsigned long long* __restrict__ acc, float2* __restrict__ spec, SpecGeom g,
                SpecScale sc, const BoxState* __restrict__ bs, const float2* __restrict__ tw,
                const float* __restrict__ fin = nullptr) {
+    pdl_wait();
     extern __shared__ __align__(16) float2 sm[];
     constexpr int Ny = NY, H = HZ, Nzc = H + 1, Ls = plane_ls(H), PN = plane_n2(H);
     // twiddles exp(-2 pi i k / n2) of the even/odd split
@@ -218,6 +219,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                 for (int cc = lane; cc < Nzc; cc += 32) out[ky * Nzc + cc] = sm[row0(ky) + cc];
         }
     }
+    pdl_trigger();
 }
 
 // ------------------------------------------------------------ pass B ---
@@ -232,6 +234,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                   const BoxState* __restrict__ bs, const Functional* __restrict__ fun,
                   const float2* __restrict__ tw, double* sums, double* partials,
                   unsigned int* ticket) {
+    pdl_wait();
     extern __shared__ __align__(16) float2 sm[];
     __shared__ float sQ[kSpecMaxT * kSpecMaxT], sb[kSpecMaxT];
     __shared__ ColInfo col[16];
@@ -367,6 +370,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             }
         }
     }
+    pdl_trigger();
     if (sums) grid_reduce_store_f<4, kSpecThreads>(acc, partials, ticket, sums);
 }
 
@@ -381,6 +385,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                       const BoxState* __restrict__ bs, const Functional* __restrict__ fun,
                       float four_pi_fac, const float2* __restrict__ tw,
                       double* sums, double* partials, unsigned int* ticket, int filter) {
+    pdl_wait();
     extern __shared__ __align__(16) float2 sm[];
     __shared__ ColInfo col[16];
     const int W = g.W, ws = g.ws, TS = g.ts;
@@ -458,6 +463,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
             }
         }
     }
+    pdl_trigger();
     if (sums) grid_reduce_store_f<1, kSpecThreads>(acc, partials, ticket, sums);
 }
 
@@ -480,6 +486,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
     k_spec_inv(const float2* __restrict__ spec, float* __restrict__ grid, SpecGeom g,
                const BoxState* __restrict__ bs, const float2* __restrict__ tw, int first,
                int pic) {
+    pdl_wait();
     extern __shared__ __align__(16) float2 sm[];
     constexpr int Ny = NY, H = HZ, Nzc = H + 1, Ls = plane_ls(H), PN = plane_n2(H);
     constexpr int zoff = Tw<2 * H>::off, step = Tw<2 * H>::stride;
@@ -567,6 +574,7 @@ __global__ void __launch_bounds__(kSpecThreads, 2)
                 for (int m = lane; m < H; m += 32) fin(r, m, m, sm[row0(r) + m]);
         }
     }
+    pdl_trigger();
 }
 
 // The k-space kernels are instantiated per x length (their register
@@ -748,27 +756,30 @@ int spectral_field_force(hpf_ctx* c, const float* type_scale, double* sums, cuda
     SpecScale sc;
     for (int t = 0; t < c->T; ++t) sc.s[t] = type_scale[t];
     const int ps = (int)plane_smem(c), ts = (int)tile_smem(c, g.W);
-    with_planes(c->n1, c->n2 / 2, [&](auto kf, auto, auto) {
-        kf<<<dim3(c->n0, c->T), kSpecThreads, ps, st>>>(c->d_acc, c->d_spec_phi, g, sc, c->d_box,
-                                                        c->d_tw, nullptr);
-        return HPF_OK;
-    });
-    HPF_LAUNCH_CHECK();
+    if (with_planes(c->n1, c->n2 / 2, [&](auto kf, auto, auto) {
+            return launch_pdl(kf, dim3(c->n0, c->T), kSpecThreads, ps, st, c->d_acc,
+                              c->d_spec_phi, g, sc, c->d_box, c->d_tw, nullptr) == cudaSuccess
+                       ? HPF_OK
+                       : HPF_ERR_CUDA;
+        }) != HPF_OK)
+        return HPF_ERR_CUDA;
     double* part = c->d_spec_ws;
     unsigned int* tick = reinterpret_cast<unsigned int*>(c->d_spec_ws + 4 * (size_t)c->spec_max_tiles);
     int r = with_kspace(c->n0, [&](auto kd, auto) {
-        kd<<<c->spec_tiles, kSpecThreads, ts, st>>>(c->d_spec_phi, c->d_spec, g, c->T, c->d_box,
-                                                    c->d_fun, c->d_tw, sums, part, tick);
-        return HPF_OK;
+        return launch_pdl(kd, c->spec_tiles, kSpecThreads, ts, st, c->d_spec_phi, c->d_spec, g,
+                          c->T, c->d_box, c->d_fun, c->d_tw, sums, part, tick) == cudaSuccess
+                   ? HPF_OK
+                   : HPF_ERR_CUDA;
     });
     if (r != HPF_OK) return r;
     HPF_LAUNCH_CHECK();
-    with_planes(c->n1, c->n2 / 2, [&](auto, auto ki, auto) {
-        ki<<<dim3(c->n0, 3 * c->T), kSpecThreads, ps, st>>>(c->d_spec, c->d_grid, g, c->d_box,
-                                                             c->d_tw, 0, 0);
-        return HPF_OK;
-    });
-    HPF_LAUNCH_CHECK();
+    if (with_planes(c->n1, c->n2 / 2, [&](auto, auto ki, auto) {
+            return launch_pdl(ki, dim3(c->n0, 3 * c->T), kSpecThreads, ps, st, c->d_spec,
+                              c->d_grid, g, c->d_box, c->d_tw, 0, 0) == cudaSuccess
+                       ? HPF_OK
+                       : HPF_ERR_CUDA;
+        }) != HPF_OK)
+        return HPF_ERR_CUDA;
     return HPF_OK;
 }
 
@@ -781,33 +792,34 @@ int spectral_pic(hpf_ctx* c, const SpecBufs& b, float four_pi_fac, bool want_psi
     SpecScale sc;
     sc.s[0] = 1.0f;
     const int ps = (int)plane_smem(c), ts = (int)tile_smem(c, g.W, true);
-    with_planes(c->n1, c->n2 / 2, [&](auto kf, auto, auto kr) {
-        if (real_in)
-            kr<<<dim3(c->n0, 1), kSpecThreads, ps, st>>>(nullptr, b.spec_phi, g, sc, c->d_box,
-                                                         c->d_tw, real_in);
-        else
-            kf<<<dim3(c->n0, 1), kSpecThreads, ps, st>>>(c->d_acc + (int64_t)c->T * c->M,
-                                                         b.spec_phi, g, sc, c->d_box, c->d_tw,
-                                                         nullptr);
-        return HPF_OK;
-    });
-    HPF_LAUNCH_CHECK();
+    if (with_planes(c->n1, c->n2 / 2, [&](auto kf, auto, auto kr) {
+            const cudaError_t e =
+                real_in ? launch_pdl(kr, dim3(c->n0, 1), kSpecThreads, ps, st, nullptr,
+                                     b.spec_phi, g, sc, c->d_box, c->d_tw, real_in)
+                        : launch_pdl(kf, dim3(c->n0, 1), kSpecThreads, ps, st,
+                                     c->d_acc + (int64_t)c->T * c->M, b.spec_phi, g, sc,
+                                     c->d_box, c->d_tw, nullptr);
+            return e == cudaSuccess ? HPF_OK : HPF_ERR_CUDA;
+        }) != HPF_OK)
+        return HPF_ERR_CUDA;
     double* part = b.ws;
     unsigned int* tick = reinterpret_cast<unsigned int*>(b.ws + 4 * (size_t)c->spec_max_tiles);
     int r = with_kspace(c->n0, [&](auto, auto kp) {
-        kp<<<c->spec_tiles_pic, kSpecThreads, ts, st>>>(b.spec_phi, b.spec, g, c->d_box, c->d_fun,
-                                                    four_pi_fac, c->d_tw, sums, part, tick,
-                                                    filter ? 1 : 0);
-        return HPF_OK;
+        return launch_pdl(kp, c->spec_tiles_pic, kSpecThreads, ts, st, b.spec_phi, b.spec, g,
+                          c->d_box, c->d_fun, four_pi_fac, c->d_tw, sums, part, tick,
+                          filter ? 1 : 0) == cudaSuccess
+                   ? HPF_OK
+                   : HPF_ERR_CUDA;
     });
     if (r != HPF_OK) return r;
     HPF_LAUNCH_CHECK();
     const int first = want_psi ? 0 : 1;
-    with_planes(c->n1, c->n2 / 2, [&](auto, auto ki, auto) {
-        ki<<<dim3(c->n0, 4 - first), kSpecThreads, ps, st>>>(b.spec, b.grid, g, c->d_box,
-                                                             c->d_tw, first, 1);
-        return HPF_OK;
-    });
-    HPF_LAUNCH_CHECK();
+    if (with_planes(c->n1, c->n2 / 2, [&](auto, auto ki, auto) {
+            return launch_pdl(ki, dim3(c->n0, 4 - first), kSpecThreads, ps, st, b.spec, b.grid,
+                              g, c->d_box, c->d_tw, first, 1) == cudaSuccess
+                       ? HPF_OK
+                       : HPF_ERR_CUDA;
+        }) != HPF_OK)
+        return HPF_ERR_CUDA;
     return HPF_OK;
 }
