@@ -990,6 +990,18 @@ def run_gpe(args):
     dev_ms = 1000.0 * float(np.median(times))
     iters = int(pm.gpe_iterations)
     W = gf.compute_field_energy_q_GPE(cfg, eps_g, None, dot)
+    line = {"metric": "PIC_Spectral_GPE solve time (update_field_force_q_GPE)",
+            "value": dev_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 1), "higher_is_better": False, "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "iterations": iters,
+            "ms_per_iteration": dev_ms / max(iters, 1),
+            "config": {"workload": "charged peptides 500k beads, box 40 nm, mesh 128^3, "
+                                   "3 types, dielectric 2/10/80",
+                       "timed": "wall time of one solve (densities resident), host "
+                                "synchronisations included"}}
+    if args.no_cpu_baseline:
+        print(json.dumps(line))
+        return 0
     # the FP64 oracle on the same inputs: filtered densities, then the solve
     names = cfg.unique_names
     chim = np.zeros((T, T))
@@ -1008,21 +1020,86 @@ def run_gpe(args):
     cpu_s = time.perf_counter() - t0
     f_ref = ref["forces"]
     f_rel = float(np.sqrt(np.mean((F.cpu().numpy() - f_ref) ** 2)) / np.sqrt(np.mean(f_ref ** 2)))
-    line = {"metric": "PIC_Spectral_GPE solve time (update_field_force_q_GPE)",
-            "value": dev_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps,
-            "warmup": max(args.warmup, 1), "higher_is_better": False, "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic", "iterations": iters,
-            "ms_per_iteration": dev_ms / max(iters, 1),
-            "accuracy": {"reference": "FP64 oracle (oracle/field.py:gpe_step) on the same "
-                                      "inputs", "force_rel_rms": f_rel,
-                         "energy_rel_err": abs(W - ref["energy"]) / abs(ref["energy"]),
-                         "oracle_iterations": int(ref["iterations"])},
-            "cpu_baseline": {"value": 1000.0 * cpu_s, "unit": "ms", "cores": 1, "kind": "port",
-                             "sample": "the whole solve, FP64 numpy oracle"},
-            "config": {"workload": "charged peptides 500k beads, box 40 nm, mesh 128^3, "
-                                   "3 types, dielectric 2/10/80",
-                       "timed": "wall time of one solve (densities resident), host "
-                                "synchronisations included"}}
+    line["accuracy"] = {"reference": "FP64 oracle (oracle/field.py:gpe_step) on the same "
+                                     "inputs", "force_rel_rms": f_rel,
+                        "energy_rel_err": abs(W - ref["energy"]) / abs(ref["energy"]),
+                        "oracle_iterations": int(ref["iterations"])}
+    line["cpu_baseline"] = {"value": 1000.0 * cpu_s, "unit": "ms", "cores": 1, "kind": "port",
+                            "sample": "the whole solve, FP64 numpy oracle"}
+    print(json.dumps(line))
+    return 0
+
+
+def run_trajectory(args):
+    """Trajectory and observable output (hymd/file_io.py:527-779 through
+    TrajectoryRecorder) on the default MD workload (500k charged peptides,
+    mesh 128^3): steps/s of the captured step replayed K times without
+    output, then with a frame every n_print = 10 steps (positions,
+    velocities and total forces in the caller's bead order, FP64 field and
+    electrostatic energies, pressure) copied to page-locked host memory on a
+    side stream and written to an in-memory H5MD tree while the next steps
+    run.  Host wall clock around the whole run, the last frame written."""
+    import tempfile
+    import time
+    import torch
+    from hymd_gb300 import file_io as fio
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    from hymd_gb300.trajectory import TrajectoryRecorder
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(0)
+    K, n_print = max(args.steps, 10), 10
+    s = systems.charged_peptides(seed=2)
+    cfg = s["config"]
+    cfg.n_steps, cfg.n_print = K, n_print
+    ham = get_hamiltonian(cfg)
+    md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham, topology=s["topology"],
+                 charges=s["charges"])
+    md.sort_particles()
+    md.couple(thermostat=True, seed=100, n_steps=2 * K + args.warmup + 8)
+    md.prime()
+    md.capture()
+    md.run(max(args.warmup, 3))
+    torch.cuda.synchronize()
+
+    def timed(with_output):
+        rec = None
+        if with_output:
+            out = fio.OutDataset(tempfile.mkdtemp(), cfg, backend="memory")
+            topo = s["topology"]
+            fio.store_static(out, list(range(md.n)), s["names"], s["types"], np.arange(md.n),
+                             cfg, topo[0], topo[1], molecules=s["molecules"], velocity_out=True,
+                             force_out=True, charges=s["charges"])
+            rec = TrajectoryRecorder(md, out, ham, velocity_out=True, force_out=True,
+                                     pressure=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for step in range(1, K + 1):
+            md.run(1)
+            if rec is not None and step % n_print == 0:
+                rec.record(step)
+                rec.drain()
+        if rec is not None:
+            rec.close()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, (rec.written if rec is not None else 0)
+
+    t_plain, _ = timed(False)
+    t_out, frames = timed(True)
+    line = {"metric": "MD steps/s with trajectory output every n_print steps",
+            "value": K / t_out, "unit": "steps/s", "n_gpus": 1, "steps": K,
+            "warmup": max(args.warmup, 3), "higher_is_better": True, "vs_baseline": None,
+            "dtype": "f32 (f64 energies)", "data": "synthetic",
+            "without_output": K / t_plain, "frames": frames, "n_print": n_print,
+            "ms_per_frame_overhead": 1000.0 * (t_out - t_plain) / max(frames, 1),
+            "frame_bytes_d2h": int(3 * 12 * md.n + 2 * 32 * 8),
+            "config": {"workload": WORKLOADS["peptide500k"][0],
+                       "output": "positions, velocities, forces (caller order), energies, "
+                                 "pressure; in-memory H5MD tree",
+                       "timed": "host wall clock over the K steps, output drained and closed"}}
     print(json.dumps(line))
     return 0
 
@@ -1306,6 +1383,8 @@ def main():
     ap.add_argument("--reverse-steps", type=int, default=200)
     ap.add_argument("--locality", action="store_true",
                     help="diagnostic: step time against the age of the bead order")
+    ap.add_argument("--trajectory", action="store_true",
+                    help="MD steps/s with trajectory output every 10 steps (one JSON line)")
     ap.add_argument("--gpe", action="store_true",
                     help="PIC_Spectral_GPE solve time on the 500k peptides (one JSON line)")
     ap.add_argument("--topology", action="store_true",
@@ -1321,6 +1400,8 @@ def main():
         return run_topology(args)
     if args.gpe:
         return run_gpe(args)
+    if args.trajectory:
+        return run_trajectory(args)
     if args.locality:
         return run_locality(args)
     if args.impl == "reference":

@@ -37,6 +37,10 @@ class Dataset:
     def __init__(self, name, shape, dtype):
         self.name = name
         self.value = np.zeros(shape, dtype=np.dtype(dtype))
+        # commit the pages now (zeros are mapped lazily), so that the frames
+        # written during the run do not fault them in one by one
+        if self.value.dtype.kind in "fiu":
+            self.value.fill(0)
         self.attrs = _Attrs()
 
     @property
@@ -345,6 +349,20 @@ def store_static(h5md, rank_range, names, types, indices, config, bonds_2_atom1,
         resid[indices[order]] = molecules
 
 
+# float64 copies of a frame's particle arrays, kept between frames: fresh
+# allocations of this size are mapped anew each time and fault in page by
+# page
+_F64_SCRATCH = {}
+
+
+def _as_f64(x, slot):
+    buf = _F64_SCRATCH.get(slot)
+    if buf is None or buf.shape != x.shape:
+        buf = _F64_SCRATCH[slot] = np.empty(x.shape, dtype=np.float64)
+    np.copyto(buf, x)
+    return buf
+
+
 def store_data(h5md, step, frame, indices, positions, velocities, forces, box_size, temperature,
                pressure, kinetic_energy, bond2_energy, bond3_energy, bond4_energy, field_energy,
                field_q_energy, plumed_bias, time_step, config, velocity_out=False,
@@ -382,25 +400,44 @@ def store_data(h5md, step, frame, indices, positions, velocities, forces, box_si
     for d in times:
         d[frame] = t
     indices = np.asarray(indices)
-    order = np.argsort(indices)
     positions = np.asarray(positions)
     velocities = np.asarray(velocities)
     forces = np.asarray(forces)
-    h5md.positions[frame, indices[order]] = positions[order]
+    # the reference sorts the rows by global index before a fancy-indexed
+    # write; rows that already hold consecutive ascending indices (one GPU
+    # holding the whole system, in the caller's order) are a plain slice
+    n_loc = indices.shape[0]
+    if n_loc and np.array_equal(indices, np.arange(indices[0], indices[0] + n_loc)):
+        rows = slice(int(indices[0]), int(indices[0]) + n_loc)
+        put = lambda dset, x: dset.__setitem__((frame, rows), x)  # noqa: E731
+    else:
+        order = np.argsort(indices)
+        put = lambda dset, x: dset.__setitem__((frame, indices[order]), x[order])  # noqa: E731
+    put(h5md.positions, positions)
     if velocity_out:
-        h5md.velocities[frame, indices[order]] = velocities[order]
+        put(h5md.velocities, velocities)
     if force_out:
-        h5md.forces[frame, indices[order]] = forces[order]
+        put(h5md.forces, forces)
     if charge_out:
         h5md.field_q_energy[frame] = field_q_energy
     if plumed_out:
         h5md.plumed_bias[frame] = plumed_bias
     potential = bond2_energy + bond3_energy + bond4_energy + field_energy + field_q_energy
-    p64 = positions.astype(np.float64, copy=False)
-    v64 = velocities.astype(np.float64, copy=False)
-    total_momentum = config.mass * np.sum(v64, axis=0)
-    angular_momentum = config.mass * np.sum(np.cross(p64, v64), axis=0)
-    torque = config.mass * np.sum(np.cross(p64, forces.astype(np.float64, copy=False)), axis=0)
+    # sums over particles in float64 (the reference adds float32 arrays in
+    # float32); sum(a x b) from column dot products, without the N x 3 cross
+    p64, v64, f64 = (_as_f64(x, k) for k, x in enumerate((positions, velocities, forces)))
+    p = [p64[:, d] for d in range(3)]
+    v = [v64[:, d] for d in range(3)]
+    fc = [f64[:, d] for d in range(3)]
+
+    def cross_sum(a, b):
+        return np.array([np.dot(a[1], b[2]) - np.dot(a[2], b[1]),
+                         np.dot(a[2], b[0]) - np.dot(a[0], b[2]),
+                         np.dot(a[0], b[1]) - np.dot(a[1], b[0])])
+
+    total_momentum = config.mass * np.array([np.sum(v[d]) for d in range(3)])
+    angular_momentum = config.mass * cross_sum(p, v)
+    torque = config.mass * cross_sum(p, fc)
     total = kinetic_energy + potential
     h5md.total_energy[frame] = total
     h5md.potential_energy[frame] = potential

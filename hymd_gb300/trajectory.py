@@ -7,15 +7,21 @@ bonded energies and virials of the last inner step, the thermostat work and
 the box, and device-to-device snapshots of positions, velocities and the
 total force (field + bonded + electrostatic, as main.py:1403-1413 sums them)
 in the caller's bead order.  A side stream then copies the slot to
-page-locked host memory while the next steps run.  `drain()` writes the
-frames whose copies have finished with file_io.store_data; `close()` waits
-for the rest.  Slots are reused round-robin: with `depth` slots in flight a
-record() waits only if the oldest snapshot has not reached the host yet.
+page-locked host memory while the next steps run, and (threaded=True, the
+default) a writer thread passes each frame to file_io.store_data as soon as
+its copy has finished, so that neither the device nor the thread launching
+the steps waits for the host-side write (numpy releases the interpreter lock
+in its copies and dot products).  Without the thread, `drain()` writes the
+frames whose copies have finished.  `close()` waits for the rest.  Slots are
+reused round-robin: with `depth` slots in flight a record() waits only if
+the oldest snapshot has not been written yet.
 
 Per frame it costs one FP64 energy evaluation and ~3 copies of N x 3 floats
 on the device; the step graph itself is untouched.
 """
 import collections
+import queue
+import threading
 
 import numpy as np
 import torch
@@ -38,6 +44,8 @@ class _Slot:
         self.hsums = torch.empty(32, dtype=torch.float64, pin_memory=True)
         self.hmisc = torch.empty(32, dtype=torch.float64, pin_memory=True)
         self.done = torch.cuda.Event()
+        self.written = threading.Event()
+        self.written.set()
         self.step = self.frame = None
 
 
@@ -50,7 +58,7 @@ class TrajectoryRecorder:
     18-vector (default: config.pressure or a barostat, as main.py does)."""
 
     def __init__(self, md, out, hamiltonian, indices=None, velocity_out=False, force_out=False,
-                 pressure=None, depth=3, dump_per_particle=False):
+                 pressure=None, depth=3, dump_per_particle=False, threaded=True):
         self.md = md
         self.out = out
         self.cfg = cfg = md.config
@@ -73,10 +81,41 @@ class TrajectoryRecorder:
         self.ws = _lib.new_workspace(dev)
         self.copy_stream = torch.cuda.Stream(device=dev)
         self.written = 0
+        self._error = None
+        self._queue = queue.Queue() if threaded else None
+        self._thread = None
+        if threaded:
+            self._thread = threading.Thread(target=self._writer, name="hpf-trajectory",
+                                            daemon=True)
+            self._thread.start()
+
+    def _writer(self):
+        while True:
+            s = self._queue.get()
+            if s is None:
+                self._queue.task_done()
+                return
+            try:
+                if self._error is None:
+                    self._write(s, block=True)
+            except BaseException as e:  # surfaced by the next record/drain/close
+                self._error = e
+            finally:
+                s.written.set()
+                self._queue.task_done()
+
+    def _check(self):
+        if self._error is not None:
+            e, self._error = self._error, None
+            raise RuntimeError("trajectory writer failed") from e
 
     def _free(self):
+        self._check()
         s = self.slots[self.next]
-        if s.step is not None:  # still holds a snapshot: write it first
+        if self._queue is not None:
+            s.written.wait()  # the writer thread is done with this slot
+            self._check()
+        elif s.step is not None:  # still holds a snapshot: write it first
             while self.pending and self.pending[0] is not s:
                 self._write(self.pending.popleft(), block=True)
             if self.pending:
@@ -135,11 +174,22 @@ class TrajectoryRecorder:
                 d.record_stream(self.copy_stream)
         s.step = int(step)
         s.frame = int(step) // int(self.cfg.n_print) if frame is None else int(frame)
-        self.pending.append(s)
+        if self._queue is not None:
+            s.written.clear()
+            self._queue.put(s)
+        else:
+            self.pending.append(s)
 
     def drain(self, block=False):
         """Write the snapshots whose host copies are complete (all of them
-        with block=True), oldest first.  Returns the number written."""
+        with block=True), oldest first.  Returns the number written.  With
+        the writer thread the frames are written as they arrive: drain()
+        only waits for them (block=True) and returns 0."""
+        if self._queue is not None:
+            if block:
+                self._queue.join()
+            self._check()
+            return 0
         k = 0
         while self.pending:
             s = self.pending[0]
@@ -151,6 +201,10 @@ class TrajectoryRecorder:
 
     def close(self):
         self.drain(block=True)
+        if self._thread is not None:
+            self._queue.put(None)
+            self._thread.join()
+            self._thread = None
 
     def _write(self, s, block):
         s.done.synchronize()
