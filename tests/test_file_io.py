@@ -124,3 +124,34 @@ def test_frame_count():
     assert fio.n_output_frames(100, 1) == 101
     assert fio.n_output_frames(100, 10) == 11
     assert fio.n_output_frames(1, 1) == 2
+
+
+def test_store_data_contiguous_rows_match_sorted_write(tmp_path):
+    """Rows that already hold the consecutive ascending global indices are
+    written as one slice; the frames equal those of the reference's
+    sort-then-scatter write of the same rows in another order, and the
+    momentum sums agree to summation order."""
+    cfg = _config()
+    idx = FIX["inputs/indices"]
+    order = np.argsort(idx)
+    box = np.array([10.0, 10.0, 10.0])
+    outs = []
+    for k, (rows, ix) in enumerate(((order, idx[order]), (FIX["frames/perm"], None))):
+        out = fio.OutDataset(str(tmp_path / str(k)), cfg, backend="memory")
+        fio.store_static(out, list(range(len(idx))), FIX["inputs/names"], FIX["inputs/types"],
+                         idx, cfg, FIX["inputs/bond_from"], FIX["inputs/bond_to"],
+                         molecules=FIX["inputs/molecules"], velocity_out=True, force_out=True)
+        ix = idx[rows] if ix is None else ix
+        for frame, step in enumerate(FIX["frames/steps"]):
+            g = lambda key: FIX[f"frames/{frame}/{key}"][rows]  # noqa: E731
+            fio.store_data(out, int(step), frame, ix, g("pos"), g("vel"), g("frc"), box, 300.0,
+                           0.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.3, cfg,
+                           velocity_out=True, force_out=True)
+        outs.append(out)
+    assert np.array_equal(idx[order], np.arange(idx[order][0], idx[order][0] + len(idx)))
+    a, b = outs
+    for name in ("positions", "velocities", "forces"):
+        assert np.array_equal(getattr(a, name)[:], getattr(b, name)[:]), name
+    for name in ("total_momentum", "angular_momentum", "torque"):
+        np.testing.assert_allclose(getattr(a, name)[:], getattr(b, name)[:], rtol=1e-12,
+                                   atol=1e-12, err_msg=name)
