@@ -5,7 +5,7 @@ output.
   restraint between two beads of a chain) against the oracle rRESPA loop
   with the same bias applied as hymd/main.py:808-812, 1097-1154 does: two
   outer steps, the same tolerances as the unbiased loop test.
-* TrajectoryRecorder: frames every n_print steps of a thermostatted membrane
+* TrajectoryRecorder (with and without its writer thread): frames every n_print steps of a thermostatted membrane
   run, written through file_io.store_data into the in-memory H5 tree, against
   the state and the drop-in energies / pressure taken synchronously at the
   same steps.
@@ -88,7 +88,8 @@ def test_bias_in_md_loop_matches_oracle(tmp_path):
     md.check_errors()
 
 
-def test_trajectory_recorder_frames(tmp_path):
+@pytest.mark.parametrize("threaded", [True, False])
+def test_trajectory_recorder_frames(tmp_path, threaded):
     from hymd_gb300 import _lib, systems
     from hymd_gb300 import file_io as fio
     from hymd_gb300.field import energy_fp64
@@ -111,7 +112,7 @@ def test_trajectory_recorder_frames(tmp_path):
     fio.store_static(out, list(range(n)), s["names"], s["types"], np.arange(n), cfg, topo[0],
                      topo[1], molecules=s["molecules"], velocity_out=True, force_out=True)
     rec = TrajectoryRecorder(md, out, ham, velocity_out=True, force_out=True, pressure=True,
-                             depth=2)
+                             depth=2, threaded=threaded)
     want = {}
 
     def expect(step):
