@@ -5,10 +5,10 @@ output.
   restraint between two beads of a chain) against the oracle rRESPA loop
   with the same bias applied as hymd/main.py:808-812, 1097-1154 does: two
   outer steps, the same tolerances as the unbiased loop test.
-* TrajectoryRecorder (with and without its writer thread): frames every n_print steps of a thermostatted membrane
-  run, written through file_io.store_data into the in-memory H5 tree, against
-  the state and the drop-in energies / pressure taken synchronously at the
-  same steps.
+* TrajectoryRecorder (with and without its writer thread): frames every
+  n_print steps of a thermostatted membrane run, written through
+  file_io.store_data into the in-memory H5 tree, against the state and the
+  drop-in energies / pressure taken synchronously at the same steps.
 """
 import os
 
