@@ -18,6 +18,7 @@ device without stalling the step.
 import getpass
 import logging
 import os
+import threading
 
 import numpy as np
 
@@ -349,16 +350,19 @@ def store_static(h5md, rank_range, names, types, indices, config, bonds_2_atom1,
         resid[indices[order]] = molecules
 
 
-# float64 copies of a frame's particle arrays, kept between frames: fresh
+# float64 copies of a frame's particle arrays, kept between frames (fresh
 # allocations of this size are mapped anew each time and fault in page by
-# page
-_F64_SCRATCH = {}
+# page); one set per thread, since trajectory writer threads call store_data
+_F64_SCRATCH = threading.local()
 
 
 def _as_f64(x, slot):
-    buf = _F64_SCRATCH.get(slot)
+    bufs = getattr(_F64_SCRATCH, "bufs", None)
+    if bufs is None:
+        bufs = _F64_SCRATCH.bufs = {}
+    buf = bufs.get(slot)
     if buf is None or buf.shape != x.shape:
-        buf = _F64_SCRATCH[slot] = np.empty(x.shape, dtype=np.float64)
+        buf = bufs[slot] = np.empty(x.shape, dtype=np.float64)
     np.copyto(buf, x)
     return buf
 

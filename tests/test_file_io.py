@@ -155,3 +155,47 @@ def test_store_data_contiguous_rows_match_sorted_write(tmp_path):
     for name in ("total_momentum", "angular_momentum", "torque"):
         np.testing.assert_allclose(getattr(a, name)[:], getattr(b, name)[:], rtol=1e-12,
                                    atol=1e-12, err_msg=name)
+
+
+def test_store_data_concurrent_threads(tmp_path):
+    """store_data from two threads at once (trajectory writer threads of two
+    runs): each tree gets its own frames and momentum sums, the same as
+    written one after the other."""
+    import threading
+    cfg = _config()
+    idx = FIX["inputs/indices"]
+    order = np.argsort(idx)
+    box = np.array([10.0, 10.0, 10.0])
+    steps = FIX["frames/steps"]
+    # the archive is read here, once: an npz file is not safe to read from
+    # two threads
+    data = {(f, k): FIX[f"frames/{f}/{k}"][order] for f in range(len(steps))
+            for k in ("pos", "vel", "frc")}
+
+    def write(out, scale, reps):
+        for _ in range(reps):
+            for frame, step in enumerate(steps):
+                g = lambda key: scale * data[(frame, key)]  # noqa: E731
+                fio.store_data(out, int(step), frame, idx[order], g("pos"), g("vel"), g("frc"),
+                               box, 300.0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.3, cfg,
+                               velocity_out=True, force_out=True)
+
+    def new_out(tag):
+        out = fio.OutDataset(str(tmp_path / tag), cfg, backend="memory")
+        fio.store_static(out, list(range(len(idx))), FIX["inputs/names"], FIX["inputs/types"],
+                         idx, cfg, FIX["inputs/bond_from"], FIX["inputs/bond_to"],
+                         molecules=FIX["inputs/molecules"], velocity_out=True, force_out=True)
+        return out
+
+    seq = [new_out("s1"), new_out("s2")]
+    write(seq[0], 1.0, 1)
+    write(seq[1], 2.0, 1)
+    par = [new_out("p1"), new_out("p2")]
+    th = [threading.Thread(target=write, args=(par[k], 1.0 + k, 50)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for a, b in zip(seq, par):
+        for name in ("positions", "total_momentum", "angular_momentum", "torque"):
+            assert np.array_equal(getattr(a, name)[:], getattr(b, name)[:]), name
