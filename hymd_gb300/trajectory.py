@@ -111,6 +111,8 @@ class TrajectoryRecorder:
 
     def _free(self):
         self._check()
+        if self._queue is not None and self._thread is None:
+            raise RuntimeError("TrajectoryRecorder.record() after close()")
         s = self.slots[self.next]
         if self._queue is not None:
             s.written.wait()  # the writer thread is done with this slot

@@ -137,6 +137,9 @@ def test_trajectory_recorder_frames(tmp_path, threaded):
         rec.drain()
     rec.close()
     assert rec.written == 4
+    if threaded:
+        with pytest.raises(RuntimeError):
+            rec.record(cfg.n_steps + cfg.n_print)
     for frame, step in enumerate(sorted(want)):
         w = want[step]
         assert out.positions_step[frame] == step
