@@ -56,6 +56,19 @@ WORKLOADS = {
 }
 
 
+def max_over_ranks(x, ws, device):
+    """The largest of the ranks' values of x (a timed region's duration: the
+    whole job is as slow as its slowest rank); x itself on one rank.  The
+    process group is NCCL in the GPU arm, gloo in the CPU tests."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -666,12 +679,8 @@ def run_gpu(args):
             b.record(st)
         torch.cuda.synchronize()
     barrier()
-    ms = sum(a.elapsed_time(b) for a, m, b in evs)
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, m, b in evs), ws, dev)
     respa_ms = sum(a.elapsed_time(m) for a, m, b in evs) / args.steps
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     ms_step = ms / args.steps
     sps = 1000.0 / ms_step
     md.check_errors()
@@ -694,6 +703,7 @@ def run_gpu(args):
             b0.synchronize()
             tot += a0.elapsed_time(b0)
         md.check_errors()
+        tot = max_over_ranks(tot, ws, dev)
         aged = {"steps_before": args.warmup + args.steps + 1000,
                 "value": 1000.0 * args.steps / tot * ws, "unit": "steps/s",
                 "ms_per_step": tot / args.steps,
@@ -701,9 +711,11 @@ def run_gpu(args):
 
     # ---- end to end, host wall clock --------------------------------------
     e2e_sps, e2e_h2d, e2e_d2h = e2e_wall(md, flush, torch, args.steps)
+    e2e_sps = 1.0 / max_over_ranks(1.0 / e2e_sps, ws, dev)  # the slowest rank's rate
     dropin = None
     if not args.no_dropin:
         d_sps, d_h2d, d_d2h = e2e_dropin(s, ham, torch, dev, max(3, min(args.steps, 20)))
+        d_sps = 1.0 / max_over_ranks(1.0 / d_sps, ws, dev)
         dropin = {"value": d_sps * ws, "unit": "steps/s", "h2d_bytes_per_step": d_h2d,
                   "d2h_bytes_per_step": d_d2h,
                   "path": "main.py-style outer step over the drop-in calls (integrate_*, "
@@ -831,6 +843,9 @@ def run_replicas(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     sys_ = systems.replica_set(n_replicas=64, seed=5 + rank)
     rb = ReplicaBatch(sys_, device=dev, seed=100 + rank)
     rb.prime()
@@ -852,10 +867,10 @@ def run_replicas(args):
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in evs) / args.steps
 
-    seq_ms = timed(lambda: rb.run_sequential(1))
+    seq_ms = max_over_ranks(timed(lambda: rb.run_sequential(1)), ws, dev)
     k = rb.tune_streams()
     with ClockSampler(local) as clk:
-        bat_ms = timed(lambda: rb.run(1))
+        bat_ms = max_over_ranks(timed(lambda: rb.run(1)), ws, dev)
     rb.check_errors()
     R = len(rb.replicas)
     line = {"metric": "aggregate replica MD steps/s (64 replicas, one graph per step)",
