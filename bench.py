@@ -1119,6 +1119,71 @@ def run_trajectory(args):
     return 0
 
 
+def run_plumed(args):
+    """The PLUMED bias coupling (hymd/plumed.py:11-235 through PlumedBias and
+    RespaMD.set_bias) on the default MD workload (500k charged peptides):
+    steps/s with a bias evaluated after every field step (a DISTANCE
+    restraint between two beads of the first chain, as the reference's PLUMED
+    test input) against the same steps without it.  py-plumed is not
+    installed: the PLUMED kernel is the stand-in of the tests
+    (tests/plumed_fake.py), so the time is this package's coupling: the
+    positions and forces copied to the host every step, the bias force copied
+    back into the outer kicks, and eager launches (a biased run is not
+    captured in a graph)."""
+    import tempfile
+    import time
+    import torch
+    from hymd_gb300 import systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from hymd_gb300.md import RespaMD
+    from hymd_gb300.plumed import PlumedBias
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests"))
+    from plumed_fake import FakePlumed
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(0)
+    K = max(args.steps, 10)
+    s = systems.charged_peptides(seed=2)
+    cfg = s["config"]
+    ham = get_hamiltonian(cfg)
+
+    def make(bias):
+        md = RespaMD(s["positions"], s["velocities"], s["types"], cfg, ham,
+                     topology=s["topology"], charges=s["charges"])
+        md.couple(thermostat=True, seed=100, n_steps=K + args.warmup + 8)
+        if bias:
+            d = tempfile.mkdtemp()
+            dat = os.path.join(d, "plumed.dat")
+            with open(dat, "w") as f:
+                f.write("d: DISTANCE ATOMS=3,17\nRESTRAINT ARG=d KAPPA=4000.0 AT=0.8\n")
+            md.set_bias(PlumedBias(cfg, dat, os.path.join(d, "log"), kernel=FakePlumed()))
+        md.prime()
+        return md
+
+    def timed(md):
+        for _ in range(max(args.warmup, 3)):
+            md.step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(K):
+            md.step()
+        torch.cuda.synchronize()
+        return K / (time.perf_counter() - t0)
+
+    plain = timed(make(False))
+    biased = timed(make(True))
+    line = {"metric": "MD steps/s with a PLUMED bias every step", "value": biased,
+            "unit": "steps/s", "n_gpus": 1, "steps": K, "warmup": max(args.warmup, 3),
+            "higher_is_better": True, "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "without_bias_eager": plain, "ms_per_step_overhead": 1000.0 * (1.0 / biased - 1.0 / plain),
+            "config": {"workload": WORKLOADS["peptide500k"][0],
+                       "bias": "DISTANCE of beads 3 and 17 + RESTRAINT (stand-in PLUMED kernel)",
+                       "timed": "host wall clock, eager steps (a bias runs on the host)"}}
+    print(json.dumps(line))
+    return 0
+
+
 def run_reverse(args):
     """Reverse mode on the membrane recipe scaled to 1.3M beads (54 nm box,
     mesh 128^3): the gradient with respect to chi of the MSE between the
@@ -1398,6 +1463,8 @@ def main():
     ap.add_argument("--reverse-steps", type=int, default=200)
     ap.add_argument("--locality", action="store_true",
                     help="diagnostic: step time against the age of the bead order")
+    ap.add_argument("--plumed", action="store_true",
+                    help="MD steps/s with a PLUMED bias every step (one JSON line)")
     ap.add_argument("--trajectory", action="store_true",
                     help="MD steps/s with trajectory output every 10 steps (one JSON line)")
     ap.add_argument("--gpe", action="store_true",
@@ -1417,6 +1484,8 @@ def main():
         return run_gpe(args)
     if args.trajectory:
         return run_trajectory(args)
+    if args.plumed:
+        return run_plumed(args)
     if args.locality:
         return run_locality(args)
     if args.impl == "reference":

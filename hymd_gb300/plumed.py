@@ -27,6 +27,17 @@ def _host(x, dtype=np.double):
     return np.asarray(x, dtype=dtype)
 
 
+def _host_raw(x):
+    """x on the host as a numpy array in its own dtype (no conversion)."""
+    try:
+        import torch
+        if isinstance(x, torch.Tensor):
+            return x.detach().cpu().numpy()
+    except ImportError:  # pragma: no cover
+        pass
+    return np.asarray(x)
+
+
 class PlumedBias:
     """PLUMED handler (hymd/plumed.py:11-235): construct once, then per step
     prepare() (positions, current forces; returns whether PLUMED needs the
@@ -104,14 +115,20 @@ class PlumedBias:
         returns True if PLUMED asks for the potential energy."""
         if self.verbose > 1:
             log.info("Setting PLUMED pointers for step %d", step)
-        # copies, as the reference's astype(np.double) makes them: PLUMED
-        # writes into the force array
-        self.plumed_forces = np.array(_host(forces).ravel(), dtype=np.double, copy=True)
-        self.charges = np.array(_host(charges), dtype=np.double, copy=True)
-        self.positions = np.array(_host(positions).ravel(), dtype=np.double, copy=True)
+        # float64 copies, as the reference's astype(np.double) makes them
+        # (PLUMED adds the bias into the force array), held in buffers that
+        # persist between steps: fresh arrays of this size fault their pages
+        # in every step
+        f_in = _host_raw(forces)
+        self._forces_in = self._copy("_forces_in", f_in)
+        self.plumed_forces = self._copy("_plumed_f", f_in)
+        self.charges = self._copy("_charges", _host_raw(charges))
+        self.positions = self._copy("_positions", _host_raw(positions))
         idx = np.ascontiguousarray(_host(indices, np.intc))
         needs_energy = np.zeros(1, np.intc)
-        masses = np.full(idx.shape[0], config.mass, dtype=np.double)
+        masses = getattr(self, "_masses", None)
+        if masses is None or masses.shape[0] != idx.shape[0] or masses[0] != config.mass:
+            masses = self._masses = np.full(idx.shape[0], config.mass, dtype=np.double)
         box = np.diag(_host(config.box_size)).astype(np.double)
         k = self.plumed_obj
         k.cmd("setAtomsNlocal", idx.shape[0])
@@ -124,9 +141,19 @@ class PlumedBias:
         k.cmd("setBox", box)
         k.cmd("prepareCalc")
         k.cmd("isEnergyNeeded", needs_energy)
-        self._shape = tuple(_host(forces).shape)
+        self._shape = tuple(f_in.shape)
         self.ready = True
         return bool(needs_energy[0] != 0)
+
+    def _copy(self, name, x):
+        """x flattened into the float64 buffer `name` (allocated on first use
+        or when the size changes)."""
+        buf = getattr(self, name, None)
+        if buf is None or buf.shape[0] != x.size:
+            buf = np.empty(x.size, dtype=np.double)
+            setattr(self, name, buf)
+        np.copyto(buf, x.reshape(-1))
+        return buf
 
     def calc(self, forces, poteng):
         """Run PLUMED on the prepared step; returns (bias forces (N, 3), bias
@@ -142,12 +169,13 @@ class PlumedBias:
         k.cmd("setEnergy", poteng)
         k.cmd("performCalc")
         k.cmd("getBias", self.plumed_bias)
-        if np.isnan(self.plumed_forces).any():
+        # min propagates NaN: NaN exactly when an element is (no mask array)
+        if self.plumed_forces.size and np.isnan(np.min(self.plumed_forces)):
             msg = ("Forces returned by PLUMED are not valid. It means there's a NaN in the "
                    "computed forces, and your input should be checked. ")
             log.error(msg)
             raise RuntimeError(msg)
-        bias_forces = (self.plumed_forces - _host(forces).ravel()).reshape(self._shape)
+        bias_forces = (self.plumed_forces - self._forces_in).reshape(self._shape)
         if self.verbose > 1:
             log.info("Done calculating PLUMED forces")
         self.ready = False

@@ -16,6 +16,16 @@ tests/test_plumed.py.
 import numpy as np
 
 
+class _Local:
+    """local[g]: the row of global index g."""
+
+    def __init__(self, inv):
+        self.inv = inv
+
+    def __getitem__(self, g):
+        return int(self.inv[g])
+
+
 class FakePlumed:
     def __init__(self):
         self.p = {}
@@ -64,7 +74,11 @@ class FakePlumed:
         x = np.asarray(self.p["setPositions"]).reshape(n, 3)
         f = self.p["setForces"].reshape(n, 3)  # a view: PLUMED adds into it
         box = np.diag(np.asarray(self.p["setBox"]).reshape(3, 3))
-        local = {int(g): i for i, g in enumerate(gat)}
+        # local row of a global index (an inverse array: the runs hold up to
+        # millions of atoms)
+        inv = np.full(int(gat.max()) + 1 if n else 1, -1, dtype=np.int64)
+        inv[gat] = np.arange(n)
+        local = _Local(inv)
         step = int(self.p["setStep"])
         time = step * float(self.p["setTimestep"])
         values, grads = {}, {}
