@@ -120,7 +120,6 @@ class PlumedBias:
         # persist between steps: fresh arrays of this size fault their pages
         # in every step
         f_in = _host_raw(forces)
-        self._forces_in = self._copy("_forces_in", f_in)
         self.plumed_forces = self._copy("_plumed_f", f_in)
         self.charges = self._copy("_charges", _host_raw(charges))
         self.positions = self._copy("_positions", _host_raw(positions))
@@ -175,7 +174,8 @@ class PlumedBias:
                    "computed forces, and your input should be checked. ")
             log.error(msg)
             raise RuntimeError(msg)
-        bias_forces = (self.plumed_forces - self._forces_in).reshape(self._shape)
+        # the forces given to calc (float32 inputs widen exactly to float64)
+        bias_forces = (self.plumed_forces - _host_raw(forces).reshape(-1)).reshape(self._shape)
         if self.verbose > 1:
             log.info("Done calculating PLUMED forces")
         self.ready = False
