@@ -1,6 +1,7 @@
 """Parity at the benchmark configurations, full size: the 10k-bead melt
 (mesh 32^3), the 162k-bead membrane (64^3, 5 types) and the 500k-bead charged
-peptides (128^3, PIC_Spectral, cosine + combined bending-torsion dihedrals).
+peptides (128^3, PIC_Spectral, cosine + combined bending-torsion dihedrals);
+and the same peptides under PIC_Spectral_GPE (the bench's GPE workload).
 
 For each: one field evaluation through the drop-in API (update_field,
 compute_field_force, compute_field_and_kinetic_energy, comp_pressure; with
@@ -134,3 +135,60 @@ def test_full_size_field_and_bonded_match_oracle(workload):
     for idx in (b2a, b2b, b3a, b3b, b3c, b4a, b4b, b4c, b4d):
         sel[np.asarray(idx, np.int64)] = True
     assert rel_rms(fb.cpu().numpy()[sel], want[sel]) < FORCE_RTOL
+
+
+def test_full_size_gpe_matches_oracle():
+    """PIC_Spectral_GPE at the benchmark size: the 500k-bead charged peptides
+    on 128^3 (the fused spectral passes and the loop graph), dielectric
+    2 / 10 / 80 for BB / SC / W, max_diff to 1e-6, against the FP64 oracle's
+    solve of the same inputs: the same iteration count, forces within 1e-5
+    relative RMS (FP32 transforms through the iterative solve), energy within
+    1e-5."""
+    from hymd_gb300 import field as gf, systems
+    from hymd_gb300.hamiltonian import get_hamiltonian
+    from oracle import field as of
+    from oracle import hamiltonian as oh
+    s = systems.charged_peptides(seed=2)
+    cfg = s["config"]
+    cfg.coulombtype = "PIC_Spectral_GPE"
+    cfg.dielectric_type = [2.0, 10.0, 80.0]
+    cfg.conv_crit, cfg.pol_mixing, cfg.convergence_type = 1e-6, 0.6, "max_diff"
+    T = cfg.n_types
+    ham = get_hamiltonian(cfg)
+    pm, fl, ecl, cl = gf.initialize_pm(None, cfg)
+    assert pm.spectral == "fused"
+    phi, phi_fourier, force_on_grid, v_ext_fourier, v_ext, phi_transfer, phi_lap = fl
+    phi_q, phi_q_fourier, psi, elec_field = ecl
+    (phi_eps, phi_eps_fourier, phi_eta, phi_eta_fourier, phi_pol, phi_pol_prev, elec_dot,
+     elec_field_contrib, Vbar_elec, Vbar_elec_fourier, force_mesh_elec,
+     force_mesh_elec_fourier) = cl
+    R = torch.as_tensor(s["positions"], device="cuda")
+    Ty = torch.as_tensor(s["types"], device="cuda")
+    Q = torch.as_tensor(s["charges"], device="cuda")
+    gf.update_field(phi, phi_lap, phi_transfer, None, force_on_grid, ham, pm, R, Ty, cfg, v_ext,
+                    phi_fourier, v_ext_fourier, cfg.m)
+    F = torch.zeros_like(R)
+    _, eps_g, dot = gf.update_field_force_q_GPE(
+        None, phi, Ty, Q, phi_q, phi_q_fourier, phi_eps, phi_eps_fourier, phi_eta,
+        phi_eta_fourier, phi_pol_prev, phi_pol, elec_field, F, elec_field_contrib, psi,
+        Vbar_elec, Vbar_elec_fourier, force_mesh_elec, force_mesh_elec_fourier, ham, None, None,
+        pm, R, cfg)
+    W = gf.compute_field_energy_q_GPE(cfg, eps_g, None, dot)
+    names = cfg.unique_names
+    chim = np.zeros((T, T))
+    for c in cfg.chi:
+        i, j = names.index(c.atom_1), names.index(c.atom_2)
+        chim[i, j] = chim[j, i] = c.interaction_energy
+    fun = oh.quadratic_from_params("DefaultWithChi", T, cfg.kappa, cfg.rho0, cfg.a, chim)
+    ref_field = of.update_field(s["positions"].astype(np.float64), s["types"], T, cfg.mesh(),
+                                cfg.box(), cfg.m, fun, cfg.sigma)
+    nshape = tuple(cfg.mesh())
+    state = dict(phi_eps=np.zeros(nshape), pol_prev=np.zeros(nshape), contrib=np.zeros(nshape))
+    ref = of.gpe_step(ref_field["phi"], s["charges"], s["positions"], s["types"], T, cfg.mesh(),
+                      cfg.box(), cfg.sigma, cfg.dielectric_type, [0.0] * T, state,
+                      conv_crit=cfg.conv_crit, mixing=cfg.pol_mixing, conv_kind="max_diff")
+    torch.cuda.synchronize()
+    assert pm.gpe_iterations == ref["iterations"]
+    assert rel_rms(F.cpu().numpy(), ref["forces"]) < FORCE_RTOL
+    assert W == pytest.approx(ref["energy"], rel=1e-5)
+    pm.check_errors()
