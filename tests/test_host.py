@@ -248,3 +248,22 @@ def test_adjoint_functional_coefficients_match_oracle():
         ref = oh.quadratic_from_params(kind, T, 0.05, 8.3, 8.0, chi)
         assert np.allclose(Q, ref.Q, rtol=1e-14) and np.allclose(b, ref.b, rtol=1e-14)
         assert c == pytest.approx(ref.c, rel=1e-14)
+
+
+def test_ctypes_signatures_match_header_parameter_counts():
+    """Every ctypes binding in _lib._SIGNATURES has as many parameters as its
+    declaration in include/hpf_gb300.h (a binding that drifts from the
+    header would pass the wrong arguments without any other symptom)."""
+    import re
+    from hymd_gb300 import _lib
+    txt = open(_lib.HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    decls = {}
+    for m in re.finditer(r"^(?:int|int64_t|const char\*)\s+(hpf_\w+)\s*\(([^;]*?)\)\s*;", txt,
+                         re.M | re.S):
+        params = m.group(2).strip()
+        n = 0 if params in ("", "void") else len(params.split(","))
+        decls[m.group(1)] = n
+    assert set(_lib._SIGNATURES) <= set(decls)
+    bad = {k: (len(v), decls[k]) for k, v in _lib._SIGNATURES.items() if len(v) != decls[k]}
+    assert not bad, bad
